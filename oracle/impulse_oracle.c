@@ -1,0 +1,821 @@
+/*
+ * impulse_oracle.c -- CPU oracle for the impulse FFT path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker that the GPU engine is
+ * compared against; it is linked only by the test-suite, by the smoke check
+ * and by the CPU-baseline leg of the benchmark.  The product (libimpulse_gpu)
+ * never links or calls it.
+ *
+ * It is an independent FP64 restatement of the algorithms behind impulse's
+ * FFT path (PocketFFT as vendored by impulse, plus impulse's Nim glue):
+ *
+ *   - plan heuristics: largest prime factor, cost guess, good size and the
+ *     FFTPACK-vs-Bluestein rule
+ *       (impulse/fft/c_pocketfft/pocketfft.c:205-260, 2066-2153);
+ *   - mixed-radix complex FFT (the reference runs FFTPACK passes,
+ *     pocketfft.c:300-929; this oracle runs a Stockham autosort formulation
+ *     of the same factorisation, with radix-2/3/4/5 butterflies and a direct
+ *     generic-radix DFT for every other prime factor);
+ *   - accurate twiddles exp(-2 pi i t/n) with exact integer octant reduction
+ *       (pocketfft.c:62-203 computes the same table by a different method);
+ *   - Bluestein for lengths with a large prime factor: chirp exp(i pi m^2/n)
+ *     with m^2 mod 2n kept as an exact integer, zero padded to
+ *     n2 = good_size(2n-1)  (pocketfft.c:1880-2008);
+ *   - real transforms in FFTPACK "halfcomplex" order
+ *     [r0, r1, i1, r2, i2, ..., (r_{n/2})]  (pocketfft.c:1701-1766,
+ *     impulse/fft/c_pocketfft/pocketfft.nim:216-288);
+ *   - the N-d strided drivers of the C++ backend: c2c over several axes with
+ *     the scale factor applied on the first axis only, r2c on the last axis
+ *     followed by c2c on the others, c2r as c2c into a contiguous temporary
+ *     followed by c2r on the last axis, byte strides
+ *       (impulse/fft/cpp_pocketfft/pocketfft_hdronly.h:3012-3050,
+ *        3125-3250, 3272-3390);
+ *   - impulse's Nim glue: unpackFFT, symmetrize, symmTargetSize,
+ *     initNormalize  (impulse/fft/c_pocketfft/pocketfft.nim:126-204).
+ *
+ * Everything is double precision.  Batched entry points run over POSIX
+ * threads so that the oracle can also serve as the timed CPU baseline.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+typedef struct { double r, i; } oc_t;
+
+/* ------------------------------------------------------------------ */
+/* plan heuristics (pocketfft.c:205-260)                               */
+/* ------------------------------------------------------------------ */
+
+size_t io_largest_prime_factor(size_t n)
+{
+    size_t res = 1;
+    while (n > 1 && (n & 1) == 0) { res = 2; n >>= 1; }
+    for (size_t x = 3; x * x <= n; x += 2)
+        while (n % x == 0) { res = x; n /= x; }
+    if (n > 1) res = n;
+    return res;
+}
+
+double io_cost_guess(size_t n)
+{
+    const double lfp = 1.1; /* penalty for factors without a dedicated pass */
+    size_t ni = n;
+    double result = 0.0;
+    while (n > 1 && (n & 1) == 0) { result += 2; n >>= 1; }
+    for (size_t x = 3; x * x <= n; x += 2)
+        while (n % x == 0) { result += (x <= 5) ? (double)x : lfp * (double)x; n /= x; }
+    if (n > 1) result += (n <= 5) ? (double)n : lfp * (double)n;
+    return result * (double)ni;
+}
+
+/* smallest 2^a 3^b 5^c 7^d 11^e >= n (pocketfft.c:245-260) */
+size_t io_good_size(size_t n)
+{
+    if (n <= 6) return n;
+    size_t best = 2 * n;
+    for (size_t f2 = 1; f2 < best; f2 *= 2)
+        for (size_t f3 = f2; f3 < best; f3 *= 3)
+            for (size_t f5 = f3; f5 < best; f5 *= 5)
+                for (size_t f7 = f5; f7 < best; f7 *= 7)
+                    for (size_t f11 = f7; f11 < best; f11 *= 11)
+                        if (f11 >= n) best = f11;
+    return best;
+}
+
+/* Bluestein decision of make_cfft_plan / make_rfft_plan (pocketfft.c:2066-2153):
+   FFTPACK when n < 50 or lpf^2 <= n; otherwise Bluestein iff
+   1.5 * 2 * cost(good_size(2n-1)) < cost(n)   (complex)
+   1.5 * 2 * cost(good_size(2n-1)) < 0.5 * cost(n)   (real). */
+int io_use_bluestein(size_t n, int real)
+{
+    if (n < 50) return 0;
+    size_t lpf = io_largest_prime_factor(n);
+    if ((double)lpf <= sqrt((double)n)) return 0;
+    double comp1 = io_cost_guess(n) * (real ? 0.5 : 1.0);
+    double comp2 = 2.0 * io_cost_guess(io_good_size(2 * n - 1)) * 1.5;
+    return comp2 < comp1;
+}
+
+/* ------------------------------------------------------------------ */
+/* twiddles                                                            */
+/* ------------------------------------------------------------------ */
+
+/* exp(+2 pi i t / n) with exact integer reduction to the first octant. */
+static void io_sincos_2pi(size_t t, size_t n, double *c, double *s)
+{
+    t %= n;
+    int neg_s = 0;
+    if (2 * t > n) { t = n - t; neg_s = 1; }              /* angle -> 2pi - angle */
+    double cc, ss;
+    /* now t/n in [0, 1/2] */
+    if (4 * t > n) {
+        /* angle = pi/2 + 2pi*(4t-n)/(4n) */
+        size_t num = 4 * t - n, den = 4 * n;
+        /* num/den in (0, 1/4] */
+        double cq, sq;
+        if (8 * num > den) { /* reflect around 1/8: 2pi*num/den = pi/2 - 2pi*(den-4num)/(4den) */
+            double a = 2.0 * M_PI * (double)(den - 4 * num) / (double)(4 * den);
+            cq = sin(a); sq = cos(a);
+        } else {
+            double a = 2.0 * M_PI * (double)num / (double)den;
+            cq = cos(a); sq = sin(a);
+        }
+        cc = -sq; ss = cq;
+    } else {
+        if (8 * t > n) {
+            double a = 2.0 * M_PI * (double)(n - 4 * t) / (double)(4 * n);
+            cc = sin(a); ss = cos(a);
+        } else {
+            double a = 2.0 * M_PI * (double)t / (double)n;
+            cc = cos(a); ss = sin(a);
+        }
+    }
+    *c = cc;
+    *s = neg_s ? -ss : ss;
+}
+
+/* ------------------------------------------------------------------ */
+/* complex plan: Stockham mixed radix or Bluestein                     */
+/* ------------------------------------------------------------------ */
+
+#define IO_MAXFCT 64
+
+typedef struct io_cplan {
+    size_t n;
+    int blue;
+    size_t nfct;
+    size_t fct[IO_MAXFCT];
+    oc_t *tw;             /* tw[t] = exp(-2 pi i t/n), t < n (Stockham plans) */
+    size_t maxr;          /* largest radix, for generic-radix scratch */
+    /* Bluestein */
+    size_t n2;
+    oc_t *bk;             /* exp(+i pi m^2/n), m < n */
+    oc_t *bkf;            /* FFT_n2 of the symmetric zero-padded bk, scaled 1/n2 */
+    struct io_cplan *sub; /* Stockham plan of length n2 */
+} io_cplan;
+
+static void io_factorize(io_cplan *p)
+{
+    /* 4s first, then a single 2 moved to the front, then odd divisors
+       (pocketfft.c:954-983). */
+    size_t n = p->n, nf = 0;
+    while (n % 4 == 0) { p->fct[nf++] = 4; n /= 4; }
+    if (n % 2 == 0) {
+        n /= 2;
+        p->fct[nf++] = 2;
+        size_t t = p->fct[0]; p->fct[0] = p->fct[nf - 1]; p->fct[nf - 1] = t;
+    }
+    for (size_t d = 3; n > 1 && d * d <= n; d += 2)
+        while (n % d == 0) { p->fct[nf++] = d; n /= d; }
+    if (n > 1) p->fct[nf++] = n;
+    p->nfct = nf;
+    p->maxr = 1;
+    for (size_t k = 0; k < nf; ++k) if (p->fct[k] > p->maxr) p->maxr = p->fct[k];
+}
+
+void io_destroy_cplan(io_cplan *p);
+
+static io_cplan *io_make_stockham(size_t n)
+{
+    io_cplan *p = (io_cplan *)calloc(1, sizeof(io_cplan));
+    if (!p) return NULL;
+    p->n = n;
+    io_factorize(p);
+    p->tw = (oc_t *)malloc(sizeof(oc_t) * (n ? n : 1));
+    if (!p->tw) { free(p); return NULL; }
+    for (size_t t = 0; t < n; ++t) {
+        double c, s;
+        io_sincos_2pi(t, n, &c, &s);
+        p->tw[t].r = c;
+        p->tw[t].i = -s;
+    }
+    return p;
+}
+
+static int io_stockham_exec(const io_cplan *p, oc_t *x, oc_t *scratch, int forward, double fct);
+
+io_cplan *io_make_cplan(size_t n)
+{
+    if (n == 0) return NULL;
+    if (!io_use_bluestein(n, 0)) return io_make_stockham(n);
+    io_cplan *p = (io_cplan *)calloc(1, sizeof(io_cplan));
+    if (!p) return NULL;
+    p->n = n;
+    p->blue = 1;
+    p->n2 = io_good_size(2 * n - 1);
+    p->sub = io_make_stockham(p->n2);
+    p->bk = (oc_t *)malloc(sizeof(oc_t) * n);
+    p->bkf = (oc_t *)calloc(p->n2, sizeof(oc_t));
+    oc_t *scr = (oc_t *)malloc(sizeof(oc_t) * p->n2);
+    if (!p->sub || !p->bk || !p->bkf || !scr) { free(scr); io_destroy_cplan(p); return NULL; }
+    /* chirp: m^2 mod 2n as an exact integer recurrence (pocketfft.c:1907-1914) */
+    size_t coeff = 0;
+    for (size_t m = 0; m < n; ++m) {
+        if (m > 0) { coeff += 2 * m - 1; if (coeff >= 2 * n) coeff -= 2 * n; }
+        double c, s;
+        io_sincos_2pi(coeff, 2 * n, &c, &s);
+        p->bk[m].r = c;
+        p->bk[m].i = s;
+    }
+    double xn2 = 1.0 / (double)p->n2;
+    p->bkf[0].r = p->bk[0].r * xn2;
+    p->bkf[0].i = p->bk[0].i * xn2;
+    for (size_t m = 1; m < n; ++m) {
+        oc_t v = { p->bk[m].r * xn2, p->bk[m].i * xn2 };
+        p->bkf[m] = v;
+        p->bkf[p->n2 - m] = v;
+    }
+    io_stockham_exec(p->sub, p->bkf, scr, 1, 1.0);
+    free(scr);
+    return p;
+}
+
+void io_destroy_cplan(io_cplan *p)
+{
+    if (!p) return;
+    free(p->tw);
+    free(p->bk);
+    free(p->bkf);
+    if (p->sub) io_destroy_cplan(p->sub);
+    free(p);
+}
+
+size_t io_cplan_n2(const io_cplan *p) { return p->blue ? p->n2 : 0; }
+size_t io_cplan_nfct(const io_cplan *p) { return p->blue ? p->sub->nfct : p->nfct; }
+size_t io_cplan_fct(const io_cplan *p, size_t k) { return p->blue ? p->sub->fct[k] : p->fct[k]; }
+
+static inline oc_t cmul(oc_t a, oc_t b) { oc_t r = { a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r }; return r; }
+static inline oc_t cmulc(oc_t a, oc_t b) { oc_t r = { a.r * b.r + a.i * b.i, a.i * b.r - a.r * b.i }; return r; } /* a*conj(b) */
+
+/* One Stockham stage of radix r: x -> y.  ns = product of the radices
+   already applied.  Butterfly j (j < n/r) reads x[j + m*n/r], twiddles
+   input m by w^(m*k) with k = j mod ns and w = exp(-+2 pi i/(ns r)), runs a
+   radix-r DFT and writes y[(j/ns)*ns*r + k + m*ns]. */
+static void io_stage(const io_cplan *p, size_t r, size_t ns, const oc_t *x, oc_t *y, int forward, oc_t *v, oc_t *w)
+{
+    const size_t n = p->n, nr = n / r, tstep = n / (ns * r);
+    const double sg = forward ? 1.0 : -1.0; /* sign of the imaginary part of the table */
+    for (size_t j = 0; j < nr; ++j) {
+        size_t k = j % ns;
+        for (size_t m = 0; m < r; ++m) {
+            oc_t a = x[j + m * nr];
+            if (m && k) {
+                oc_t t = p->tw[m * k * tstep];
+                t.i *= sg;
+                a = cmul(a, t);
+            }
+            v[m] = a;
+        }
+        /* radix-r DFT: V[q] = sum_m v[m] exp(-+2 pi i m q / r) */
+        if (r == 2) {
+            oc_t a = v[0], b = v[1];
+            v[0].r = a.r + b.r; v[0].i = a.i + b.i;
+            v[1].r = a.r - b.r; v[1].i = a.i - b.i;
+        } else if (r == 4) {
+            oc_t t0 = { v[0].r + v[2].r, v[0].i + v[2].i }, t1 = { v[0].r - v[2].r, v[0].i - v[2].i };
+            oc_t t2 = { v[1].r + v[3].r, v[1].i + v[3].i }, t3 = { v[1].r - v[3].r, v[1].i - v[3].i };
+            /* multiply t3 by -i (forward) or +i (backward) */
+            oc_t t3r = forward ? (oc_t){ t3.i, -t3.r } : (oc_t){ -t3.i, t3.r };
+            v[0].r = t0.r + t2.r; v[0].i = t0.i + t2.i;
+            v[2].r = t0.r - t2.r; v[2].i = t0.i - t2.i;
+            v[1].r = t1.r + t3r.r; v[1].i = t1.i + t3r.i;
+            v[3].r = t1.r - t3r.r; v[3].i = t1.i - t3r.i;
+        } else {
+            /* direct DFT with the plan's own table: exp(-2 pi i mq/r) = tw[(mq mod r) * n/r] */
+            for (size_t q = 0; q < r; ++q) {
+                oc_t acc = v[0];
+                for (size_t m = 1; m < r; ++m) {
+                    oc_t t = p->tw[((m * q) % r) * nr];
+                    t.i *= sg;
+                    oc_t pr = cmul(v[m], t);
+                    acc.r += pr.r; acc.i += pr.i;
+                }
+                w[q] = acc;
+            }
+            memcpy(v, w, r * sizeof(oc_t));
+        }
+        size_t base = (j / ns) * ns * r + k;
+        for (size_t m = 0; m < r; ++m) y[base + m * ns] = v[m];
+    }
+}
+
+static int io_stockham_exec(const io_cplan *p, oc_t *x, oc_t *scratch, int forward, double fct)
+{
+    size_t n = p->n;
+    if (n == 1) { x[0].r *= fct; x[0].i *= fct; return 0; }
+    oc_t *v = (oc_t *)malloc(sizeof(oc_t) * 2 * p->maxr);
+    if (!v) return -1;
+    oc_t *a = x, *b = scratch;
+    size_t ns = 1;
+    for (size_t s = 0; s < p->nfct; ++s) {
+        io_stage(p, p->fct[s], ns, a, b, forward, v, v + p->maxr);
+        ns *= p->fct[s];
+        oc_t *t = a; a = b; b = t;
+    }
+    if (a != x) {
+        for (size_t i = 0; i < n; ++i) { x[i].r = a[i].r * fct; x[i].i = a[i].i * fct; }
+    } else if (fct != 1.0) {
+        for (size_t i = 0; i < n; ++i) { x[i].r *= fct; x[i].i *= fct; }
+    }
+    free(v);
+    return 0;
+}
+
+/* Bluestein (pocketfft.c:1945-2008): premultiply by the chirp, convolve with
+   the chirp through two length-n2 FFTs, postmultiply by the chirp. */
+static int io_blue_exec(const io_cplan *p, oc_t *c, int forward, double fct)
+{
+    size_t n = p->n, n2 = p->n2;
+    oc_t *akf = (oc_t *)calloc(2 * n2, sizeof(oc_t));
+    if (!akf) return -1;
+    oc_t *scr = akf + n2;
+    for (size_t m = 0; m < n; ++m)
+        akf[m] = forward ? cmulc(c[m], p->bk[m]) : cmul(c[m], p->bk[m]);
+    io_stockham_exec(p->sub, akf, scr, 1, fct);
+    for (size_t m = 0; m < n2; ++m)
+        akf[m] = forward ? cmul(akf[m], p->bkf[m]) : cmulc(akf[m], p->bkf[m]);
+    io_stockham_exec(p->sub, akf, scr, 0, 1.0);
+    for (size_t m = 0; m < n; ++m)
+        c[m] = forward ? cmulc(akf[m], p->bk[m]) : cmul(akf[m], p->bk[m]);
+    free(akf);
+    return 0;
+}
+
+/* In-place complex transform of one line with an existing plan. */
+int io_cplan_exec(const io_cplan *p, double *c, int forward, double fct)
+{
+    if (p->blue) return io_blue_exec(p, (oc_t *)c, forward, fct);
+    oc_t *scr = (oc_t *)malloc(sizeof(oc_t) * p->n);
+    if (!scr) return -1;
+    int rc = io_stockham_exec(p, (oc_t *)c, scr, forward, fct);
+    free(scr);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* real plan: halfcomplex layout                                       */
+/* ------------------------------------------------------------------ */
+
+typedef struct io_rplan {
+    size_t n;
+    io_cplan *cp;   /* complex plan of length n/2 (even n) or n (odd n) */
+    oc_t *wn;       /* exp(-2 pi i k/n), k <= n/2 (even n) */
+} io_rplan;
+
+io_rplan *io_make_rplan(size_t n)
+{
+    if (n == 0) return NULL;
+    io_rplan *p = (io_rplan *)calloc(1, sizeof(io_rplan));
+    if (!p) return NULL;
+    p->n = n;
+    if (n == 1) return p;
+    size_t h = (n % 2 == 0) ? n / 2 : n;
+    p->cp = io_make_cplan(h);
+    if (n % 2 == 0) {
+        p->wn = (oc_t *)malloc(sizeof(oc_t) * (n / 2 + 1));
+        for (size_t k = 0; k <= n / 2; ++k) {
+            double c, s;
+            io_sincos_2pi(k, n, &c, &s);
+            p->wn[k].r = c;
+            p->wn[k].i = -s;
+        }
+    }
+    return p;
+}
+
+void io_destroy_rplan(io_rplan *p)
+{
+    if (!p) return;
+    io_destroy_cplan(p->cp);
+    free(p->wn);
+    free(p);
+}
+
+/* r2hc / hc2r in place on n doubles (pocketfft.c:2176-2190 semantics):
+   forward: halfcomplex of sum_m x[m] exp(-2 pi i m k/n), times fct;
+   backward: x[m] = fct * sum_k X[k] exp(+2 pi i m k/n) over the full
+   Hermitian spectrum described by the halfcomplex input. */
+int io_rplan_exec(const io_rplan *p, double *c, int forward, double fct)
+{
+    size_t n = p->n;
+    if (n == 1) { c[0] *= fct; return 0; }
+    if (n % 2 == 1) {
+        oc_t *z = (oc_t *)malloc(sizeof(oc_t) * n);
+        if (!z) return -1;
+        if (forward) {
+            for (size_t m = 0; m < n; ++m) { z[m].r = c[m]; z[m].i = 0.0; }
+            io_cplan_exec(p->cp, (double *)z, 1, fct);
+            c[0] = z[0].r;
+            for (size_t k = 1; 2 * k < n + 1; ++k) { c[2 * k - 1] = z[k].r; c[2 * k] = z[k].i; }
+        } else {
+            z[0].r = c[0]; z[0].i = 0.0;
+            for (size_t k = 1; 2 * k < n + 1; ++k) {
+                z[k].r = c[2 * k - 1]; z[k].i = c[2 * k];
+                z[n - k].r = c[2 * k - 1]; z[n - k].i = -c[2 * k];
+            }
+            io_cplan_exec(p->cp, (double *)z, 0, fct);
+            for (size_t m = 0; m < n; ++m) c[m] = z[m].r;
+        }
+        free(z);
+        return 0;
+    }
+    size_t h = n / 2;
+    oc_t *z = (oc_t *)malloc(sizeof(oc_t) * h);
+    if (!z) return -1;
+    if (forward) {
+        /* z[m] = x[2m] + i x[2m+1]; Z = FFT_h(z); split into X[0..h] */
+        for (size_t m = 0; m < h; ++m) { z[m].r = c[2 * m]; z[m].i = c[2 * m + 1]; }
+        io_cplan_exec(p->cp, (double *)z, 1, 1.0);
+        for (size_t k = 0; k <= h; ++k) {
+            oc_t zk = z[k % h], zm = z[(h - k) % h];
+            /* E = (zk + conj(zm))/2, O = (zk - conj(zm))/(2i) */
+            oc_t e = { 0.5 * (zk.r + zm.r), 0.5 * (zk.i - zm.i) };
+            oc_t o = { 0.5 * (zk.i + zm.i), -0.5 * (zk.r - zm.r) };
+            oc_t t = cmul(o, p->wn[k]);
+            double xr = (e.r + t.r) * fct, xi = (e.i + t.i) * fct;
+            if (k == 0) c[0] = xr;
+            else if (k == h) c[n - 1] = xr;
+            else { c[2 * k - 1] = xr; c[2 * k] = xi; }
+        }
+    } else {
+        /* X from halfcomplex; Z[k] = A + i exp(+2 pi i k/n) B,
+           A = X[k] + conj(X[h-k]), B = X[k] - conj(X[h-k]); z = IFFT_h(Z) */
+        for (size_t k = 0; k < h; ++k) {
+            oc_t xk, xm;
+            if (k == 0) { xk.r = c[0]; xk.i = 0.0; } else { xk.r = c[2 * k - 1]; xk.i = c[2 * k]; }
+            size_t q = h - k;
+            if (q == h) { xm.r = c[n - 1]; xm.i = 0.0; } else if (q == 0) { xm.r = c[0]; xm.i = 0.0; }
+            else { xm.r = c[2 * q - 1]; xm.i = c[2 * q]; }
+            oc_t a = { xk.r + xm.r, xk.i - xm.i };
+            oc_t b = { xk.r - xm.r, xk.i + xm.i };
+            oc_t wc = { p->wn[k].r, -p->wn[k].i }; /* exp(+2 pi i k/n) */
+            oc_t t = cmul(b, wc);
+            z[k].r = a.r - t.i;
+            z[k].i = a.i + t.r;
+        }
+        io_cplan_exec(p->cp, (double *)z, 0, fct);
+        for (size_t m = 0; m < h; ++m) { c[2 * m] = z[m].r; c[2 * m + 1] = z[m].i; }
+    }
+    free(z);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* pocketfft.h-shaped one-shot entry points (plan built per call, as  */
+/* impulse's C backend does: pocketfft.nim:206-214)                    */
+/* ------------------------------------------------------------------ */
+
+int io_cfft(size_t n, double *c, int forward, double fct)
+{
+    io_cplan *p = io_make_cplan(n);
+    if (!p) return -1;
+    int rc = io_cplan_exec(p, c, forward, fct);
+    io_destroy_cplan(p);
+    return rc;
+}
+
+int io_rfft(size_t n, double *c, int forward, double fct)
+{
+    io_rplan *p = io_make_rplan(n);
+    if (!p) return -1;
+    int rc = io_rplan_exec(p, c, forward, fct);
+    io_destroy_rplan(p);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* threaded batch drivers                                              */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    const void *plan;
+    int real;
+    double *base;
+    size_t batch, dist; /* dist in doubles */
+    int forward;
+    double fct;
+    size_t t, nt;
+    int rc;
+} io_batch_job;
+
+static void *io_batch_worker(void *arg)
+{
+    io_batch_job *j = (io_batch_job *)arg;
+    size_t lo = j->batch * j->t / j->nt, hi = j->batch * (j->t + 1) / j->nt;
+    for (size_t b = lo; b < hi; ++b) {
+        double *line = j->base + b * j->dist;
+        int rc = j->real ? io_rplan_exec((const io_rplan *)j->plan, line, j->forward, j->fct)
+                         : io_cplan_exec((const io_cplan *)j->plan, line, j->forward, j->fct);
+        if (rc) j->rc = rc;
+    }
+    return NULL;
+}
+
+static int io_run_batch(const void *plan, int real, double *c, size_t batch, size_t dist, int forward, double fct, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if ((size_t)nthreads > batch) nthreads = (int)(batch ? batch : 1);
+    io_batch_job *jobs = (io_batch_job *)calloc((size_t)nthreads, sizeof(io_batch_job));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!jobs || !th) { free(jobs); free(th); return -1; }
+    for (int t = 0; t < nthreads; ++t) {
+        io_batch_job v = { plan, real, c, batch, dist, forward, fct, (size_t)t, (size_t)nthreads, 0 };
+        jobs[t] = v;
+    }
+    for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, io_batch_worker, &jobs[t]);
+    io_batch_worker(&jobs[0]);
+    int rc = jobs[0].rc;
+    for (int t = 1; t < nthreads; ++t) { pthread_join(th[t], NULL); if (jobs[t].rc) rc = jobs[t].rc; }
+    free(jobs);
+    free(th);
+    return rc;
+}
+
+/* batch lines of n complex numbers, line b at c + 2*b*dist doubles */
+int io_cfft_batch(size_t n, size_t batch, double *c, size_t dist, int forward, double fct, int nthreads)
+{
+    io_cplan *p = io_make_cplan(n);
+    if (!p) return -1;
+    int rc = io_run_batch(p, 0, c, batch, 2 * dist, forward, fct, nthreads);
+    io_destroy_cplan(p);
+    return rc;
+}
+
+/* batch lines of n reals (halfcomplex in place), line b at c + b*dist doubles */
+int io_rfft_batch(size_t n, size_t batch, double *c, size_t dist, int forward, double fct, int nthreads)
+{
+    io_rplan *p = io_make_rplan(n);
+    if (!p) return -1;
+    int rc = io_run_batch(p, 1, c, batch, dist, forward, fct, nthreads);
+    io_destroy_rplan(p);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* N-d strided drivers (pocketfft_hdronly.h:3012-3050, 3125-3390)       */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    size_t ndim;
+    const size_t *shape;
+    const ptrdiff_t *sin, *sout; /* byte strides */
+    size_t axis;
+    size_t nlines;
+} io_lines;
+
+/* byte offsets (in, out) of line number l along `axis` */
+static void io_line_offsets(const io_lines *L, size_t l, ptrdiff_t *oi, ptrdiff_t *oo)
+{
+    ptrdiff_t a = 0, b = 0;
+    for (size_t d = L->ndim; d-- > 0;) {
+        if (d == L->axis) continue;
+        size_t idx = l % L->shape[d];
+        l /= L->shape[d];
+        a += (ptrdiff_t)idx * L->sin[d];
+        b += (ptrdiff_t)idx * L->sout[d];
+    }
+    *oi = a;
+    *oo = b;
+}
+
+/* kind: 0 c2c, 1 r2c (real in -> n/2+1 complex out), 2 c2r (n/2+1 complex in -> real out)
+   `len` is the logical transform length (real length for r2c/c2r). */
+typedef struct {
+    io_lines L;
+    int kind;
+    size_t len;
+    const char *in;
+    char *out;
+    int forward;
+    double fct;
+    const void *plan;
+    size_t t, nt;
+    int rc;
+} io_nd_job;
+
+static void *io_nd_worker(void *arg)
+{
+    io_nd_job *j = (io_nd_job *)arg;
+    const size_t len = j->len, ax = j->L.axis;
+    const ptrdiff_t si = j->L.sin[ax], so = j->L.sout[ax];
+    double *buf = (double *)malloc(sizeof(double) * 2 * (len + 1));
+    if (!buf) { j->rc = -1; return NULL; }
+    size_t lo = j->L.nlines * j->t / j->nt, hi = j->L.nlines * (j->t + 1) / j->nt;
+    for (size_t l = lo; l < hi; ++l) {
+        ptrdiff_t oi, oo;
+        io_line_offsets(&j->L, l, &oi, &oo);
+        const char *pi = j->in + oi;
+        char *po = j->out + oo;
+        if (j->kind == 0) {
+            for (size_t m = 0; m < len; ++m) {
+                const double *s = (const double *)(pi + (ptrdiff_t)m * si);
+                buf[2 * m] = s[0]; buf[2 * m + 1] = s[1];
+            }
+            if (io_cplan_exec((const io_cplan *)j->plan, buf, j->forward, j->fct)) j->rc = -1;
+            for (size_t m = 0; m < len; ++m) {
+                double *d = (double *)(po + (ptrdiff_t)m * so);
+                d[0] = buf[2 * m]; d[1] = buf[2 * m + 1];
+            }
+        } else if (j->kind == 1) {
+            /* general_r2c: always the forward r2hc, conjugate when !forward */
+            for (size_t m = 0; m < len; ++m) buf[m] = *(const double *)(pi + (ptrdiff_t)m * si);
+            if (io_rplan_exec((const io_rplan *)j->plan, buf, 1, j->fct)) j->rc = -1;
+            double sg = j->forward ? 1.0 : -1.0;
+            double *d = (double *)po;
+            d[0] = buf[0]; d[1] = 0.0;
+            size_t i = 1, ii = 1;
+            for (; i + 1 < len; i += 2, ++ii) {
+                d = (double *)(po + (ptrdiff_t)ii * so);
+                d[0] = buf[i]; d[1] = sg * buf[i + 1];
+            }
+            if (i < len) { d = (double *)(po + (ptrdiff_t)ii * so); d[0] = buf[i]; d[1] = 0.0; }
+        } else {
+            /* general_c2r: halfcomplex from the input (conjugated when forward), then hc2r */
+            double sg = j->forward ? -1.0 : 1.0;
+            buf[0] = ((const double *)pi)[0];
+            size_t i = 1, ii = 1;
+            for (; i + 1 < len; i += 2, ++ii) {
+                const double *s = (const double *)(pi + (ptrdiff_t)ii * si);
+                buf[i] = s[0]; buf[i + 1] = sg * s[1];
+            }
+            if (i < len) buf[i] = ((const double *)(pi + (ptrdiff_t)ii * si))[0];
+            if (io_rplan_exec((const io_rplan *)j->plan, buf, 0, j->fct)) j->rc = -1;
+            for (size_t m = 0; m < len; ++m) *(double *)(po + (ptrdiff_t)m * so) = buf[m];
+        }
+    }
+    free(buf);
+    return NULL;
+}
+
+static int io_run_axis(int kind, size_t ndim, const size_t *shape_lines, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                       size_t axis, size_t len, const void *in, void *out, int forward, double fct, int nthreads)
+{
+    size_t nlines = 1;
+    for (size_t d = 0; d < ndim; ++d) if (d != axis) nlines *= shape_lines[d];
+    const void *plan = (kind == 0) ? (const void *)io_make_cplan(len) : (const void *)io_make_rplan(len);
+    if (!plan) return -1;
+    if (nthreads < 1) nthreads = 1;
+    if ((size_t)nthreads > nlines) nthreads = (int)(nlines ? nlines : 1);
+    io_nd_job *jobs = (io_nd_job *)calloc((size_t)nthreads, sizeof(io_nd_job));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    int rc = 0;
+    if (!jobs || !th) rc = -1;
+    else {
+        for (int t = 0; t < nthreads; ++t) {
+            io_nd_job v;
+            memset(&v, 0, sizeof v);
+            v.L.ndim = ndim; v.L.shape = shape_lines; v.L.sin = sin; v.L.sout = sout; v.L.axis = axis; v.L.nlines = nlines;
+            v.kind = kind; v.len = len; v.in = (const char *)in; v.out = (char *)out;
+            v.forward = forward; v.fct = fct; v.plan = plan; v.t = (size_t)t; v.nt = (size_t)nthreads;
+            jobs[t] = v;
+        }
+        for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, io_nd_worker, &jobs[t]);
+        io_nd_worker(&jobs[0]);
+        rc = jobs[0].rc;
+        for (int t = 1; t < nthreads; ++t) { pthread_join(th[t], NULL); if (jobs[t].rc) rc = jobs[t].rc; }
+    }
+    free(jobs);
+    free(th);
+    if (kind == 0) io_destroy_cplan((io_cplan *)plan); else io_destroy_rplan((io_rplan *)plan);
+    return rc;
+}
+
+/* error codes shared with the product's C ABI */
+#define IO_EINVAL_AXIS   (-2)
+#define IO_EREPEAT_AXIS  (-3)
+#define IO_ESTRIDE       (-4)
+#define IO_ENDIM         (-7)
+
+static int io_check_axes(size_t ndim, size_t naxes, const size_t *axes)
+{
+    if (ndim < 1) return IO_ENDIM;
+    unsigned char seen[64] = { 0 };
+    for (size_t a = 0; a < naxes; ++a) {
+        if (axes[a] >= ndim) return IO_EINVAL_AXIS;
+        if (axes[a] < 64 && seen[axes[a]]++) return IO_EREPEAT_AXIS;
+    }
+    return 0;
+}
+
+/* pocketfft::c2c (pocketfft_hdronly.h:3272-3282): axes in order, the first
+   axis reads `in`, later axes read and write `out`, fct on the first axis. */
+int io_c2c(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+           size_t naxes, const size_t *axes, int forward, const double *in, double *out, double fct, int nthreads)
+{
+    size_t tot = 1;
+    for (size_t d = 0; d < ndim; ++d) tot *= shape[d];
+    if (ndim >= 1 && tot == 0) return 0;
+    int rc = io_check_axes(ndim, naxes, axes);
+    if (rc) return rc;
+    if (in == out) for (size_t d = 0; d < ndim; ++d) if (sin[d] != sout[d]) return IO_ESTRIDE;
+    for (size_t a = 0; a < naxes; ++a) {
+        const void *src = a == 0 ? (const void *)in : (const void *)out;
+        const ptrdiff_t *ss = a == 0 ? sin : sout;
+        rc = io_run_axis(0, ndim, shape, ss, sout, axes[a], shape[axes[a]], src, out, forward, a == 0 ? fct : 1.0, nthreads);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+/* pocketfft::r2c over axes (pocketfft_hdronly.h:3320-3350) */
+int io_r2c(size_t ndim, const size_t *shape_in, const ptrdiff_t *sin, const ptrdiff_t *sout,
+           size_t naxes, const size_t *axes, int forward, const double *in, double *out, double fct, int nthreads)
+{
+    size_t tot = 1;
+    for (size_t d = 0; d < ndim; ++d) tot *= shape_in[d];
+    if (ndim >= 1 && tot == 0) return 0;
+    int rc = io_check_axes(ndim, naxes, axes);
+    if (rc) return rc;
+    if (naxes == 0) return 0;
+    size_t last = axes[naxes - 1];
+    size_t shape_out[64];
+    for (size_t d = 0; d < ndim; ++d) shape_out[d] = shape_in[d];
+    shape_out[last] = shape_in[last] / 2 + 1;
+    /* the line iterator walks the non-transformed axes, which share the shape */
+    rc = io_run_axis(1, ndim, shape_in, sin, sout, last, shape_in[last], in, out, forward, fct, nthreads);
+    if (rc || naxes == 1) return rc;
+    return io_c2c(ndim, shape_out, sout, sout, naxes - 1, axes, forward, out, out, 1.0, nthreads);
+}
+
+/* pocketfft::c2r over axes (pocketfft_hdronly.h:3352-3390) */
+int io_c2r(size_t ndim, const size_t *shape_out, const ptrdiff_t *sin, const ptrdiff_t *sout,
+           size_t naxes, const size_t *axes, int forward, const double *in, double *out, double fct, int nthreads)
+{
+    size_t tot = 1;
+    for (size_t d = 0; d < ndim; ++d) tot *= shape_out[d];
+    if (ndim >= 1 && tot == 0) return 0;
+    int rc = io_check_axes(ndim, naxes, axes);
+    if (rc) return rc;
+    if (naxes == 0) return 0;
+    size_t last = axes[naxes - 1];
+    if (naxes == 1)
+        return io_run_axis(2, ndim, shape_out, sin, sout, last, shape_out[last], in, out, forward, fct, nthreads);
+    size_t shape_in[64];
+    for (size_t d = 0; d < ndim; ++d) shape_in[d] = shape_out[d];
+    shape_in[last] = shape_out[last] / 2 + 1;
+    size_t nval = 1;
+    for (size_t d = 0; d < ndim; ++d) nval *= shape_in[d];
+    ptrdiff_t sinter[64];
+    sinter[ndim - 1] = 16;
+    for (size_t d = ndim - 1; d-- > 0;) sinter[d] = sinter[d + 1] * (ptrdiff_t)shape_in[d + 1];
+    double *tmp = (double *)malloc(sizeof(double) * 2 * nval);
+    if (!tmp) return -1;
+    rc = io_c2c(ndim, shape_in, sin, sinter, naxes - 1, axes, forward, in, tmp, 1.0, nthreads);
+    if (!rc) rc = io_run_axis(2, ndim, shape_out, sinter, sout, last, shape_out[last], tmp, out, forward, fct, nthreads);
+    free(tmp);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* impulse's Nim glue (pocketfft.nim:126-204)                          */
+/* ------------------------------------------------------------------ */
+
+/* unpackFFT: halfcomplex of length in_len -> in_len/2+1 (even) or (in_len+1)/2 (odd) complex */
+void io_unpack_fft(const double *data, double *out, size_t in_len)
+{
+    size_t k = 0;
+    double re = data[0], im = 0.0;
+    out[0] = re; out[1] = im;
+    ++k;
+    for (size_t i = 1; i < in_len; ++i) {
+        if (i & 1) re = data[i];
+        else { im = data[i]; out[2 * k] = re; out[2 * k + 1] = im; ++k; }
+    }
+    if ((in_len & 1) == 0) { out[2 * k] = re; out[2 * k + 1] = 0.0; }
+}
+
+/* symmTargetSize (pocketfft.nim:173-180) */
+size_t io_symm_target_size_real(size_t len) { return len; }
+size_t io_symm_target_size_complex(double last_im, size_t len) { return len * 2 - (last_im == 0.0 ? 2 : 1); }
+
+/* symmetrize: mirror conj(res[i]) into res[out_len-i] for i in 1 ..< ceil(out_len/2)
+   (pocketfft.nim:160-171); `is_real` selects the unpackFFT pre-step. */
+void io_symmetrize(const double *data, int is_real, size_t in_len, double *res, size_t out_len)
+{
+    if (is_real) io_unpack_fft(data, res, in_len);
+    else memcpy(res, data, in_len * 2 * sizeof(double));
+    size_t k = out_len - 1;
+    for (size_t i = 1; i < (out_len + 1) / 2; ++i) {
+        res[2 * k] = res[2 * i];
+        res[2 * k + 1] = -res[2 * i + 1];
+        --k;
+    }
+}
+
+/* initNormalize (pocketfft.nim:199-204): kind 0 backward, 1 ortho, 2 forward, 3 custom */
+double io_init_normalize(int kind, int forward, double value, size_t length)
+{
+    switch (kind) {
+    case 0: return forward ? 1.0 : 1.0 / (double)length;
+    case 1: return 1.0 / sqrt((double)length);
+    case 2: return forward ? 1.0 / (double)length : 1.0;
+    default: return value;
+    }
+}
