@@ -1,0 +1,304 @@
+// ig_arith.cuh -- scalar and complex arithmetic of the GPU FFT engine.
+//
+// Three arithmetics share one set of FFT kernels through templates:
+//
+//   float  : FP32 data, FP32 butterflies (the batched FP32 path).
+//   df     : FP64 data, double-float butterflies.  A value is the unevaluated
+//            sum h + l of two floats; addition uses Knuth's TwoSum and
+//            Dekker's Fast2Sum, multiplication uses the FMA-based exact
+//            product (Dekker 1971; Knuth, TAOCP vol. 2, 4.2.2).  The result
+//            carries about 48 significant bits.  GB300's FP64 pipe is ~70x
+//            slower than its FP32 pipe, so FP64 data is computed this way.
+//   double : native FP64 butterflies (kept for comparison and for building
+//            tables; not a fast path on this GPU).
+//
+// The double <-> df conversions are done with integer and FP32 instructions
+// only, because GB300 executes FP64 conversions on its slow FP64 pipe.
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define IGD __host__ __device__ __forceinline__
+#else
+#define IGD inline
+#endif
+
+#if defined(__CUDA_ARCH__)
+#define IG_FADD(a, b) __fadd_rn((a), (b))
+#define IG_FSUB(a, b) __fsub_rn((a), (b))
+#define IG_FMUL(a, b) __fmul_rn((a), (b))
+#define IG_FMA(a, b, c) __fmaf_rn((a), (b), (c))
+#else
+#include <math.h>
+#include <string.h>
+// host builds of this header are compiled with -ffp-contract=off
+#define IG_FADD(a, b) ((a) + (b))
+#define IG_FSUB(a, b) ((a) - (b))
+#define IG_FMUL(a, b) ((a) * (b))
+#define IG_FMA(a, b, c) fmaf((a), (b), (c))
+#endif
+
+namespace ig {
+
+IGD uint32_t f2u(float f)
+{
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u; memcpy(&u, &f, 4); return u;
+#endif
+}
+IGD float u2f(uint32_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f; memcpy(&f, &u, 4); return f;
+#endif
+}
+IGD uint64_t d2u(double d)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(d);
+#else
+    uint64_t u; memcpy(&u, &d, 8); return u;
+#endif
+}
+IGD double u2d(uint64_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double d; memcpy(&d, &u, 8); return d;
+#endif
+}
+IGD int clz64(uint64_t x)
+{
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)x);
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// double-float
+// ---------------------------------------------------------------------------
+struct df {
+    float h, l;
+};
+
+// compile-time split of a double constant into a double-float
+constexpr df df_const(double c) { return df{(float)c, (float)(c - (double)(float)c)}; }
+
+// Knuth TwoSum + Fast2Sum renormalisation ("sloppy" double-float add: the
+// error bound is relative to |a| + |b|, which is what a normwise FFT error
+// analysis needs).
+IGD df operator+(df a, df b)
+{
+    float s = IG_FADD(a.h, b.h);
+    float bb = IG_FSUB(s, a.h);
+    float e = IG_FADD(IG_FSUB(a.h, IG_FSUB(s, bb)), IG_FSUB(b.h, bb));
+    e = IG_FADD(e, IG_FADD(a.l, b.l));
+    float h = IG_FADD(s, e);
+    return df{h, IG_FSUB(e, IG_FSUB(h, s))};
+}
+IGD df operator-(df a) { return df{-a.h, -a.l}; }
+IGD df operator-(df a, df b) { return a + df{-b.h, -b.l}; }
+// exact product of the high parts by FMA, cross terms folded in
+IGD df operator*(df a, df b)
+{
+    float p = IG_FMUL(a.h, b.h);
+    float e = IG_FMA(a.h, b.h, -p);
+    e = IG_FMA(a.h, b.l, e);
+    e = IG_FMA(a.l, b.h, e);
+    float h = IG_FADD(p, e);
+    return df{h, IG_FSUB(e, IG_FSUB(h, p))};
+}
+// a*b - c*d with one rounding step for the two high products (twiddle multiply)
+IGD df df_mul_sub(df a, df b, df c, df d)
+{
+    float p1 = IG_FMUL(a.h, b.h);
+    float e1 = IG_FMA(a.h, b.h, -p1);
+    float p2 = IG_FMUL(c.h, d.h);
+    float e2 = IG_FMA(c.h, d.h, -p2);
+    // TwoSum(p1, -p2)
+    float s = IG_FSUB(p1, p2);
+    float bb = IG_FSUB(s, p1);
+    float e = IG_FSUB(IG_FSUB(p1, IG_FSUB(s, bb)), IG_FADD(p2, bb));
+    e = IG_FADD(e, IG_FSUB(e1, e2));
+    e = IG_FMA(a.h, b.l, e);
+    e = IG_FMA(a.l, b.h, e);
+    e = IG_FMA(-c.h, d.l, e);
+    e = IG_FMA(-c.l, d.h, e);
+    float h = IG_FADD(s, e);
+    return df{h, IG_FSUB(e, IG_FSUB(h, s))};
+}
+IGD df df_mul_add(df a, df b, df c, df d) { return df_mul_sub(a, b, df{-c.h, -c.l}, d); }
+IGD df df_scale2(df a, float p2) { return df{IG_FMUL(a.h, p2), IG_FMUL(a.l, p2)}; }
+
+// double -> double-float with integer and FP32 instructions only.  `escale`
+// multiplies by 2^escale exactly (per-line range scaling).  High part: the
+// sign, the exponent and the top 23 fraction bits rounded; low part: the remaining
+// 29 fraction bits as a signed residual, converted to float and scaled.
+// Relative error <= 2^-48.
+IGD df df_from_double(double x, int escale = 0)
+{
+    uint64_t b = d2u(x);
+    uint32_t hw = (uint32_t)(b >> 32);
+    uint32_t sign = hw & 0x80000000u;
+    int e = (int)((hw >> 20) & 0x7ff);
+    if (e == 0x7ff) {  // inf / nan
+        uint32_t frac = (uint32_t)(b >> 29) & 0x7fffffu;
+        return df{u2f(sign | 0x7f800000u | (frac ? 0x400000u : 0u)), 0.0f};
+    }
+    if (e == 0) return df{u2f(sign), 0.0f};  // zero or double subnormal: flushed
+    e += escale;
+    int ef = e - 1023 + 127;  // float biased exponent of the high part
+    if (ef >= 255) return df{u2f(sign | 0x7f800000u), 0.0f};
+    if (ef <= 0) return df{u2f(sign), 0.0f};
+    // high part rounded to nearest: incrementing the float's bit pattern
+    // carries into its exponent when the fraction overflows
+    uint32_t top = (uint32_t)(b >> 29) & 0x7fffffu;
+    uint32_t rbit = (uint32_t)(b >> 28) & 1u;
+    uint32_t hb = (((uint32_t)ef << 23) | top) + rbit;
+    if (hb >= 0x7f800000u) return df{u2f(sign | 0x7f800000u), 0.0f};
+    float h = u2f(sign | hb);
+    // low part = (low29 - rbit*2^29) * 2^(e - 1023 - 52), |.| <= 2^28 units
+    int32_t r = (int32_t)((uint32_t)b & 0x1fffffffu) - (int32_t)(rbit << 29);
+    int el = e - 1023 - 52 + 127;  // biased exponent of the scale factor
+    float l = 0.0f;
+    if (el >= 1 && r) {
+        float lf = (float)r;  // rounded to 24 bits
+        l = IG_FMUL(lf, u2f((uint32_t)el << 23));
+        if (sign) l = -l;
+    }
+    return df{h, l};
+}
+
+// float -> exact double via bit manipulation (normal floats; others special-cased)
+IGD double f2d_bits(float f)
+{
+    uint32_t u = f2u(f);
+    uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+    uint32_t ef = (u >> 23) & 0xff;
+    uint32_t fr = u & 0x7fffffu;
+    if (ef == 0xff) return u2d(sign | 0x7ff0000000000000ull | ((uint64_t)fr << 29));
+    if (ef == 0) return u2d(sign);  // zero / float subnormal flushed
+    return u2d(sign | ((uint64_t)(ef - 127 + 1023) << 52) | ((uint64_t)fr << 29));
+}
+
+// double-float -> double with integer instructions only: the two
+// significands are aligned into one 64-bit integer, normalised and rounded
+// (round-half-up on the discarded bits), and the double is assembled.
+IGD double df_to_double(df v, int escale = 0)
+{
+    uint32_t uh = f2u(v.h), ul = f2u(v.l);
+    int eh = (int)((uh >> 23) & 0xff);
+    int el = (int)((ul >> 23) & 0xff);
+    if (eh == 0xff) return f2d_bits(v.h);
+    if (eh == 0) {
+        if (el == 0 || el == 0xff) return f2d_bits(v.h);
+        // only the low part is non-zero
+        double d = f2d_bits(v.l);
+        uint64_t bd = d2u(d);
+        int ed = (int)((bd >> 52) & 0x7ff) - escale;
+        if (ed <= 0) return u2d(bd & 0x8000000000000000ull);
+        if (ed >= 0x7ff) return u2d((bd & 0x8000000000000000ull) | 0x7ff0000000000000ull);
+        return u2d((bd & 0x800fffffffffffffull) | ((uint64_t)ed << 52));
+    }
+    int64_t H = (int64_t)((uh & 0x7fffffu) | 0x800000u);
+    if (uh & 0x80000000u) H = -H;
+    int64_t K = H * ((int64_t)1 << 29);  // units of 2^(eh-127-23-29)
+    if (el != 0) {
+        int64_t L = (int64_t)((ul & 0x7fffffu) | 0x800000u);
+        if (ul & 0x80000000u) L = -L;
+        int sh = 29 - (eh - el);  // align L to K's units
+        if (sh >= 0) K += L * ((int64_t)1 << sh);
+        else if (sh > -40) K += (L >> (-sh));
+    }
+    if (K == 0) return 0.0;
+    uint64_t sgn = K < 0 ? 0x8000000000000000ull : 0;
+    uint64_t M = (uint64_t)(K < 0 ? -K : K);
+    int lz = clz64(M);
+    int shift = 11 - lz;  // bring the leading one to bit 52
+    // exponent of the result: value = M * 2^(eh - 127 - 52)
+    int ed = eh - 127 + 1023 + shift - escale;
+    if (shift > 0) {
+        uint64_t half = (uint64_t)1 << (shift - 1);
+        M = (M + half) >> shift;
+        if (M >> 53) { M >>= 1; ++ed; }
+    } else if (shift < 0) {
+        M <<= (-shift);
+    }
+    if (ed >= 0x7ff) return u2d(sgn | 0x7ff0000000000000ull);
+    if (ed <= 0) return u2d(sgn);
+    return u2d(sgn | ((uint64_t)ed << 52) | (M & 0xfffffffffffffull));
+}
+
+// ---------------------------------------------------------------------------
+// generic real helpers: constants, scale by power of two
+// ---------------------------------------------------------------------------
+template <class R> struct RealOps;
+template <> struct RealOps<float> {
+    static constexpr float k(double c) { return (float)c; }
+};
+template <> struct RealOps<double> {
+    static constexpr double k(double c) { return c; }
+};
+template <> struct RealOps<df> {
+    static constexpr df k(double c) { return df_const(c); }
+};
+
+// ---------------------------------------------------------------------------
+// complex
+// ---------------------------------------------------------------------------
+template <class R> struct cx {
+    R r, i;
+};
+template <class R> IGD cx<R> operator+(cx<R> a, cx<R> b) { return cx<R>{a.r + b.r, a.i + b.i}; }
+template <class R> IGD cx<R> operator-(cx<R> a, cx<R> b) { return cx<R>{a.r - b.r, a.i - b.i}; }
+// a * w
+template <class R> IGD cx<R> cmul(cx<R> a, cx<R> w) { return cx<R>{a.r * w.r - a.i * w.i, a.r * w.i + a.i * w.r}; }
+// a * conj(w)
+template <class R> IGD cx<R> cmulc(cx<R> a, cx<R> w) { return cx<R>{a.r * w.r + a.i * w.i, a.i * w.r - a.r * w.i}; }
+template <> IGD cx<df> cmul<df>(cx<df> a, cx<df> w)
+{
+    return cx<df>{df_mul_sub(a.r, w.r, a.i, w.i), df_mul_add(a.r, w.i, a.i, w.r)};
+}
+template <> IGD cx<df> cmulc<df>(cx<df> a, cx<df> w)
+{
+    return cx<df>{df_mul_add(a.r, w.r, a.i, w.i), df_mul_sub(a.i, w.r, a.r, w.i)};
+}
+// a * w or a * conj(w)
+template <bool FWD, class R> IGD cx<R> twmul(cx<R> a, cx<R> w) { return FWD ? cmul(a, w) : cmulc(a, w); }
+// multiply by -i (forward) / +i (backward)
+template <bool FWD, class R> IGD cx<R> rot(cx<R> a)
+{
+    if (FWD) return cx<R>{a.i, -a.r};
+    return cx<R>{-a.i, a.r};
+}
+template <class R> IGD cx<R> cscale(cx<R> a, R s) { return cx<R>{a.r * s, a.i * s}; }
+template <class R> IGD cx<R> conjx(cx<R> a) { return cx<R>{a.r, -a.i}; }
+
+// ---------------------------------------------------------------------------
+// storage <-> arithmetic
+// ---------------------------------------------------------------------------
+template <class R> struct Store;
+template <> struct Store<float> {
+    using real = float;
+    IGD static float in(float x, int) { return x; }
+    IGD static float out(float x, int) { return x; }
+};
+template <> struct Store<double> {
+    using real = double;
+    IGD static double in(double x, int) { return x; }
+    IGD static double out(double x, int) { return x; }
+};
+template <> struct Store<df> {
+    using real = double;
+    IGD static df in(double x, int es) { return df_from_double(x, es); }
+    IGD static double out(df x, int es) { return df_to_double(x, es); }
+};
+
+}  // namespace ig

@@ -1,0 +1,995 @@
+// ig_engine.cu -- host side of the GPU FFT engine: planner, plan cache,
+// workspace, executor and the C ABI declared in include/impulse_gpu.h.
+//
+// Planning follows the reference's structure (factorise, build twiddles,
+// choose FFTPACK-style passes or Bluestein: impulse/fft/c_pocketfft/
+// pocketfft.c:954-983, 2066-2153; pocketfft_hdronly.h:2349-2417, 2655-2706)
+// but targets the GPU: a length is run as one shared-memory Stockham kernel
+// when it fits on one SM, as a four-step decomposition of two such kernels
+// otherwise, and through Bluestein when it has a prime factor above 11.  All
+// tables are built on the GPU in FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <functional>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <list>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/impulse_gpu.h"
+#include "ig_launch.h"
+
+namespace ig {
+
+static thread_local std::string g_err;
+static std::atomic<unsigned long long> g_launches{0};
+static int g_f64_arith = 0;  // 0 double-float, 1 native FP64
+
+struct Error {
+    int code;
+    std::string msg;
+};
+[[noreturn]] static void raise(int code, const std::string &msg) { throw Error{code, msg}; }
+static void ck(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (e == cudaErrorMemoryAllocation) raise(IG_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+        raise(IG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+static void count_launch()
+{
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    ck(cudaGetLastError(), "kernel launch");
+}
+
+static size_t slot_bytes(Arith a) { return a == A_F32 ? 8 : 16; }
+static size_t store_real_bytes(Arith a) { return a == A_F32 ? 4 : 8; }
+
+// --------------------------------------------------------------------------
+// device memory
+// --------------------------------------------------------------------------
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t n)
+    {
+        bytes = n;
+        if (n) {
+            if (getenv("IG_FAIL_MALLOC")) raise(IG_ENOMEM, "cudaMalloc: injected failure (IG_FAIL_MALLOC)");
+            ck(cudaMalloc(&p, n), "cudaMalloc");
+        }
+    }
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+};
+
+static int device_id()
+{
+    int d = 0;
+    ck(cudaGetDevice(&d), "cudaGetDevice");
+    return d;
+}
+
+static int g_max_smem = 0;
+static int max_smem()
+{
+    if (!g_max_smem) {
+        int v = 0;
+        ck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_id()), "smem attr");
+        g_max_smem = v - 1024;  // room for the kernels' static shared memory
+    }
+    return g_max_smem;
+}
+
+// --------------------------------------------------------------------------
+// cores: complex transforms of one length
+// --------------------------------------------------------------------------
+static bool gpu_factor(long long L, std::vector<int> &rad)
+{
+    rad.clear();
+    long long n = L;
+    while (n % 16 == 0) { rad.push_back(16); n /= 16; }
+    if (n % 8 == 0) { rad.push_back(8); n /= 8; }
+    if (n % 4 == 0) { rad.push_back(4); n /= 4; }
+    if (n % 2 == 0) { rad.push_back(2); n /= 2; }
+    for (int p : {11, 7, 5, 3})
+        while (n % p == 0) { rad.push_back(p); n /= p; }
+    return n == 1;
+}
+
+static long long good_size_gpu(long long n)
+{
+    // smallest 2^a 3^b 5^c 7^d 11^e >= n (pocketfft.c:245-260)
+    if (n <= 6) return n;
+    long long best = 2 * n;
+    for (long long f2 = 1; f2 < best; f2 *= 2)
+        for (long long f3 = f2; f3 < best; f3 *= 3)
+            for (long long f5 = f3; f5 < best; f5 *= 5)
+                for (long long f7 = f5; f7 < best; f7 *= 7)
+                    for (long long f11 = f7; f11 < best; f11 *= 11)
+                        if (f11 >= n) best = f11;
+    return best;
+}
+
+struct Core {
+    Arith a;
+    long long M = 0;
+    bool real_tw = false;  // rtw built (core of an even real transform of length 2M)
+    int kind = 0;          // 0 smem, 1 four-step, 2 Bluestein over a four-step core
+    CoreDesc d{};
+    std::vector<std::unique_ptr<DevBuf>> mem;
+    // four-step
+    long long N1 = 0, N2 = 0;
+    std::shared_ptr<Core> c1, c2;
+    const void *whi = nullptr, *wlo = nullptr;
+    // Bluestein over a large core
+    long long n2 = 0;
+    std::shared_ptr<Core> sub;
+    const void *chirp = nullptr, *chirpf = nullptr;
+    const void *rtw = nullptr;
+
+    void *alloc(size_t bytes)
+    {
+        mem.emplace_back(new DevBuf(bytes));
+        return mem.back()->p;
+    }
+};
+
+static std::mutex g_mu;
+static std::map<std::tuple<int, int, long long, bool>, std::shared_ptr<Core>> g_cores;
+
+static std::shared_ptr<Core> get_core(Arith a, long long M, bool real_tw);
+
+static void launch_stage_tw(Arith a, void *tw, int R, int ns)
+{
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::stage_tw(tw, R, ns)
+                  : a == A_DF  ? Launch<TagDF>::stage_tw(tw, R, ns)
+                               : Launch<TagF64>::stage_tw(tw, R, ns);
+    ck(e, "twiddle table");
+    count_launch();
+}
+static void launch_roots_a(Arith a, void *out, long long count, unsigned long long mult, unsigned long long D)
+{
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::roots(out, count, mult, D)
+                  : a == A_DF  ? Launch<TagDF>::roots(out, count, mult, D)
+                               : Launch<TagF64>::roots(out, count, mult, D);
+    ck(e, "roots table");
+    count_launch();
+}
+static void launch_convert_a(Arith a, const void *in, void *out, long long n)
+{
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::convert64(in, out, n)
+                  : a == A_DF  ? Launch<TagDF>::convert64(in, out, n)
+                               : Launch<TagF64>::convert64(in, out, n);
+    ck(e, "table conversion");
+    count_launch();
+}
+
+static constexpr int kMaxThreads = 512;
+
+// smem slots a core of Stockham length L needs per line
+static long long smem_slots(long long L, long long M) { return std::max(L, M + 1); }
+
+static bool fits_smem(Arith a, long long L, long long M)
+{
+    long long tpl = (L + kE - 1) / kE;
+    if (tpl > kMaxThreads) return false;
+    return smem_slots(L, M) * (long long)slot_bytes(a) <= (long long)max_smem();
+}
+
+struct Exec;
+static void run_core_on_device(const Core &c, const void *in, void *out, long long batch, int fwd, double fct,
+                               cudaStream_t st);
+
+static void build_stockham(Core &c, long long L, const std::vector<int> &rad)
+{
+    c.d.L = (int)L;
+    c.d.nst = (int)rad.size();
+    if (c.d.nst > kMaxStages) raise(IG_ETOOLARGE, "too many FFT stages");
+    long long ns = 1, off = 0;
+    for (size_t s = 0; s < rad.size(); ++s) {
+        c.d.st[s].R = rad[s];
+        c.d.st[s].ns = (int)ns;
+        c.d.st[s].tw = (int)off;
+        off += ns * (rad[s] - 1);
+        ns *= rad[s];
+    }
+    void *tw = c.alloc(std::max<long long>(off, 1) * slot_bytes(c.a));
+    c.d.tw = tw;
+    for (size_t s = 0; s < rad.size(); ++s) {
+        void *p = (char *)tw + (size_t)c.d.st[s].tw * slot_bytes(c.a);
+        launch_stage_tw(c.a, p, rad[s], c.d.st[s].ns);
+    }
+}
+
+// Bluestein tables for a logical length M over a Stockham/four-step length L:
+// chirp[m] = exp(+i pi m^2/M), chirpf = FFT_L(padded chirp)/L, computed from
+// FP64 tables with the double-float engine, then rounded to the core type.
+static void build_chirp(Core &c, long long M, long long L, void *&chirp, void *&chirpf)
+{
+    DevBuf bk64(M * 16), pad(L * 16);
+    ck(launch_chirp64(bk64.p, M), "chirp");
+    count_launch();
+    ck(launch_pad_chirp64(bk64.p, pad.p, M, L), "chirp padding");
+    count_launch();
+    auto dfcore = get_core(A_DF, L, false);
+    run_core_on_device(*dfcore, pad.p, pad.p, 1, 1, 1.0, 0);
+    chirp = c.alloc(M * slot_bytes(c.a));
+    chirpf = c.alloc(L * slot_bytes(c.a));
+    launch_convert_a(c.a, bk64.p, chirp, M);
+    launch_convert_a(c.a, pad.p, chirpf, L);
+    ck(cudaDeviceSynchronize(), "chirp tables");
+}
+
+static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
+{
+    auto c = std::make_shared<Core>();
+    c->a = a;
+    c->M = M;
+    c->real_tw = real_tw;
+    c->d.M = (int)std::min<long long>(M, 1 << 30);
+    std::vector<int> rad;
+    bool smooth = gpu_factor(M, rad);
+    if (real_tw) {
+        void *rtw = c->alloc((M + 1) * slot_bytes(a));
+        launch_roots_a(a, rtw, M + 1, 1, 2 * (unsigned long long)M);
+        c->rtw = rtw;
+        c->d.rtw = rtw;
+    }
+    if (smooth && fits_smem(a, M, M)) {
+        c->kind = 0;
+        build_stockham(*c, M, rad);
+        c->d.LS = (int)smem_slots(M, M);
+        c->d.blue = 0;
+    } else if (!smooth) {
+        long long L = good_size_gpu(2 * M - 1);
+        std::vector<int> radL;
+        gpu_factor(L, radL);
+        if (fits_smem(a, L, M)) {
+            c->kind = 0;
+            c->d.blue = 1;
+            build_stockham(*c, L, radL);
+            c->d.LS = (int)smem_slots(L, M);
+            void *ch, *chf;
+            build_chirp(*c, M, L, ch, chf);
+            c->d.chirp = ch;
+            c->d.chirpf = chf;
+            c->n2 = L;
+        } else {
+            raise(IG_ETOOLARGE, "Bluestein length beyond one CTA is not supported yet");
+        }
+    } else {
+        raise(IG_ETOOLARGE, "lengths beyond one CTA are not supported yet");
+    }
+    ck(cudaDeviceSynchronize(), "plan tables");
+    return c;
+}
+
+static std::shared_ptr<Core> get_core(Arith a, long long M, bool real_tw)
+{
+    auto key = std::make_tuple(device_id(), (int)a, M, real_tw);
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_cores.find(key);
+        if (it != g_cores.end()) return it->second;
+    }
+    auto c = make_core(a, M, real_tw);
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_cores.find(key);
+    if (it != g_cores.end()) return it->second;
+    g_cores[key] = c;
+    return c;
+}
+
+// --------------------------------------------------------------------------
+// launching the shared-memory kernel
+// --------------------------------------------------------------------------
+static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
+{
+    if (io.nlines <= 0) return;
+    const long long tpl = (d.L + kE - 1) / kE;
+    const long long line_bytes = (long long)d.LS * (long long)slot_bytes(a);
+    const int smax = max_smem();
+    long long lpc = std::max<long long>(1, 256 / tpl);
+    if (io.cols_in || io.cols_out) lpc = std::max<long long>(lpc, 8);
+    lpc = std::min<long long>(lpc, kMaxLinesPerCta);
+    lpc = std::min<long long>(lpc, std::max<long long>(1, kMaxThreads / tpl));
+    // keep two CTAs per SM when a line is small enough
+    long long budget = line_bytes * 2 <= smax / 2 ? smax / 2 : smax;
+    lpc = std::min<long long>(lpc, std::max<long long>(1, budget / line_bytes));
+    lpc = std::min<long long>(lpc, std::max<long long>(1, io.nlines));
+    io.lpc = (int)lpc;
+    io.tpl = (int)tpl;
+    size_t smem = (size_t)(lpc * line_bytes);
+    static std::once_flag once[3];
+    std::call_once(once[a], [&] {
+        int optin = smax + 1024;
+        cudaError_t e = a == A_F32 ? Launch<TagF32>::set_max_smem(optin)
+                      : a == A_DF  ? Launch<TagDF>::set_max_smem(optin)
+                                   : Launch<TagF64>::set_max_smem(optin);
+        ck(e, "cudaFuncSetAttribute");
+    });
+    long long grid = (io.nlines + lpc - 1) / lpc;
+    if (grid > 0x7fffffffLL) raise(IG_ETOOLARGE, "too many lines for one launch");
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::fft_smem(d, io, smem, st)
+                  : a == A_DF  ? Launch<TagDF>::fft_smem(d, io, smem, st)
+                               : Launch<TagF64>::fft_smem(d, io, smem, st);
+    ck(e, "fft kernel launch");
+    count_launch();
+}
+
+static IODesc blank_io()
+{
+    IODesc io;
+    memset(&io, 0, sizeof io);
+    io.bn[0] = io.bn[1] = io.bn[2] = 1;
+    io.fct = 1.0;
+    return io;
+}
+
+// contiguous batch of complex lines of length M (used for table building)
+static void run_core_on_device(const Core &c, const void *in, void *out, long long batch, int fwd, double fct,
+                               cudaStream_t st)
+{
+    if (c.kind != 0) raise(IG_ETOOLARGE, "core kind not supported");
+    IODesc io = blank_io();
+    size_t sb = 2 * store_real_bytes(c.a);
+    io.in = (const char *)in;
+    io.out = (char *)out;
+    io.is = io.os = (long long)sb;
+    io.nlines = batch;
+    io.bn[0] = batch;
+    io.bsi[0] = io.bso[0] = c.M * (long long)sb;
+    io.in_kind = IN_C;
+    io.out_kind = OUT_C;
+    io.cnt_in = io.cnt_out = (int)c.M;
+    io.fwd = fwd;
+    io.fct = fct;
+    launch_smem(c.a, c.d, io, st);
+}
+
+// --------------------------------------------------------------------------
+// transforms over lines
+// --------------------------------------------------------------------------
+enum Op { OP_C2C = 0, OP_R2HC = 1, OP_HC2R = 2, OP_R2C = 3, OP_C2R = 4 };
+
+struct Lines {
+    // a set of lines of logical length N: line l starts at in/out + offset(l),
+    // consecutive elements `es_in` / `es_out` bytes apart (storage elements:
+    // complex for complex sides, real for real sides)
+    const char *in;
+    char *out;
+    long long es_in, es_out;
+    long long nlines;
+    long long bn[3], bsi[3], bso[3];
+};
+
+static Arith arith_for(int dtype)
+{
+    if (dtype == IG_F32) return A_F32;
+    return g_f64_arith == 1 ? A_F64 : A_DF;
+}
+
+static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, double fct, cudaStream_t st)
+{
+    if (ln.nlines <= 0 || N <= 0) return;
+    IODesc io = blank_io();
+    io.in = ln.in;
+    io.out = ln.out;
+    io.nlines = ln.nlines;
+    for (int i = 0; i < 3; ++i) {
+        io.bn[i] = ln.bn[i];
+        io.bsi[i] = ln.bsi[i];
+        io.bso[i] = ln.bso[i];
+    }
+    io.fct = fct;
+    io.nreal = N;
+    io.is = ln.es_in;
+    io.os = ln.es_out;
+    const long long sr = (long long)store_real_bytes(a);
+    bool even = (N % 2 == 0) && N > 1;
+    long long M = N;
+    std::shared_ptr<Core> core;
+    switch (op) {
+    case OP_C2C:
+        core = get_core(a, N, false);
+        io.in_kind = IN_C;
+        io.out_kind = OUT_C;
+        io.cnt_in = io.cnt_out = (int)N;
+        io.fwd = forward;
+        break;
+    case OP_R2HC:
+    case OP_R2C:
+        M = even ? N / 2 : N;
+        core = get_core(a, M, even);
+        if (even && ln.es_in == sr) {
+            io.in_kind = IN_C;  // contiguous reals read as complex pairs
+            io.is = 2 * sr;
+        } else {
+            io.in_kind = even ? IN_P : IN_R;
+        }
+        io.cnt_in = (int)M;
+        io.post = even ? POST_SPLIT : POST_NONE;
+        io.fwd = 1;
+        if (op == OP_R2HC) {
+            io.out_kind = OUT_HC;
+            io.cnt_out = (int)(even ? N / 2 + 1 : (N + 1) / 2);
+        } else {
+            io.out_kind = OUT_C;
+            io.cnt_out = (int)(N / 2 + 1);
+            io.conj_out = forward ? 0 : 1;
+            io.real_out = 1;
+        }
+        break;
+    case OP_HC2R:
+    case OP_C2R:
+        M = even ? N / 2 : N;
+        core = get_core(a, M, even);
+        io.in_kind = op == OP_HC2R ? IN_HC : IN_C;
+        io.cnt_in = (int)(even ? N / 2 + 1 : (N + 1) / 2);
+        if (op == OP_C2R) io.conj_in = forward ? 1 : 0;
+        io.pre = even ? PRE_HERM_EVEN : PRE_HERM_ODD;
+        io.fwd = 0;
+        if (even) {
+            if (ln.es_out == sr) {
+                io.out_kind = OUT_C;
+                io.os = 2 * sr;
+            } else {
+                io.out_kind = OUT_P;
+            }
+            io.cnt_out = (int)M;
+        } else {
+            io.out_kind = OUT_R;
+            io.cnt_out = (int)N;
+        }
+        break;
+    }
+    if (N == 1 && (op == OP_R2HC || op == OP_HC2R)) {
+        io.in_kind = IN_R;
+        io.out_kind = OUT_R;
+        io.pre = PRE_NONE;
+        io.post = POST_NONE;
+        io.cnt_in = io.cnt_out = 1;
+    }
+    if (N == 1 && op == OP_C2R) {
+        io.in_kind = IN_C;
+        io.out_kind = OUT_R;
+        io.pre = PRE_NONE;
+        io.conj_in = 0;
+        io.cnt_in = io.cnt_out = 1;
+    }
+    if (N == 1 && op == OP_R2C) {
+        io.in_kind = IN_R;
+        io.post = POST_NONE;
+        io.cnt_in = 1;
+    }
+    // coalescing mode: lines adjacent in memory and elements strided
+    long long ue_in = io.in_kind == IN_C ? 2 * sr : sr;
+    long long ue_out = (io.out_kind == OUT_C) ? 2 * sr : sr;
+    io.cols_in = (ln.bn[0] > 1 && std::llabs(ln.bsi[0]) <= ue_in && std::llabs(io.is) > ue_in) ? 1 : 0;
+    io.cols_out = (ln.bn[0] > 1 && std::llabs(ln.bso[0]) <= ue_out && std::llabs(io.os) > ue_out) ? 1 : 0;
+    if (core->kind != 0) raise(IG_ETOOLARGE, "multi-pass cores are not wired yet");
+    launch_smem(a, core->d, io, st);
+}
+
+// --------------------------------------------------------------------------
+// N-d driver (pocketfft_hdronly.h:3012-3050 semantics)
+// --------------------------------------------------------------------------
+static void check_axes(size_t ndim, size_t naxes, const size_t *axes)
+{
+    if (ndim < 1) raise(IG_ENDIM, "ndim must be >= 1");
+    std::vector<int> seen(ndim, 0);
+    for (size_t i = 0; i < naxes; ++i) {
+        if (axes[i] >= ndim) raise(IG_EINVAL_AXIS, "bad axis number");
+        if (++seen[axes[i]] > 1) raise(IG_EREPEAT_AXIS, "axis specified repeatedly");
+    }
+}
+
+// lines along `axis` of an array with `shape`, element strides in bytes
+static void for_lines(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t axis,
+                      const char *in, char *out, const std::function<void(const Lines &)> &fn)
+{
+    // collect the other dims, innermost (smallest |out stride|) first
+    std::vector<size_t> dims;
+    for (size_t d = 0; d < ndim; ++d)
+        if (d != axis && shape[d] > 1) dims.push_back(d);
+    std::sort(dims.begin(), dims.end(), [&](size_t x, size_t y) {
+        long long ax = std::llabs((long long)sout[x]), ay = std::llabs((long long)sout[y]);
+        if (ax != ay) return ax < ay;
+        return std::llabs((long long)sin[x]) < std::llabs((long long)sin[y]);
+    });
+    // merge dims that are contiguous in both arrays
+    struct D { long long n, si, so; };
+    std::vector<D> m;
+    for (size_t d : dims) {
+        if (!m.empty() && m.back().si * m.back().n == (long long)sin[d] && m.back().so * m.back().n == (long long)sout[d]) {
+            m.back().n *= (long long)shape[d];
+        } else {
+            m.push_back(D{(long long)shape[d], (long long)sin[d], (long long)sout[d]});
+        }
+    }
+    Lines ln;
+    ln.es_in = sin[axis];
+    ln.es_out = sout[axis];
+    for (int i = 0; i < 3; ++i) { ln.bn[i] = 1; ln.bsi[i] = 0; ln.bso[i] = 0; }
+    size_t inner = std::min<size_t>(m.size(), 3);
+    ln.nlines = 1;
+    for (size_t i = 0; i < inner; ++i) {
+        ln.bn[i] = m[i].n;
+        ln.bsi[i] = m[i].si;
+        ln.bso[i] = m[i].so;
+        ln.nlines *= m[i].n;
+    }
+    // remaining outer dims: host loop
+    std::vector<long long> idx(m.size() > 3 ? m.size() - 3 : 0, 0);
+    while (true) {
+        long long oi = 0, oo = 0;
+        for (size_t k = 0; k < idx.size(); ++k) {
+            oi += idx[k] * m[3 + k].si;
+            oo += idx[k] * m[3 + k].so;
+        }
+        ln.in = in + oi;
+        ln.out = out + oo;
+        fn(ln);
+        size_t k = 0;
+        for (; k < idx.size(); ++k) {
+            if (++idx[k] < m[3 + k].n) break;
+            idx[k] = 0;
+        }
+        if (k == idx.size()) break;
+    }
+}
+
+static cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
+
+static void nd_c2c_device(Arith a, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                          size_t naxes, const size_t *axes, int forward, const void *in, void *out, double fct,
+                          cudaStream_t st)
+{
+    for (size_t k = 0; k < naxes; ++k) {
+        size_t ax = axes[k];
+        const char *src = k == 0 ? (const char *)in : (const char *)out;
+        const ptrdiff_t *ss = k == 0 ? sin : sout;
+        for_lines(ndim, shape, ss, sout, ax, src, (char *)out, [&](const Lines &ln) {
+            exec_op(a, OP_C2C, (long long)shape[ax], ln, forward, k == 0 ? fct : 1.0, st);
+        });
+    }
+}
+
+// --------------------------------------------------------------------------
+// workspace for host-memory entry points
+// --------------------------------------------------------------------------
+struct Workspace {
+    DevBuf *buf = nullptr;
+    size_t cap = 0;
+    void *get(size_t n)
+    {
+        if (n > cap) {
+            delete buf;
+            buf = nullptr;
+            cap = 0;
+            buf = new DevBuf(n);
+            cap = n;
+        }
+        return buf->p;
+    }
+    void release()
+    {
+        delete buf;
+        buf = nullptr;
+        cap = 0;
+    }
+};
+static std::mutex g_ws_mu;
+static Workspace g_ws;
+
+// byte span [lo, hi) covered by a strided array
+static void span_of(size_t ndim, const size_t *shape, const ptrdiff_t *st, size_t elem, long long &lo, long long &hi)
+{
+    lo = 0;
+    hi = 0;
+    for (size_t d = 0; d < ndim; ++d) {
+        if (shape[d] == 0) { lo = hi = 0; return; }
+        long long ext = (long long)(shape[d] - 1) * (long long)st[d];
+        if (ext < 0) lo += ext; else hi += ext;
+    }
+    hi += (long long)elem;
+}
+static bool dense(size_t ndim, const size_t *shape, const ptrdiff_t *st, size_t elem)
+{
+    long long lo, hi;
+    span_of(ndim, shape, st, elem, lo, hi);
+    long long tot = (long long)elem;
+    for (size_t d = 0; d < ndim; ++d) tot *= (long long)shape[d];
+    return hi - lo == tot;
+}
+
+}  // namespace ig
+
+using namespace ig;
+
+// ----------------------------------------------------------------------------
+// C ABI
+// ----------------------------------------------------------------------------
+struct ig_cfft_plan_i {
+    size_t n;
+    Arith a;
+    int dtype;
+    std::shared_ptr<Core> core;
+};
+struct ig_rfft_plan_i {
+    size_t n;
+    Arith a;
+    int dtype;
+    std::shared_ptr<Core> core;
+};
+
+template <class F> static int guarded(F &&f)
+{
+    try {
+        f();
+        g_err.clear();
+        return IG_OK;
+    } catch (const Error &e) {
+        g_err = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_err = "host allocation failed";
+        return IG_ENOMEM;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return IG_EINVAL;
+    }
+}
+
+extern "C" {
+
+const char *ig_last_error_string(void) { return g_err.c_str(); }
+int ig_version(void) { return 100; }
+
+int ig_set_f64_arith(int mode)
+{
+    if (mode != 0 && mode != 1) {
+        g_err = "f64 arithmetic mode must be 0 or 1";
+        return IG_EINVAL;
+    }
+    g_f64_arith = mode;
+    return IG_OK;
+}
+
+void ig_release_caches(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_cores.clear();
+    std::lock_guard<std::mutex> lk2(g_ws_mu);
+    g_ws.release();
+}
+
+unsigned long long ig_launch_count(int reset)
+{
+    return reset ? g_launches.exchange(0) : g_launches.load();
+}
+
+// ---- 1-D plans ----
+ig_cfft_plan ig_make_cfft_plan(size_t length, int dtype)
+{
+    ig_cfft_plan p = nullptr;
+    int rc = guarded([&] {
+        if (length == 0) raise(IG_EZERO_LEN, "zero-length FFT requested");
+        if (dtype != IG_F64 && dtype != IG_F32) raise(IG_EINVAL, "bad dtype");
+        auto pl = std::make_unique<ig_cfft_plan_i>();
+        pl->n = length;
+        pl->dtype = dtype;
+        pl->a = arith_for(dtype);
+        pl->core = get_core(pl->a, (long long)length, false);
+        p = pl.release();
+    });
+    (void)rc;
+    return p;
+}
+void ig_destroy_cfft_plan(ig_cfft_plan plan) { delete plan; }
+size_t ig_cfft_length(ig_cfft_plan plan) { return plan ? plan->n : 0; }
+
+ig_rfft_plan ig_make_rfft_plan(size_t length, int dtype)
+{
+    ig_rfft_plan p = nullptr;
+    guarded([&] {
+        if (length == 0) raise(IG_EZERO_LEN, "zero-length FFT requested");
+        if (dtype != IG_F64 && dtype != IG_F32) raise(IG_EINVAL, "bad dtype");
+        auto pl = std::make_unique<ig_rfft_plan_i>();
+        pl->n = length;
+        pl->dtype = dtype;
+        pl->a = arith_for(dtype);
+        bool even = length % 2 == 0 && length > 1;
+        pl->core = get_core(pl->a, even ? (long long)length / 2 : (long long)length, even);
+        p = pl.release();
+    });
+    return p;
+}
+void ig_destroy_rfft_plan(ig_rfft_plan plan) { delete plan; }
+size_t ig_rfft_length(ig_rfft_plan plan) { return plan ? plan->n : 0; }
+
+int ig_cfft_uses_bluestein(ig_cfft_plan plan, size_t *n2)
+{
+    if (!plan) return IG_EINVAL;
+    bool b = plan->core->d.blue || plan->core->kind == 2;
+    if (n2) *n2 = b ? (size_t)plan->core->n2 : 0;
+    return b ? 1 : 0;
+}
+int ig_rfft_uses_bluestein(ig_rfft_plan plan, size_t *n2)
+{
+    if (!plan) return IG_EINVAL;
+    bool b = plan->core->d.blue || plan->core->kind == 2;
+    if (n2) *n2 = b ? (size_t)plan->core->n2 : 0;
+    return b ? 1 : 0;
+}
+
+static Lines contiguous_lines(const void *in, void *out, long long batch, long long dist_in, long long dist_out,
+                              long long es_in, long long es_out)
+{
+    Lines ln;
+    ln.in = (const char *)in;
+    ln.out = (char *)out;
+    ln.es_in = es_in;
+    ln.es_out = es_out;
+    ln.nlines = batch;
+    ln.bn[0] = batch;
+    ln.bn[1] = ln.bn[2] = 1;
+    ln.bsi[0] = dist_in * es_in;
+    ln.bso[0] = dist_out * es_out;
+    ln.bsi[1] = ln.bsi[2] = ln.bso[1] = ln.bso[2] = 0;
+    return ln;
+}
+
+int ig_cfft_exec_device(ig_cfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in, size_t dist_out,
+                        int forward, double fct, void *stream)
+{
+    return guarded([&] {
+        if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        long long es = 2 * (long long)store_real_bytes(plan->a);
+        exec_op(plan->a, OP_C2C, (long long)plan->n,
+                contiguous_lines(in, out, (long long)batch, (long long)dist_in, (long long)dist_out, es, es), forward,
+                fct, as_stream(stream));
+    });
+}
+
+int ig_rfft_exec_device(ig_rfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in, size_t dist_out,
+                        int forward, double fct, void *stream)
+{
+    return guarded([&] {
+        if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        long long es = (long long)store_real_bytes(plan->a);
+        exec_op(plan->a, forward ? OP_R2HC : OP_HC2R, (long long)plan->n,
+                contiguous_lines(in, out, (long long)batch, (long long)dist_in, (long long)dist_out, es, es), forward,
+                fct, as_stream(stream));
+    });
+}
+
+static int host_batch(bool real, size_t n, Arith a, void *c, size_t batch, size_t dist, int forward, double fct)
+{
+    return guarded([&] {
+        if (!c) raise(IG_EINVAL, "null data pointer");
+        if (batch == 0) return;
+        long long es = (real ? 1 : 2) * (long long)store_real_bytes(a);
+        if (dist < n) raise(IG_EINVAL, "line distance smaller than the length");
+        size_t bytes = ((batch - 1) * dist + n) * (size_t)es;
+        std::lock_guard<std::mutex> lk(g_ws_mu);
+        void *d = g_ws.get(bytes);
+        ck(cudaMemcpy(d, c, bytes, cudaMemcpyHostToDevice), "H2D copy");
+        Lines ln = contiguous_lines(d, d, (long long)batch, (long long)dist, (long long)dist, es, es);
+        exec_op(a, real ? (forward ? OP_R2HC : OP_HC2R) : OP_C2C, (long long)n, ln, forward, fct, 0);
+        ck(cudaMemcpy(c, d, bytes, cudaMemcpyDeviceToHost), "D2H copy");
+    });
+}
+
+int ig_cfft_forward(ig_cfft_plan plan, void *c, double fct)
+{
+    if (!plan) { g_err = "null plan"; return IG_EINVAL; }
+    return host_batch(false, plan->n, plan->a, c, 1, plan->n, 1, fct);
+}
+int ig_cfft_backward(ig_cfft_plan plan, void *c, double fct)
+{
+    if (!plan) { g_err = "null plan"; return IG_EINVAL; }
+    return host_batch(false, plan->n, plan->a, c, 1, plan->n, 0, fct);
+}
+int ig_rfft_forward(ig_rfft_plan plan, void *c, double fct)
+{
+    if (!plan) { g_err = "null plan"; return IG_EINVAL; }
+    return host_batch(true, plan->n, plan->a, c, 1, plan->n, 1, fct);
+}
+int ig_rfft_backward(ig_rfft_plan plan, void *c, double fct)
+{
+    if (!plan) { g_err = "null plan"; return IG_EINVAL; }
+    return host_batch(true, plan->n, plan->a, c, 1, plan->n, 0, fct);
+}
+int ig_cfft_exec_batch(ig_cfft_plan plan, void *c, size_t batch, size_t dist, int forward, double fct)
+{
+    if (!plan) { g_err = "null plan"; return IG_EINVAL; }
+    return host_batch(false, plan->n, plan->a, c, batch, dist, forward, fct);
+}
+int ig_rfft_exec_batch(ig_rfft_plan plan, void *c, size_t batch, size_t dist, int forward, double fct)
+{
+    if (!plan) { g_err = "null plan"; return IG_EINVAL; }
+    return host_batch(true, plan->n, plan->a, c, batch, dist, forward, fct);
+}
+
+// ---- N-d ----
+static void nd_checks(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                      size_t naxes, const size_t *axes, const void *in, void *out, bool allow_inplace)
+{
+    if (dtype != IG_F64 && dtype != IG_F32) raise(IG_EINVAL, "bad dtype");
+    if (ndim < 1) raise(IG_ENDIM, "ndim must be >= 1");
+    if (!shape || !sin || !sout || (naxes && !axes)) raise(IG_EINVAL, "null argument");
+    check_axes(ndim, naxes, axes);
+    if (in == out) {
+        if (!allow_inplace) raise(IG_ESTRIDE_INPLACE, "stride mismatch");
+        for (size_t d = 0; d < ndim; ++d)
+            if (sin[d] != sout[d]) raise(IG_ESTRIDE_INPLACE, "stride mismatch");
+    }
+    if (!in || !out) raise(IG_EINVAL, "null data pointer");
+}
+
+static size_t prod(size_t ndim, const size_t *shape)
+{
+    size_t p = 1;
+    for (size_t d = 0; d < ndim; ++d) p *= shape[d];
+    return p;
+}
+
+int ig_c2c_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                  size_t naxes, const size_t *axes, int forward, const void *in, void *out, double fct, void *stream)
+{
+    return guarded([&] {
+        if (ndim >= 1 && shape && prod(ndim, shape) == 0) return;
+        nd_checks(dtype, ndim, shape, sin, sout, naxes, axes, in, out, true);
+        nd_c2c_device(arith_for(dtype), ndim, shape, sin, sout, naxes, axes, forward, in, out, fct,
+                      as_stream(stream));
+    });
+}
+
+static void nd_r2c_device(Arith a, size_t ndim, const size_t *shape_in, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                          size_t naxes, const size_t *axes, int forward, const void *in, void *out, double fct,
+                          cudaStream_t st)
+{
+    if (naxes == 0) return;
+    size_t last = axes[naxes - 1];
+    for_lines(ndim, shape_in, sin, sout, last, (const char *)in, (char *)out, [&](const Lines &ln) {
+        exec_op(a, OP_R2C, (long long)shape_in[last], ln, forward, fct, st);
+    });
+    if (naxes == 1) return;
+    std::vector<size_t> shape_out(shape_in, shape_in + ndim);
+    shape_out[last] = shape_in[last] / 2 + 1;
+    nd_c2c_device(a, ndim, shape_out.data(), sout, sout, naxes - 1, axes, forward, out, out, 1.0, st);
+}
+
+int ig_r2c_device(int dtype, size_t ndim, const size_t *shape_in, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                  size_t naxes, const size_t *axes, int forward, const void *in, void *out, double fct, void *stream)
+{
+    return guarded([&] {
+        if (ndim >= 1 && shape_in && prod(ndim, shape_in) == 0) return;
+        nd_checks(dtype, ndim, shape_in, sin, sout, naxes, axes, in, out, false);
+        nd_r2c_device(arith_for(dtype), ndim, shape_in, sin, sout, naxes, axes, forward, in, out, fct,
+                      as_stream(stream));
+    });
+}
+
+static void nd_c2r_device(Arith a, size_t ndim, const size_t *shape_out, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                          size_t naxes, const size_t *axes, int forward, const void *in, void *out, double fct,
+                          cudaStream_t st)
+{
+    if (naxes == 0) return;
+    size_t last = axes[naxes - 1];
+    if (naxes == 1) {
+        for_lines(ndim, shape_out, sin, sout, last, (const char *)in, (char *)out, [&](const Lines &ln) {
+            exec_op(a, OP_C2R, (long long)shape_out[last], ln, forward, fct, st);
+        });
+        return;
+    }
+    // c2c over the other axes into a contiguous temporary, then c2r on the last axis
+    std::vector<size_t> shape_in(shape_out, shape_out + ndim);
+    shape_in[last] = shape_out[last] / 2 + 1;
+    size_t ce = 2 * store_real_bytes(a);
+    std::vector<ptrdiff_t> sinter(ndim);
+    sinter[ndim - 1] = (ptrdiff_t)ce;
+    for (size_t d = ndim - 1; d-- > 0;) sinter[d] = sinter[d + 1] * (ptrdiff_t)shape_in[d + 1];
+    DevBuf tmp(prod(ndim, shape_in.data()) * ce);
+    nd_c2c_device(a, ndim, shape_in.data(), sin, sinter.data(), naxes - 1, axes, forward, in, tmp.p, 1.0, st);
+    for_lines(ndim, shape_out, sinter.data(), sout, last, (const char *)tmp.p, (char *)out, [&](const Lines &ln) {
+        exec_op(a, OP_C2R, (long long)shape_out[last], ln, forward, fct, st);
+    });
+    ck(cudaStreamSynchronize(st), "c2r temporary");
+}
+
+int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                  size_t naxes, const size_t *axes, int forward, const void *in, void *out, double fct, void *stream)
+{
+    return guarded([&] {
+        if (ndim >= 1 && shape_out && prod(ndim, shape_out) == 0) return;
+        nd_checks(dtype, ndim, shape_out, sin, sout, naxes, axes, in, out, false);
+        nd_c2r_device(arith_for(dtype), ndim, shape_out, sin, sout, naxes, axes, forward, in, out, fct,
+                      as_stream(stream));
+    });
+}
+
+// host-memory N-d: copy the byte spans to the GPU, run, copy back
+static void host_nd(int kind, int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                    size_t naxes, const size_t *axes, int forward, const void *in, void *out, double fct)
+{
+    Arith a = arith_for(dtype);
+    size_t sr = store_real_bytes(a);
+    std::vector<size_t> shp_in(shape, shape + ndim), shp_out(shape, shape + ndim);
+    size_t e_in = 2 * sr, e_out = 2 * sr;
+    if (kind == 1) {  // r2c
+        e_in = sr;
+        if (naxes) shp_out[axes[naxes - 1]] = shape[axes[naxes - 1]] / 2 + 1;
+    } else if (kind == 2) {  // c2r
+        e_out = sr;
+        if (naxes) shp_in[axes[naxes - 1]] = shape[axes[naxes - 1]] / 2 + 1;
+    }
+    long long ilo, ihi, olo, ohi;
+    span_of(ndim, shp_in.data(), sin, e_in, ilo, ihi);
+    span_of(ndim, shp_out.data(), sout, e_out, olo, ohi);
+    bool inplace = in == out;
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    size_t ibytes = (size_t)(ihi - ilo), obytes = (size_t)(ohi - olo);
+    size_t oalign = inplace ? 0 : ((ibytes + 255) / 256) * 256;
+    char *d = (char *)g_ws.get(oalign + (inplace ? std::max(ibytes, obytes) : obytes));
+    char *din = d - ilo;
+    char *dout = inplace ? din : d + oalign - olo;
+    ck(cudaMemcpy(d, (const char *)in + ilo, ibytes, cudaMemcpyHostToDevice), "H2D copy");
+    if (!inplace && !dense(ndim, shp_out.data(), sout, e_out))
+        ck(cudaMemcpy(dout + olo, (char *)out + olo, obytes, cudaMemcpyHostToDevice), "H2D copy (output gaps)");
+    if (kind == 0) nd_c2c_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
+    else if (kind == 1) nd_r2c_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
+    else nd_c2r_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
+    ck(cudaMemcpy((char *)out + olo, dout + olo, obytes, cudaMemcpyDeviceToHost), "D2H copy");
+}
+
+int ig_c2c(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
+           const size_t *axes, int forward, const void *in, void *out, double fct, size_t nthreads)
+{
+    (void)nthreads;
+    return guarded([&] {
+        if (ndim >= 1 && shape && prod(ndim, shape) == 0) return;
+        nd_checks(dtype, ndim, shape, sin, sout, naxes, axes, in, out, true);
+        host_nd(0, dtype, ndim, shape, sin, sout, naxes, axes, forward, in, out, fct);
+    });
+}
+int ig_r2c(int dtype, size_t ndim, const size_t *shape_in, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
+           const size_t *axes, int forward, const void *in, void *out, double fct, size_t nthreads)
+{
+    (void)nthreads;
+    return guarded([&] {
+        if (ndim >= 1 && shape_in && prod(ndim, shape_in) == 0) return;
+        nd_checks(dtype, ndim, shape_in, sin, sout, naxes, axes, in, out, false);
+        host_nd(1, dtype, ndim, shape_in, sin, sout, naxes, axes, forward, in, out, fct);
+    });
+}
+int ig_c2r(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
+           const size_t *axes, int forward, const void *in, void *out, double fct, size_t nthreads)
+{
+    (void)nthreads;
+    return guarded([&] {
+        if (ndim >= 1 && shape_out && prod(ndim, shape_out) == 0) return;
+        nd_checks(dtype, ndim, shape_out, sin, sout, naxes, axes, in, out, false);
+        host_nd(2, dtype, ndim, shape_out, sin, sout, naxes, axes, forward, in, out, fct);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// ig_inst.cuh -- launcher definitions, instantiated once per arithmetic.
+#pragma once
+#include "ig_kernels.cuh"
+#include "ig_launch.h"
+
+namespace ig {
+
+template <class Tag> struct TagType;
+template <> struct TagType<TagF32> { using T = float; };
+template <> struct TagType<TagDF> { using T = df; };
+template <> struct TagType<TagF64> { using T = double; };
+
+template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    long long grid = (io.nlines + io.lpc - 1) / io.lpc;
+    k_fft_smem<T><<<(unsigned)grid, (unsigned)(io.lpc * io.tpl), smem, st>>>(d, io);
+    return cudaGetLastError();
+}
+template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
+{
+    using T = typename TagType<Tag>::T;
+    // the dynamic limit excludes the kernel's static shared memory
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_fft_smem<T>);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_fft_smem<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                bytes - (int)fa.sharedSizeBytes);
+}
+template <class Tag> cudaError_t Launch<Tag>::stage_tw(void *tw, int R, int ns)
+{
+    using T = typename TagType<Tag>::T;
+    int n = ns * (R - 1);
+    if (!n) return cudaSuccess;
+    k_gen_stage_tw<T><<<(n + 255) / 256, 256>>>((cx<T> *)tw, R, ns);
+    return cudaGetLastError();
+}
+template <class Tag>
+cudaError_t Launch<Tag>::roots(void *out, long long count, unsigned long long mult, unsigned long long D)
+{
+    using T = typename TagType<Tag>::T;
+    if (!count) return cudaSuccess;
+    k_gen_roots<T><<<(unsigned)((count + 255) / 256), 256>>>((cx<T> *)out, count, mult, D);
+    return cudaGetLastError();
+}
+template <class Tag> cudaError_t Launch<Tag>::convert64(const void *in, void *out, long long n)
+{
+    using T = typename TagType<Tag>::T;
+    if (!n) return cudaSuccess;
+    k_convert64<T><<<(unsigned)((n + 255) / 256), 256>>>((const double2 *)in, (cx<T> *)out, n);
+    return cudaGetLastError();
+}
+
+}  // namespace ig

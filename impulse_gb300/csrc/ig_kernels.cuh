@@ -1,0 +1,509 @@
+// ig_kernels.cuh -- device kernels of the GPU FFT engine (templates).
+//
+// k_fft_smem is the workhorse: one CTA owns `lpc` whole lines, stages them
+// from HBM into shared memory, runs a Stockham autosort FFT of length L in
+// shared memory with register-resident radix-R butterflies, and writes the
+// result back.  Around the core it fuses the layout work of impulse's FFT
+// path:
+//   - complex lines (pocketfft::c2c, pocketfft_hdronly.h:3272);
+//   - real input packed as N/2 complex values with the split step that
+//     writes FFTPACK halfcomplex order directly (rfft_forward,
+//     impulse/fft/c_pocketfft/pocketfft.c:2184) or the N/2+1 half spectrum
+//     (general_r2c, pocketfft_hdronly.h:3125);
+//   - the inverse of both (rfft_backward pocketfft.c:2176, general_c2r
+//     pocketfft_hdronly.h:3180);
+//   - Bluestein for lengths with large prime factors (fftblue_fft,
+//     pocketfft.c:1945): chirp premultiply, zero padding, forward FFT,
+//     pointwise product with the transformed chirp, backward FFT and chirp
+//     postmultiply, all in shared memory;
+//   - the inter-pass twiddle of the four-step decomposition used for lines
+//     longer than shared memory.
+// FP64 lines computed in double-float are range-scaled per line by a power
+// of two (exact), so any finite input magnitude keeps ~48-bit accuracy.
+#pragma once
+#include <cuda_runtime.h>
+#include "ig_dft.cuh"
+#include "ig_types.h"
+
+namespace ig {
+
+template <class T> struct Traits;
+template <> struct Traits<float> {
+    using S = float;
+    using S2 = float2;
+    static constexpr bool kRaw = false;
+};
+template <> struct Traits<double> {
+    using S = double;
+    using S2 = double2;
+    static constexpr bool kRaw = false;
+};
+template <> struct Traits<df> {
+    using S = double;
+    using S2 = double2;
+    static constexpr bool kRaw = true;  // prologue stages raw doubles, first reader converts
+};
+
+__device__ __forceinline__ long long line_off(const IODesc &io, long long l, bool out)
+{
+    long long i0 = l % io.bn[0];
+    long long r = l / io.bn[0];
+    long long i1 = r % io.bn[1];
+    long long i2 = r / io.bn[1];
+    return out ? i0 * io.bso[0] + i1 * io.bso[1] + i2 * io.bso[2]
+               : i0 * io.bsi[0] + i1 * io.bsi[1] + i2 * io.bsi[2];
+}
+
+__device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+
+// slot read with optional raw-double conversion
+template <class T, bool RAW> __device__ __forceinline__ cx<T> sload(const cx<T> *p, int esc)
+{
+    if constexpr (RAW) {
+        double2 d = *reinterpret_cast<const double2 *>(p);
+        return cx<T>{Store<T>::in(d.x, esc), Store<T>::in(d.y, esc)};
+    } else {
+        return *p;
+    }
+}
+
+// one Stockham stage of radix R in shared memory, in place through registers
+template <class T, int R, bool FWD>
+__device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int nl, int tpl)
+{
+    constexpr int NB = (kE + R - 1) / R;
+    const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
+    const int L = P.L, nr = L / R, ns = P.st[si].ns;
+    const cx<T> *tw = reinterpret_cast<const cx<T> *>(P.tw) + P.st[si].tw;
+    cx<T> *line = sm + (size_t)g * P.LS;
+    cx<T> v[NB][R];
+    int jj[NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        int j = t + i * tpl;
+        jj[i] = (g < nl && j < nr) ? j : -1;
+        if (jj[i] >= 0) {
+            int k = j % ns;
+#pragma unroll
+            for (int m = 0; m < R; ++m) v[i][m] = line[j + m * nr];
+            if (k) {
+#pragma unroll
+                for (int m = 1; m < R; ++m) {
+                    cx<T> w = tw[k * (R - 1) + m - 1];
+                    v[i][m] = twmul<FWD>(v[i][m], w);
+                }
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        if (jj[i] >= 0) {
+            int j = jj[i], k = j % ns;
+            dft<R, FWD>(v[i]);
+            int base = (j / ns) * ns * R + k;
+#pragma unroll
+            for (int m = 0; m < R; ++m) line[base + m * ns] = v[i][m];
+        }
+    }
+    __syncthreads();
+}
+
+template <class T, bool FWD>
+__device__ __forceinline__ void stage_dispatch(cx<T> *sm, const CoreDesc &P, int si, int nl, int tpl)
+{
+    switch (P.st[si].R) {
+    case 2: stage<T, 2, FWD>(sm, P, si, nl, tpl); break;
+    case 3: stage<T, 3, FWD>(sm, P, si, nl, tpl); break;
+    case 4: stage<T, 4, FWD>(sm, P, si, nl, tpl); break;
+    case 5: stage<T, 5, FWD>(sm, P, si, nl, tpl); break;
+    case 7: stage<T, 7, FWD>(sm, P, si, nl, tpl); break;
+    case 8: stage<T, 8, FWD>(sm, P, si, nl, tpl); break;
+    case 11: stage<T, 11, FWD>(sm, P, si, nl, tpl); break;
+    case 16: stage<T, 16, FWD>(sm, P, si, nl, tpl); break;
+    default: break;
+    }
+}
+
+template <class T, bool FWD>
+__device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl, int tpl)
+{
+    for (int s = 0; s < P.nst; ++s) stage_dispatch<T, FWD>(sm, P, s, nl, tpl);
+}
+
+// scale helper: multiply by fct and store with the per-line exponent
+template <class T> struct OutScale;
+template <> struct OutScale<float> {
+    float f;
+    __device__ void init(double fct) { f = (float)fct; }
+    __device__ float apply(float v, int) const { return v * f; }
+};
+template <> struct OutScale<double> {
+    double f;
+    __device__ void init(double fct) { f = fct; }
+    __device__ double apply(double v, int) const { return v * f; }
+};
+template <> struct OutScale<df> {
+    df m;
+    int e;
+    __device__ void init(double fct)
+    {
+        // fct = m * 2^e with m in [1, 2): the exponent is folded into the
+        // integer output conversion, so no FP64 instruction is needed
+        if (fct == 0.0) { m = df{0.f, 0.f}; e = 0; return; }
+        int be = dexp(fct);
+        e = be - 1023;
+        m = df_from_double(fct, -e);
+    }
+    __device__ double apply(df v, int esc) const { return df_to_double(v * m, esc - e); }
+};
+
+template <class T>
+__global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
+{
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    constexpr bool RAW = Traits<T>::kRaw;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<T> *sm = reinterpret_cast<cx<T> *>(smraw);
+    __shared__ int s_esc[kMaxLinesPerCta];
+
+    const int lpc = io.lpc, tpl = io.tpl;
+    const long long line0 = (long long)blockIdx.x * lpc;
+    const int nl = (int)min((long long)lpc, io.nlines - line0);
+    const int M = P.M;
+
+    if (RAW && threadIdx.x < lpc) s_esc[threadIdx.x] = 0;
+    if (RAW) __syncthreads();
+
+    // ---- prologue: HBM -> shared memory ---------------------------------
+    {
+        // each thread walks units of one line: rows mode (g, t) = (tid / tpl, tid % tpl),
+        // cols mode (g, t) = (tid % lpc, tid / lpc)
+        int g, t;
+        if (io.cols_in) { g = threadIdx.x % lpc; t = threadIdx.x / lpc; }
+        else { g = threadIdx.x / tpl; t = threadIdx.x - g * tpl; }
+        int emax = 0;
+        if (g < nl && t < tpl) {
+            const char *base = io.in + line_off(io, line0 + g, false);
+            cx<T> *line = sm + (size_t)g * P.LS;
+            for (int u = t; u < io.cnt_in; u += tpl) {
+                S re, im;
+                if (io.in_kind == IN_C) {
+                    S2 z = *reinterpret_cast<const S2 *>(base + u * io.is);
+                    re = z.x; im = z.y;
+                } else if (io.in_kind == IN_R) {
+                    re = *reinterpret_cast<const S *>(base + u * io.is);
+                    im = 0;
+                } else if (io.in_kind == IN_P) {
+                    re = *reinterpret_cast<const S *>(base + (2 * (long long)u) * io.is);
+                    im = *reinterpret_cast<const S *>(base + (2 * (long long)u + 1) * io.is);
+                } else {  // IN_HC: unit 0 = (r0, 0); unit k = (r_{2k-1}, r_{2k}); even N: last = (r_{N-1}, 0)
+                    if (u == 0) { re = *reinterpret_cast<const S *>(base); im = 0; }
+                    else {
+                        re = *reinterpret_cast<const S *>(base + (2 * (long long)u - 1) * io.is);
+                        long long ii = 2 * (long long)u;
+                        im = (ii < io.nreal) ? *reinterpret_cast<const S *>(base + ii * io.is) : (S)0;
+                    }
+                }
+                if (io.conj_in) im = -im;
+                // general_c2r reads only the real part of the DC and Nyquist bins
+                if (io.pre != PRE_NONE && (u == 0 || (io.pre == PRE_HERM_EVEN && u == M))) im = 0;
+                if constexpr (RAW) {
+                    emax = max(emax, max(dexp(re), dexp(im)));
+                    *reinterpret_cast<double2 *>(line + u) = make_double2(re, im);
+                    if (io.pre == PRE_HERM_ODD && u > 0)
+                        *reinterpret_cast<double2 *>(line + (M - u)) = make_double2(re, -im);
+                } else {
+                    line[u] = cx<T>{(T)re, (T)im};
+                    if (io.pre == PRE_HERM_ODD && u > 0) line[M - u] = cx<T>{(T)re, (T)(-im)};
+                }
+            }
+        }
+        if constexpr (RAW) {
+            // per-line exponent: scale the largest element of the line to [1, 2)
+            if (g < nl && t < tpl && emax > 0) atomicMax(&s_esc[g], emax);
+        }
+    }
+    __syncthreads();
+    if constexpr (RAW) {
+        if ((int)threadIdx.x < lpc) {
+            int em = s_esc[threadIdx.x];
+            s_esc[threadIdx.x] = em > 0 ? 1023 - em : 0;
+        }
+        __syncthreads();
+        // raw doubles -> double-float, scaled by the line's power of two
+        for (int idx = threadIdx.x; idx < nl * P.LS; idx += blockDim.x) {
+            int l = idx / P.LS;
+            sm[idx] = sload<T, true>(sm + idx, s_esc[l]);
+        }
+        __syncthreads();
+    }
+
+    // ---- pre-processing ---------------------------------------------------
+    const int g = threadIdx.x / tpl, t = threadIdx.x - (threadIdx.x / tpl) * tpl;
+    cx<T> *myline = sm + (size_t)(g < lpc ? g : 0) * P.LS;
+    if (io.pre == PRE_HERM_EVEN) {
+        // X[0..M] (X[M] Nyquist) -> Z[k] = (X[k] + conj(X[M-k])) + i e^{+2 pi i k/2M} (X[k] - conj(X[M-k]))
+        const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
+        constexpr int NP = kE / 2 + 1;
+        cx<T> a[NP], b[NP];
+        int kk[NP];
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            int k = t + i * tpl;
+            kk[i] = (g < nl && k <= M / 2) ? k : -1;
+            if (kk[i] >= 0) {
+                a[i] = myline[k];
+                b[i] = myline[M - k];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            int k = kk[i];
+            if (k < 0) continue;
+            // Z[k] from (X[k], X[M-k]); Z[M-k] from (X[M-k], X[k])
+            {
+                cx<T> xa = a[i], xb = conjx(b[i]);
+                cx<T> A = xa + xb, Bv = xa - xb;
+                cx<T> w = conjx(rtw[k]);          // e^{+2 pi i k / N}
+                cx<T> tB = cmul(Bv, w);
+                myline[k] = cx<T>{A.r - tB.i, A.i + tB.r};
+            }
+            int k2 = M - k;
+            if (k > 0 && k2 != k) {
+                cx<T> xa = b[i], xb = conjx(a[i]);
+                cx<T> A = xa + xb, Bv = xa - xb;
+                cx<T> w = conjx(rtw[k2]);
+                cx<T> tB = cmul(Bv, w);
+                myline[k2] = cx<T>{A.r - tB.i, A.i + tB.r};
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- core ---------------------------------------------------------------
+    // Stockham: one pass in the transform's direction.  Bluestein (fftblue_fft,
+    // pocketfft.c:1945): a = x * chirp(-+), zero pad to L, FFT_L, multiply by
+    // chirpf (conjugated for the backward transform), IFFT_L, multiply by chirp(-+).
+    {
+        const cx<T> *ch = reinterpret_cast<const cx<T> *>(P.chirp);
+        const cx<T> *chf = reinterpret_cast<const cx<T> *>(P.chirpf);
+        const int L = P.L;
+        const int npass = P.blue ? 2 : 1;
+        for (int pass = 0; pass < npass; ++pass) {
+            if (P.blue && pass == 0) {
+                for (int idx = threadIdx.x; idx < nl * L; idx += blockDim.x) {
+                    int l = idx / L, u = idx - l * L;
+                    cx<T> *ln = sm + (size_t)l * P.LS;
+                    if (u < M) ln[u] = io.fwd ? cmulc(ln[u], ch[u]) : cmul(ln[u], ch[u]);
+                    else ln[u] = cx<T>{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
+                }
+                __syncthreads();
+            } else if (P.blue) {
+                for (int idx = threadIdx.x; idx < nl * L; idx += blockDim.x) {
+                    int l = idx / L, u = idx - l * L;
+                    cx<T> *ln = sm + (size_t)l * P.LS;
+                    ln[u] = io.fwd ? cmul(ln[u], chf[u]) : cmulc(ln[u], chf[u]);
+                }
+                __syncthreads();
+            }
+            const bool fwd = P.blue ? (pass == 0) : (io.fwd != 0);
+            if (fwd) run_stages<T, true>(sm, P, nl, tpl);
+            else run_stages<T, false>(sm, P, nl, tpl);
+        }
+        if (P.blue) {
+            for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
+                int l = idx / M, u = idx - l * M;
+                cx<T> *ln = sm + (size_t)l * P.LS;
+                ln[u] = io.fwd ? cmulc(ln[u], ch[u]) : cmul(ln[u], ch[u]);
+            }
+            __syncthreads();
+        }
+    }
+
+    // ---- post-processing ----------------------------------------------------
+    if (io.post == POST_SPLIT) {
+        // Z = FFT_M(x_even + i x_odd) -> X[k] = E_k + w^k O_k, k = 0..M,
+        // E_k = (Z[k] + conj(Z[M-k]))/2, O_k = -i (Z[k] - conj(Z[M-k]))/2, w = e^{-2 pi i/2M}
+        const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
+        constexpr int NP = kE / 2 + 1;
+        cx<T> a[NP], b[NP];
+        int kk[NP];
+        constexpr T half = RealOps<T>::k(0.5);
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            int k = t + i * tpl;
+            kk[i] = (g < nl && k <= M / 2) ? k : -1;
+            if (kk[i] >= 0) {
+                a[i] = myline[k];
+                b[i] = myline[k == 0 ? 0 : M - k];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            int k = kk[i];
+            if (k < 0) continue;
+            {
+                cx<T> za = a[i], zb = conjx(b[i]);
+                cx<T> E = cscale(za + zb, half);
+                cx<T> D = cscale(za - zb, half);
+                cx<T> O = cx<T>{D.i, -D.r};  // -i D
+                myline[k] = E + cmul(O, rtw[k]);
+            }
+            int k2 = M - k;  // k = 0 -> slot M (Nyquist)
+            if (k2 != k) {
+                cx<T> za = b[i], zb = conjx(a[i]);
+                cx<T> E = cscale(za + zb, half);
+                cx<T> D = cscale(za - zb, half);
+                cx<T> O = cx<T>{D.i, -D.r};
+                myline[k2] = E + cmul(O, rtw[k2]);
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- epilogue: shared memory -> HBM ---------------------------------------
+    {
+        int g2, t2;
+        if (io.cols_out) { g2 = threadIdx.x % lpc; t2 = threadIdx.x / lpc; }
+        else { g2 = threadIdx.x / tpl; t2 = threadIdx.x - g2 * tpl; }
+        if (g2 < nl && t2 < tpl) {
+            OutScale<T> sc;
+            sc.init(io.fct);
+            const int esc = RAW ? s_esc[g2] : 0;
+            const long long l = line0 + g2;
+            char *base = io.out + line_off(io, l, true);
+            const cx<T> *line = sm + (size_t)g2 * P.LS;
+            long long n2 = io.tw4 ? (l % io.bn[0]) : 0;
+            const cx<T> *whi = reinterpret_cast<const cx<T> *>(io.tw4hi);
+            const cx<T> *wlo = reinterpret_cast<const cx<T> *>(io.tw4lo);
+            for (int u = t2; u < io.cnt_out; u += tpl) {
+                cx<T> z = line[u];
+                if (io.tw4) {
+                    long long tt = (n2 * u) % io.tw4N;
+                    long long hi = tt / io.tw4S, lo = tt - hi * io.tw4S;
+                    cx<T> w = cmul(whi[hi], wlo[lo]);
+                    z = io.fwd ? cmul(z, w) : cmulc(z, w);
+                }
+                if (io.conj_out) z.i = -z.i;
+                // general_r2c stores the DC and Nyquist bins with a zero imaginary part
+                if (io.real_out && (u == 0 || (io.post == POST_SPLIT && u == M))) z.i = RealOps<T>::k(0.0);
+                if (io.out_kind == OUT_C) {
+                    S2 o;
+                    o.x = sc.apply(z.r, esc);
+                    o.y = sc.apply(z.i, esc);
+                    *reinterpret_cast<S2 *>(base + u * io.os) = o;
+                } else if (io.out_kind == OUT_R) {
+                    *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
+                } else if (io.out_kind == OUT_P) {
+                    *reinterpret_cast<S *>(base + (2 * (long long)u) * io.os) = sc.apply(z.r, esc);
+                    *reinterpret_cast<S *>(base + (2 * (long long)u + 1) * io.os) = sc.apply(z.i, esc);
+                } else {  // OUT_HC
+                    if (u == 0) *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
+                    else {
+                        *reinterpret_cast<S *>(base + (2 * (long long)u - 1) * io.os) = sc.apply(z.r, esc);
+                        long long ii = 2 * (long long)u;
+                        if (ii < io.nreal)
+                            *reinterpret_cast<S *>(base + ii * io.os) = sc.apply(z.i, esc);
+                    }
+                }
+            }
+        }
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// table builders (FP64, exact integer angle reduction, CUDA's sincospi)
+// ---------------------------------------------------------------------------
+
+// exp(+2 pi i t / D) for 0 <= t: reduce t/D to the first octant with integer
+// arithmetic, evaluate sincospi there, and undo the reduction by symmetry.
+__device__ inline double2 exp2pi_frac(unsigned long long t, unsigned long long D)
+{
+    t %= D;
+    bool neg = false;
+    if (2 * t > D) { t = D - t; neg = true; }
+    double c, s;
+    if (4 * t > D) {
+        // angle = pi/2 + 2 pi (4t - D) / (4D)
+        unsigned long long num = 4 * t - D, den = 4 * D;
+        double cq, sq;
+        if (8 * num > den) {
+            double x = 2.0 * (double)(den - 4 * num) / (double)(4 * den);
+            sincospi(x, &cq, &sq);  // cos(q) = sin(pi/2 - q)
+        } else {
+            double x = 2.0 * (double)num / (double)den;
+            sincospi(x, &sq, &cq);
+        }
+        c = -sq;
+        s = cq;
+    } else if (8 * t > D) {
+        double x = 2.0 * (double)(D - 4 * t) / (double)(4 * D);
+        sincospi(x, &c, &s);  // swapped: angle = pi/2 - x pi
+    } else {
+        double x = 2.0 * (double)t / (double)D;
+        sincospi(x, &s, &c);
+    }
+    return make_double2(c, neg ? -s : s);
+}
+
+template <class T> __device__ inline cx<T> to_arith(double2 v);
+template <> __device__ inline cx<float> to_arith<float>(double2 v) { return cx<float>{__double2float_rn(v.x), __double2float_rn(v.y)}; }
+template <> __device__ inline cx<double> to_arith<double>(double2 v) { return cx<double>{v.x, v.y}; }
+template <> __device__ inline cx<df> to_arith<df>(double2 v) { return cx<df>{df_from_double(v.x), df_from_double(v.y)}; }
+
+// stage twiddles: entry k*(R-1) + m-1 = exp(-2 pi i m k / (ns R)), k < ns, 1 <= m < R
+template <class T> __global__ void k_gen_stage_tw(cx<T> *tw, int R, int ns)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ns * (R - 1)) return;
+    int k = e / (R - 1), m = e % (R - 1) + 1;
+    double2 v = exp2pi_frac((unsigned long long)m * k, (unsigned long long)ns * R);
+    v.y = -v.y;
+    tw[e] = to_arith<T>(v);
+}
+
+// roots: out[j] = exp(-2 pi i (j * mult) / D), j < count
+template <class T> __global__ void k_gen_roots(cx<T> *out, long long count, unsigned long long mult, unsigned long long D)
+{
+    long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= count) return;
+    double2 v = exp2pi_frac(((unsigned long long)j * mult) % D, D);
+    v.y = -v.y;
+    out[j] = to_arith<T>(v);
+}
+
+// Bluestein chirp exp(+i pi m^2 / n) with m^2 mod 2n in exact integers
+// (pocketfft.c:1907-1914 keeps the same quantity by a recurrence)
+static __global__ void k_gen_chirp64(double2 *bk, long long n)
+{
+    long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    unsigned long long mm = (unsigned long long)m % (2ull * n);
+    unsigned long long coeff = (mm * mm) % (2ull * n);
+    bk[m] = exp2pi_frac(coeff, 2ull * n);
+}
+
+// symmetric zero padding of the chirp to length L (scaled 1/L), for its FFT
+static __global__ void k_pad_chirp64(const double2 *bk, double2 *out, long long n, long long L)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= L) return;
+    double s = 1.0 / (double)L;
+    double2 v = make_double2(0.0, 0.0);
+    if (k < n) v = bk[k];
+    else if (L - k < n) v = bk[L - k];
+    out[k] = make_double2(v.x * s, v.y * s);
+}
+
+template <class T> __global__ void k_convert64(const double2 *in, cx<T> *out, long long n)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = to_arith<T>(in[k]);
+}
+
+}  // namespace ig

@@ -1,0 +1,29 @@
+// ig_launch.h -- host entry points into the per-arithmetic kernel units
+// (ig_inst_f32.cu, ig_inst_df.cu, ig_inst_f64.cu).  Each returns the CUDA
+// launch status.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ig_types.h"
+
+namespace ig {
+
+// tag types standing for the device arithmetic of each unit
+struct TagF32 {};
+struct TagDF {};
+struct TagF64 {};
+
+template <class Tag> struct Launch {
+    // k_fft_smem with `lpc` lines of `tpl` threads per CTA and `smem` bytes
+    static cudaError_t fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
+    static cudaError_t set_max_smem(int bytes);
+    static cudaError_t stage_tw(void *tw, int R, int ns);
+    static cudaError_t roots(void *out, long long count, unsigned long long mult, unsigned long long D);
+    static cudaError_t convert64(const void *in, void *out, long long n);
+};
+
+// FP64 helpers for Bluestein tables (built in ig_inst_df.cu)
+cudaError_t launch_chirp64(void *bk, long long n);
+cudaError_t launch_pad_chirp64(const void *bk, void *out, long long n, long long L);
+
+}  // namespace ig

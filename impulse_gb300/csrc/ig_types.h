@@ -1,0 +1,58 @@
+// ig_types.h -- plain descriptors shared by the host engine and the kernels.
+#pragma once
+
+namespace ig {
+
+constexpr int kMaxStages = 24;
+constexpr int kMaxLinesPerCta = 128;
+constexpr int kE = 16;  // complex elements per thread in the core
+
+struct StageDesc {
+    int R, ns, tw;  // radix, product of previous radices, twiddle offset (cx units)
+};
+
+enum InKind { IN_C = 0, IN_R = 1, IN_P = 2, IN_HC = 3 };
+enum OutKind { OUT_C = 0, OUT_R = 1, OUT_P = 2, OUT_HC = 3 };
+enum PreKind { PRE_NONE = 0, PRE_HERM_EVEN = 1, PRE_HERM_ODD = 2 };
+enum PostKind { POST_NONE = 0, POST_SPLIT = 1 };
+
+struct CoreDesc {
+    int M;    // logical complex length of the core transform
+    int L;    // Stockham length run in shared memory (M, or n2 for Bluestein)
+    int LS;   // shared-memory complex slots per line (>= max(L, M + 1))
+    int blue; // 1: Bluestein core
+    int nst;
+    StageDesc st[kMaxStages];
+    const void *tw;     // cx<T> stage twiddles, forward sign
+    const void *chirp;  // cx<T> exp(+i pi m^2 / M), m < M  (Bluestein)
+    const void *chirpf; // cx<T> FFT_L of the padded chirp / L  (Bluestein)
+    const void *rtw;    // cx<T> exp(-2 pi i k / (2M)), k <= M  (real split)
+};
+
+struct IODesc {
+    const char *in;
+    char *out;
+    long long is, os;       // byte stride along the line (between storage units of the kind)
+    long long nlines;
+    long long bn[3];        // batch dims: line l -> (l % bn0, (l / bn0) % bn1, l / (bn0 bn1))
+    long long bsi[3], bso[3];
+    int in_kind, out_kind, pre, post;
+    int cnt_in, cnt_out;    // storage units per line
+    int conj_in, conj_out;
+    int real_out;           // output is the spectrum of real data (zero DC / Nyquist imaginary parts)
+    int cols_in, cols_out;  // 1: consecutive threads walk consecutive lines
+    int lpc, tpl;           // lines per CTA, threads per line
+    long long nreal;        // real length N for halfcomplex units
+    int fwd;                // direction of the core transform
+    double fct;             // output scale
+    // four-step inter-pass twiddle on output unit u of line l:
+    // t = ((l % bn0) * u) mod tw4N, value w_hi[t / tw4S] * w_lo[t % tw4S]
+    int tw4;
+    long long tw4N, tw4S;
+    const void *tw4hi, *tw4lo;
+};
+
+
+enum Arith { A_F32 = 0, A_DF = 1, A_F64 = 2 };
+
+}  // namespace ig

@@ -1,0 +1,153 @@
+/*
+ * impulse_gpu.h -- C ABI of the GB300 FFT engine behind impulse's FFT API.
+ *
+ * The engine replaces the native numerics under impulse's Nim FFT module:
+ *
+ *   C backend   impulse/fft/c_pocketfft/pocketfft.nim binds pocketfft.h
+ *               (impulse/fft/c_pocketfft/pocketfft.h:18-32) with
+ *               {.importc, header.} at pocketfft.nim:71-81;
+ *   C++ backend impulse/fft/cpp_pocketfft/pocketfft.nim binds the
+ *               templates pocketfft::c2c / r2c / c2r
+ *               (impulse/fft/cpp_pocketfft/pocketfft_hdronly.h:3272, 3334,
+ *               3366) with {.importcpp.} at pocketfft.nim:35-69.
+ *
+ * Every function here is a plain C entry point (no exceptions, no C++ or
+ * torch types) that a Nim module binds with {.importc, dynlib.}.
+ * Data pointers of the pocketfft-shaped entry points are HOST pointers, as in
+ * the reference; the engine copies to the GPU, runs hand-written sm_103a
+ * kernels and copies back.  The *_device entry points take device pointers
+ * and a CUDA stream and do no host copies.
+ *
+ * dtype: IG_F64 (double / complex128 data) or IG_F32 (float / complex64).
+ * Complex data is interleaved (re, im), binary-compatible with Nim's
+ * Complex64 / Complex32 and std::complex.
+ */
+#ifndef IMPULSE_GPU_H
+#define IMPULSE_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define IG_OK 0
+#define IG_ENOMEM (-1)          /* allocation failed: pocketfft's -1 (pocketfft.c:878) */
+#define IG_EINVAL_AXIS (-2)     /* "bad axis number" (pocketfft_hdronly.h:466) */
+#define IG_EREPEAT_AXIS (-3)    /* "axis specified repeatedly" (pocketfft_hdronly.h:467) */
+#define IG_ESTRIDE_INPLACE (-4) /* "stride mismatch" (pocketfft_hdronly.h:453) */
+#define IG_EZERO_LEN (-5)       /* "zero-length FFT requested" (pocketfft_hdronly.h:2360) */
+#define IG_ECUDA (-6)           /* CUDA runtime error */
+#define IG_ENDIM (-7)           /* "ndim must be >= 1" / "stride dimension mismatch" (pocketfft_hdronly.h:450-452) */
+#define IG_EINVAL (-8)          /* other invalid argument (null pointer, bad dtype, ...) */
+#define IG_ETIMEOUT (-9)        /* a bounded device-side wait expired */
+#define IG_ETOOLARGE (-10)      /* size beyond a documented limit */
+
+#define IG_F64 0
+#define IG_F32 1
+
+/* Message of the last failing call on this thread ("" after success). */
+const char *ig_last_error_string(void);
+/* ABI version (major * 10000 + minor * 100 + patch). */
+int ig_version(void);
+
+/* ---- 1-D plans: mirror of pocketfft.h (pocketfft.h:18-32) ---------------
+ * A plan is a host handle to device-resident twiddle / chirp tables, built on
+ * the GPU.  Plans are read-only after construction and may be shared between
+ * threads, as the reference's plans are (c_pocketfft/README.md:32-36).
+ * make_* returns NULL for length 0 or on failure (reason in
+ * ig_last_error_string), like make_cfft_plan (pocketfft.c:2068).        */
+typedef struct ig_cfft_plan_i *ig_cfft_plan;
+typedef struct ig_rfft_plan_i *ig_rfft_plan;
+
+/* replaces make_cfft_plan (pocketfft.h:20) */
+ig_cfft_plan ig_make_cfft_plan(size_t length, int dtype);
+/* replaces destroy_cfft_plan (pocketfft.h:21) */
+void ig_destroy_cfft_plan(ig_cfft_plan plan);
+/* replaces cfft_backward (pocketfft.h:22): in place on `length` complex values
+ * at host pointer c, c[k] = fct * sum_m c[m] exp(+2 pi i m k / n) */
+int ig_cfft_backward(ig_cfft_plan plan, void *c, double fct);
+/* replaces cfft_forward (pocketfft.h:23): exp(-2 pi i m k / n) */
+int ig_cfft_forward(ig_cfft_plan plan, void *c, double fct);
+/* replaces cfft_length (pocketfft.h:24) */
+size_t ig_cfft_length(ig_cfft_plan plan);
+
+/* replaces make_rfft_plan (pocketfft.h:28) */
+ig_rfft_plan ig_make_rfft_plan(size_t length, int dtype);
+/* replaces destroy_rfft_plan (pocketfft.h:29) */
+void ig_destroy_rfft_plan(ig_rfft_plan plan);
+/* replaces rfft_backward (pocketfft.h:30): halfcomplex
+ * [r0, r1, i1, ..., (r_{n/2})] -> n reals, in place */
+int ig_rfft_backward(ig_rfft_plan plan, void *c, double fct);
+/* replaces rfft_forward (pocketfft.h:31): n reals -> halfcomplex, in place */
+int ig_rfft_forward(ig_rfft_plan plan, void *c, double fct);
+/* replaces rfft_length (pocketfft.h:32) */
+size_t ig_rfft_length(ig_rfft_plan plan);
+
+/* Batched host-memory variants: `batch` lines, line b starting `dist`
+ * elements (complex for cfft, real for rfft) after line b-1.  The reference
+ * loops over lines in Nim (one pocketfft call each); these move the loop
+ * into one GPU launch. */
+int ig_cfft_exec_batch(ig_cfft_plan plan, void *c, size_t batch, size_t dist, int forward, double fct);
+int ig_rfft_exec_batch(ig_rfft_plan plan, void *c, size_t batch, size_t dist, int forward, double fct);
+
+/* Device-memory variants (no host copies; `in` may equal `out`).  Line b of
+ * the input starts dist_in elements after line b-1, likewise the output. */
+int ig_cfft_exec_device(ig_cfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in,
+                        size_t dist_out, int forward, double fct, void *stream);
+int ig_rfft_exec_device(ig_rfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in,
+                        size_t dist_out, int forward, double fct, void *stream);
+
+/* Plan introspection: 1 when the plan runs Bluestein; the padded length. */
+int ig_cfft_uses_bluestein(ig_cfft_plan plan, size_t *n2);
+int ig_rfft_uses_bluestein(ig_rfft_plan plan, size_t *n2);
+
+/* ---- N-d strided transforms: mirror of pocketfft::c2c / r2c / c2r --------
+ * shape, strides (in BYTES, may be negative), axes and fct as in
+ * pocketfft_hdronly.h:3272 (c2c), 3334 (r2c: shape is the real input's
+ * shape, the output has shape[axes.back()]/2+1 there), 3366 (c2r: shape is
+ * the real OUTPUT's shape).  `nthreads` is accepted for signature parity and
+ * ignored: the GPU grid replaces the host thread pool.  Host pointers. */
+int ig_c2c(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in, const ptrdiff_t *stride_out,
+           size_t naxes, const size_t *axes, int forward, const void *data_in, void *data_out, double fct,
+           size_t nthreads);
+int ig_r2c(int dtype, size_t ndim, const size_t *shape_in, const ptrdiff_t *stride_in,
+           const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int forward, const void *data_in,
+           void *data_out, double fct, size_t nthreads);
+int ig_c2r(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *stride_in,
+           const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int forward, const void *data_in,
+           void *data_out, double fct, size_t nthreads);
+
+/* Device-pointer variants of the three above, on `stream` (cudaStream_t;
+ * NULL = the default stream). */
+int ig_c2c_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in,
+                  const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int forward, const void *data_in,
+                  void *data_out, double fct, void *stream);
+int ig_r2c_device(int dtype, size_t ndim, const size_t *shape_in, const ptrdiff_t *stride_in,
+                  const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int forward,
+                  const void *data_in, void *data_out, double fct, void *stream);
+int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *stride_in,
+                  const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int forward,
+                  const void *data_in, void *data_out, double fct, void *stream);
+
+/* ---- engine control ------------------------------------------------------ */
+/* Select the arithmetic used for IG_F64 data: 0 = double-float (default;
+ * FP32-pair butterflies, ~48-bit significand, for GB300's narrow FP64
+ * pipe), 1 = native FP64 butterflies.  Applies to plans made afterwards. */
+int ig_set_f64_arith(int mode);
+/* Release cached plans and workspace memory. */
+void ig_release_caches(void);
+/* Number of kernel launches the engine issued since the last reset. */
+unsigned long long ig_launch_count(int reset);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMPULSE_GPU_H */

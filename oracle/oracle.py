@@ -279,8 +279,14 @@ def ref_r2r_fftpack(x, axes, real2hermitian=True, forward=True, fct=1.0, nthread
 
 
 def rel_l2(a, b):
-    a = np.asarray(a)
-    b = np.asarray(b)
-    den = np.linalg.norm(b.ravel())
-    num = np.linalg.norm((a - b).ravel())
-    return float(num / den) if den else float(num)
+    """||a - b||_2 / ||b||_2, scaled first so that huge or tiny values do not overflow."""
+    a = np.asarray(a).astype(np.complex128 if np.iscomplexobj(a) or np.iscomplexobj(b) else np.float64)
+    b = np.asarray(b).astype(a.dtype)
+    s = float(np.max(np.abs(b))) if b.size else 0.0
+    if not np.isfinite(s):
+        return float("nan")
+    if s == 0.0:
+        return float(np.linalg.norm((a - b).ravel()))
+    den = np.linalg.norm((b / s).ravel())
+    num = np.linalg.norm(((a - b) / s).ravel())
+    return float(num / den)
