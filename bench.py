@@ -1,0 +1,431 @@
+"""Benchmark of the impulse FFT path on GB300.
+
+Workload (one "step"): the real-input FFT in packed halfcomplex layout
+(impulse's ``fft(var openArray[float], forward)``, i.e. PocketFFT
+``rfft_forward``) over seeded lengths 2^a 3^b 5^c 7^d 11^e in [64, 65536]
+plus the primes 1009, 8191 and 65521 (Bluestein), each length batched to
+about 2^24 real elements, values i.i.d. normal(0, 1).  Every length's batch
+is one call of ``ig_rfft_exec_device``; a step is one forward transform of
+every length.  The FP64 form is the headline; the FP32 form of the same
+workload is reported beside it.
+
+Metric: GB/s of algorithmic traffic (one read and one write of the real data
+per transform: 2 * sizeof(real) * N bytes per line), with inputs resident in
+HBM; ``e2e`` is the same metric through the host-memory C ABI
+(``ig_rfft_exec_batch``: host->device copy, transform, device->host copy
+inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 2
+TOTAL_REALS = 1 << 24
+PRIMES = [1009, 8191, 65521]
+
+
+def smooth_numbers(lo, hi):
+    out = []
+    p2 = 1
+    while p2 <= hi:
+        p3 = p2
+        while p3 <= hi:
+            p5 = p3
+            while p5 <= hi:
+                p7 = p5
+                while p7 <= hi:
+                    p11 = p7
+                    while p11 <= hi:
+                        if p11 >= lo:
+                            out.append(p11)
+                        p11 *= 11
+                    p7 *= 7
+                p5 *= 5
+            p3 *= 3
+        p2 *= 2
+    return sorted(out)
+
+
+def workload_lengths(count=32):
+    """32 log-uniform draws in [64, 65536] rounded (in log) to the nearest 11-smooth length, + 3 primes."""
+    rng = np.random.default_rng(SEED)
+    sm = np.array(smooth_numbers(64, 65536), dtype=np.float64)
+    logs = np.log(sm)
+    out = []
+    for u in rng.uniform(math.log(64), math.log(65536), count):
+        out.append(int(sm[np.argmin(np.abs(logs - u))]))
+    return sorted(set(out)) + PRIMES
+
+
+def batch_for(n):
+    return max(1, int(round(TOTAL_REALS / n)))
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# CPU side: the reference's algorithm restated (oracle port) on host threads
+# --------------------------------------------------------------------------
+def cpu_sample_run(lengths, min_seconds=10.0, max_passes=50):
+    """Time the oracle's threaded halfcomplex transform on a bounded sample of the workload:
+    each length at 1/64 of its batch.  Returns (GB/s, passes, seconds, sample description)."""
+    from oracle import oracle as O  # CPU-baseline leg only
+    if not os.path.exists(O.ORACLE_SO):
+        O.build(ref=False)
+    lib = O.lib()
+    nth = os.cpu_count() or 1
+    rng = np.random.default_rng(SEED)
+    data = []
+    for n in lengths:
+        b = max(1, batch_for(n) // 64)
+        data.append((n, b, rng.standard_normal((b, n))))
+    bytes_pass = sum(2 * 8 * n * b for n, b, _ in data)
+    t0 = time.perf_counter()
+    passes = 0
+    while True:
+        for n, b, x in data:
+            lib.io_rfft_batch(n, b, x.ctypes.data_as(C.POINTER(C.c_double)), n, 1, 1.0, nth)
+        passes += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or passes >= max_passes:
+            break
+    gbs = bytes_pass * passes / el / 1e9
+    sample = (f"{len(lengths)} lengths x 1/64 of each batch ({bytes_pass / 2 / 8 / 1e6:.1f} M reals f64 per pass), "
+              f"{passes} passes, {el:.1f} s, oracle port (FP64 C restatement of PocketFFT's algorithm)")
+    return gbs, nth, sample, el / passes
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    import torch
+    from impulse_gb300 import _lib as L
+    from impulse_gb300 import fft as F
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    lib = L.load()
+    stream = torch.cuda.current_stream(dev)
+    sptr = C.c_void_p(stream.cuda_stream)
+    lengths = workload_lengths()
+
+    def make(dtype):
+        dt = torch.float64 if dtype == "f64" else torch.float32
+        code = L.IG_F64 if dtype == "f64" else L.IG_F32
+        g = torch.Generator(device=dev)
+        g.manual_seed(SEED)
+        items = []
+        for n in lengths:
+            b = batch_for(n)
+            x = torch.randn((b, n), generator=g, device=dev, dtype=dt)
+            y = torch.empty_like(x)
+            plan = lib.ig_make_rfft_plan(n, code)
+            if not plan:
+                raise RuntimeError(lib.ig_last_error_string().decode())
+            items.append((n, b, x, y, plan))
+        return items
+
+    def step(items):
+        for n, b, x, y, plan in items:
+            rc = lib.ig_rfft_exec_device(plan, x.data_ptr(), y.data_ptr(), b, n, n, 1, 1.0, sptr)
+            if rc:
+                raise RuntimeError(lib.ig_last_error_string().decode())
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(items, steps, warmup, per_length=False):
+        for _ in range(warmup):
+            step(items)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        lib.ig_launch_count(1)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        per = None
+        if per_length:
+            per = [[torch.cuda.Event(enable_timing=True) for _ in range(len(items) + 1)] for _ in range(steps)]
+        ev0.record(stream)
+        for s in range(steps):
+            if per_length:
+                for i, it in enumerate(items):
+                    per[s][i].record(stream)
+                    step([it])
+                per[s][-1].record(stream)
+            else:
+                step(items)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        launches = lib.ig_launch_count(0)
+        barrier()
+        ms = ev0.elapsed_time(ev1)
+        per_ms = None
+        if per_length:
+            per_ms = [sum(per[s][i].elapsed_time(per[s][i + 1]) for s in range(steps)) / steps
+                      for i in range(len(items))]
+        return ms, launches, per_ms
+
+    def max_over_ranks(v):
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([v], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    result = {}
+    items64 = make("f64")
+    bytes64 = sum(2 * 8 * n * b for n, b, *_ in items64)
+    clk = ClockSampler(dev.index)
+    clk.start()
+    ms64, launches, per_ms = timed(items64, args.steps, args.warmup, per_length=True)
+    clocks = clk.stop()
+    ms64 = max_over_ranks(ms64)
+    step_ms = ms64 / args.steps
+    value = world * bytes64 / (step_ms / 1e3) / 1e9
+
+    # FP32 form of the same workload, and its error against the FP64 result
+    items32 = make("f32")
+    ms32, _, _ = timed(items32, args.steps, args.warmup)
+    ms32 = max_over_ranks(ms32)
+    errs = []
+    for (n, b, x64, y64, _), (_, _, x32, y32, _) in zip(items64, items32):
+        # same seeded input in FP64 for the FP32 error: transform x32 upcast with the FP64 path
+        xr = x32[:4].double().contiguous()
+        yr = torch.empty_like(xr)
+        rc = lib.ig_rfft_exec_device(items64[[i[0] for i in items64].index(n)][4], xr.data_ptr(), yr.data_ptr(),
+                                     xr.shape[0], n, n, 1, 1.0, sptr)
+        assert rc == 0
+        torch.cuda.synchronize()
+        d = (y32[:4].double() - yr)
+        errs.append((n, float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(yr))))
+    bytes32 = sum(2 * 4 * n * b for n, b, *_ in items32)
+
+    # end to end through the host-memory C ABI (pinned host buffers)
+    e2e = None
+    if not args.no_e2e:
+        host = []
+        for n, b, x, y, plan in items64:
+            h = torch.empty((b, n), dtype=torch.float64, pin_memory=True)
+            h.copy_(x.cpu())
+            host.append((n, b, h))
+        plans = {n: F.FFTPlanReal(n, L.IG_F64) for n, _, _ in host}
+        e_steps = max(1, min(args.steps, 5))
+        for _ in range(1):
+            for n, b, h in host:
+                L.check(lib.ig_rfft_exec_batch(plans[n].pocket, h.data_ptr(), b, n, 1, 1.0))
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            for n, b, h in host:
+                L.check(lib.ig_rfft_exec_batch(plans[n].pocket, h.data_ptr(), b, n, 1, 1.0))
+        torch.cuda.synchronize()
+        el = max_over_ranks(time.perf_counter() - t0)
+        hb = sum(8 * n * b for n, b, _ in host)
+        e2e = {"value": round(world * bytes64 * e_steps / el / 1e9, 3), "unit": "GB/s",
+               "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "steps": e_steps,
+               "api": "ig_rfft_exec_batch (host memory, in place)"}
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_kind = "measured"
+    if not peak:
+        peak, peak_kind = 6800.0, "fallback"
+    # roofline over the FFT launches: algorithmic bytes / event-timed duration per length
+    achieved = bytes64 / (sum(per_ms) / 1e3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_ratio.txt")
+    if os.path.exists(prof):
+        for ln in open(prof):
+            if ln.startswith("dram_bytes_per_algorithmic_byte:"):
+                traffic = round(float(ln.split(":")[1]) * bytes64 / len(items64), 1)
+    slow = [(n, round(2 * 8 * n * b / (t / 1e3) / 1e9, 1)) for (n, b, *_), t in zip(items64, per_ms)]
+    result = {
+        "metric": "FFT GB/s (halfcomplex real FFT, algorithmic bytes) vs HBM peak",
+        "value": round(value, 2),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(step_ms, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded normal(0,1))",
+        "config": {"workload": "real-input FFT, packed halfcomplex, f64: "
+                               f"{len(lengths)} lengths 2^a3^b5^c7^d11^e in [64,65536] + primes 1009/8191/65521, "
+                               "~2^24 reals per length, out of place",
+                   "lengths": lengths, "reals_per_step": int(bytes64 / 16),
+                   "l2": "inputs larger than L2 (128 MiB per length, 35 lengths per step)",
+                   "arith": "double-float butterflies on FP64 data"},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                     else "fallback 6.8 TB/s",
+                     "note": "achieved = algorithmic bytes of all lengths / sum of their event-timed call durations"},
+        "fp32": {"value": round(world * bytes32 / (ms32 / args.steps / 1e3) / 1e9, 2), "unit": "GB/s",
+                 "ms_per_step": round(ms32 / args.steps, 4),
+                 "speedup_vs_f64": round(ms64 / ms32, 3),
+                 "max_rel_l2_vs_f64": max(e for _, e in errs),
+                 "bound_1e-6_log2N": all(e <= 1e-6 * math.log2(n) for n, e in errs)},
+        "per_length_gbs": slow,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        gbs, nth, sample, _ = cpu_sample_run(lengths, min_seconds=args.cpu_seconds)
+        result["cpu_baseline"] = {"value": round(gbs, 3), "unit": "GB/s", "cores": nth, "kind": "port",
+                                  "sample": sample}
+    return result
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's algorithm on the host cores (the compiled
+    PocketFFT cannot travel to the GPU host, so the oracle port stands in)."""
+    if rank != 0:
+        return None
+    lengths = workload_lengths()
+    # warmup
+    for _ in range(args.warmup):
+        cpu_sample_run(lengths, min_seconds=0.0, max_passes=1)
+    vals = []
+    t0 = time.perf_counter()
+    sample = ""
+    nth = os.cpu_count() or 1
+    for _ in range(args.steps):
+        gbs, nth, sample, _ = cpu_sample_run(lengths, min_seconds=0.0, max_passes=1)
+        vals.append(gbs)
+    el = time.perf_counter() - t0
+    value = statistics.mean(vals)
+    return {
+        "metric": "FFT GB/s (halfcomplex real FFT, algorithmic bytes) vs HBM peak",
+        "impl": "reference",
+        "value": round(value, 3),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(el / args.steps * 1e3, 2),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded normal(0,1))",
+        "config": {"workload": "real-input FFT, packed halfcomplex, f64 (bounded CPU sample: 1/64 of each batch)",
+                   "lengths": lengths},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": nth, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        if args.warmup < 3:
+            args.warmup = 3
+        res = run_ours(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

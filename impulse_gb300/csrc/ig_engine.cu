@@ -272,10 +272,36 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
             c->d.chirpf = chf;
             c->n2 = L;
         } else {
-            raise(IG_ETOOLARGE, "Bluestein length beyond one CTA is not supported yet");
+            // Bluestein over a length-L core that itself runs as a four-step
+            c->kind = 2;
+            c->n2 = L;
+            c->sub = get_core(a, L, false);
+            void *ch, *chf;
+            build_chirp(*c, M, L, ch, chf);
+            c->chirp = ch;
+            c->chirpf = chf;
         }
     } else {
-        raise(IG_ETOOLARGE, "lengths beyond one CTA are not supported yet");
+        // four-step: M = N1 * N2, both run as shared-memory cores
+        long long best = 0;
+        for (long long d = 2; d * d <= M; ++d) {
+            if (M % d) continue;
+            std::vector<int> r1, r2;
+            if (gpu_factor(d, r1) && gpu_factor(M / d, r2) && fits_smem(a, d, d) && fits_smem(a, M / d, M / d))
+                best = d;
+        }
+        if (!best) raise(IG_ETOOLARGE, "no four-step split of this length fits the GPU kernels");
+        c->kind = 1;
+        c->N1 = best;
+        c->N2 = M / best;
+        c->c1 = get_core(a, c->N1, false);
+        c->c2 = get_core(a, c->N2, false);
+        void *whi = c->alloc(c->N1 * slot_bytes(a));
+        void *wlo = c->alloc(c->N2 * slot_bytes(a));
+        launch_roots_a(a, whi, c->N1, 1, (unsigned long long)c->N1);
+        launch_roots_a(a, wlo, c->N2, 1, (unsigned long long)M);
+        c->whi = whi;
+        c->wlo = wlo;
     }
     ck(cudaDeviceSynchronize(), "plan tables");
     return c;
@@ -343,11 +369,281 @@ static IODesc blank_io()
     return io;
 }
 
+// --------------------------------------------------------------------------
+// scratch for the multi-pass paths: per (device, stream), grow-only
+// --------------------------------------------------------------------------
+struct Scratch {
+    std::unique_ptr<DevBuf> buf[3];
+    void *get(int i, size_t bytes)
+    {
+        if (!buf[i] || buf[i]->bytes < bytes) {
+            buf[i].reset();
+            buf[i].reset(new DevBuf(bytes));
+        }
+        return buf[i]->p;
+    }
+};
+static std::mutex g_scr_mu;
+static std::map<std::pair<int, cudaStream_t>, std::unique_ptr<Scratch>> g_scratch;
+static Scratch &scratch_for(cudaStream_t st)
+{
+    std::lock_guard<std::mutex> lk(g_scr_mu);
+    auto &p = g_scratch[std::make_pair(device_id(), st)];
+    if (!p) p.reset(new Scratch);
+    return *p;
+}
+
+static void launch_map(Arith a, bool gather, const IODesc &io, const MapDesc &mp, cudaStream_t st)
+{
+    cudaError_t e;
+    if (gather)
+        e = a == A_F32 ? Launch<TagF32>::gather(io, mp, st)
+          : a == A_DF  ? Launch<TagDF>::gather(io, mp, st)
+                       : Launch<TagF64>::gather(io, mp, st);
+    else
+        e = a == A_F32 ? Launch<TagF32>::scatter(io, mp, st)
+          : a == A_DF  ? Launch<TagDF>::scatter(io, mp, st)
+                       : Launch<TagF64>::scatter(io, mp, st);
+    ck(e, gather ? "gather launch" : "scatter launch");
+    count_launch();
+}
+
+static void run_complex(const Core &c, const IODesc &io, cudaStream_t st);
+
+// contiguous scratch lines as an IODesc side
+static void contig_side(IODesc &io, bool out, char *base, long long es, long long len, long long nl)
+{
+    if (out) {
+        io.out = base;
+        io.os = es;
+        io.bso[0] = len * es;
+    } else {
+        io.in = (const char *)base;
+        io.is = es;
+        io.bsi[0] = len * es;
+    }
+    io.bn[0] = nl;
+    io.bn[1] = io.bn[2] = 1;
+    if (out) io.bso[1] = io.bso[2] = 0; else io.bsi[1] = io.bsi[2] = 0;
+}
+
+// Four-step over M = N1 * N2 (column FFTs of length N1 with the inter-pass
+// twiddle, then row FFTs of length N2 written transposed).  io describes
+// the user-facing sides with kinds IN_C/IN_R/IN_P and OUT_C/OUT_R/OUT_P and
+// at most two batch dims; `B` is a scratch of nlines * M complex elements.
+static void run_fourstep(const Core &c, const IODesc &io, char *B, cudaStream_t st)
+{
+    const long long N1 = c.N1, N2 = c.N2, M = c.M;
+    const long long ES = 2 * (long long)store_real_bytes(c.a);
+    const long long nl = io.nlines;
+    // pass 1: columns
+    IODesc p1 = io;
+    const long long ub_in = io.is;  // bytes between units
+    p1.nlines = nl * N2;
+    p1.bn[0] = N2;
+    p1.bsi[0] = ub_in;
+    p1.bn[1] = io.bn[0];
+    p1.bsi[1] = io.bsi[0];
+    p1.bn[2] = io.bn[1];
+    p1.bsi[2] = io.bsi[1];
+    p1.is = N2 * io.is;
+    p1.cnt_in = p1.cnt_out = (int)N1;
+    p1.out = B;
+    p1.out_kind = OUT_C;
+    p1.os = N2 * ES;
+    p1.bso[0] = ES;
+    p1.bso[1] = M * ES;
+    p1.bso[2] = M * ES * io.bn[0];
+    p1.pre = PRE_NONE;
+    p1.post = POST_NONE;
+    p1.conj_out = 0;
+    p1.real_out = 0;
+    p1.mul = nullptr;
+    p1.fct = 1.0;
+    p1.tw4 = 1;
+    p1.tw4N = M;
+    p1.tw4S = N2;
+    p1.tw4hi = c.whi;
+    p1.tw4lo = c.wlo;
+    p1.cols_in = 1;
+    p1.cols_out = 1;
+    launch_smem(c.a, c.c1->d, p1, st);
+    // pass 2: rows, transposed write
+    IODesc p2 = io;
+    const long long ub_out = io.os;
+    p2.in = B;
+    p2.in_kind = IN_C;
+    p2.conj_in = 0;
+    p2.is = ES;
+    p2.nlines = nl * N1;
+    p2.bn[0] = N1;
+    p2.bsi[0] = N2 * ES;
+    p2.bn[1] = io.bn[0];
+    p2.bsi[1] = M * ES;
+    p2.bn[2] = io.bn[1];
+    p2.bsi[2] = M * ES * io.bn[0];
+    p2.bso[0] = ub_out;
+    p2.bso[1] = io.bso[0];
+    p2.bso[2] = io.bso[1];
+    p2.os = N1 * io.os;
+    p2.cnt_in = p2.cnt_out = (int)N2;
+    p2.pre = PRE_NONE;
+    p2.post = POST_NONE;
+    p2.tw4 = 0;
+    p2.cols_in = 0;
+    p2.cols_out = 1;
+    if (io.mul) {
+        p2.mul_a = 1;
+        p2.mul_b = N1;
+    }
+    launch_smem(c.a, c.c2->d, p2, st);
+}
+
+// Run a complex core of any kind.  io: user-facing sides, kinds, pre/post,
+// conj flags and fct, as for the shared-memory kernel.
+static void run_complex(const Core &c, const IODesc &io_all, cudaStream_t st)
+{
+    if (io_all.nlines <= 0) return;
+    if (c.kind == 0) {
+        launch_smem(c.a, c.d, io_all, st);
+        return;
+    }
+    // at most two batch dims on the user side per multi-pass run
+    for (long long i2 = 0; i2 < io_all.bn[2]; ++i2) {
+        IODesc io = io_all;
+        io.in += i2 * io_all.bsi[2];
+        io.out += i2 * io_all.bso[2];
+        io.bn[2] = 1;
+        io.bsi[2] = io.bso[2] = 0;
+        io.nlines = io.bn[0] * io.bn[1];
+        const long long nl = io.nlines;
+        const long long ES = 2 * (long long)store_real_bytes(c.a);
+        Scratch &scr = scratch_for(st);
+        if (c.kind == 1) {
+            const long long M = c.M;
+            bool gath = io.pre != PRE_NONE || io.in_kind == IN_HC;
+            bool scat = io.post != POST_NONE || io.out_kind == OUT_HC || io.cnt_out != (int)M || io.real_out;
+            char *B = (char *)scr.get(1, (size_t)(nl * M * ES));
+            // scratch lines keep the user's (bn0, bn1) line numbering: line l at l * M * ES
+            IODesc f = io;
+            if (gath) {
+                char *A = (char *)scr.get(0, (size_t)(nl * M * ES));
+                MapDesc mp{};
+                mp.kind = io.pre == PRE_HERM_EVEN ? MAP_HERM_EVEN : MAP_PLAIN;
+                mp.M = M;
+                mp.scr_len = M;
+                mp.scr = A;
+                mp.rtw = c.rtw;
+                launch_map(c.a, true, io, mp, st);
+                f.in = A;
+                f.is = ES;
+                f.bsi[0] = M * ES;
+                f.bsi[1] = M * ES * io.bn[0];
+                f.in_kind = IN_C;
+                f.conj_in = 0;
+                f.pre = PRE_NONE;
+                f.cnt_in = (int)M;
+            }
+            if (scat) {
+                char *C = (char *)scr.get(2, (size_t)(nl * M * ES));
+                f.out = C;
+                f.os = ES;
+                f.bso[0] = M * ES;
+                f.bso[1] = M * ES * io.bn[0];
+                f.out_kind = OUT_C;
+                f.conj_out = 0;
+                f.real_out = 0;
+                f.post = POST_NONE;
+                f.fct = 1.0;
+                f.cnt_out = (int)M;
+                run_fourstep(c, f, B, st);
+                MapDesc mp{};
+                mp.kind = io.post == POST_SPLIT ? MAP_SPLIT_EVEN : MAP_PLAIN;
+                mp.M = M;
+                mp.scr_len = M;
+                mp.scr = C;
+                mp.rtw = c.rtw;
+                IODesc h = io;
+                h.pre = PRE_NONE;
+                launch_map(c.a, false, h, mp, st);
+            } else {
+                run_fourstep(c, f, B, st);
+            }
+        } else {
+            // Bluestein over a (four-step) core of length n2
+            const long long M = c.M, L = c.n2;
+            char *A = (char *)scr.get(0, (size_t)(nl * L * ES));
+            IODesc src = io;
+            if (io.pre == PRE_HERM_EVEN) {
+                char *C = (char *)scr.get(2, (size_t)(nl * M * ES));
+                MapDesc mp{};
+                mp.kind = MAP_HERM_EVEN;
+                mp.M = M;
+                mp.scr_len = M;
+                mp.scr = C;
+                mp.rtw = c.rtw;
+                launch_map(c.a, true, io, mp, st);
+                contig_side(src, false, C, ES, M, nl);
+                src.in_kind = IN_C;
+                src.conj_in = 0;
+                src.pre = PRE_NONE;
+                src.cnt_in = (int)M;
+            }
+            MapDesc mp{};
+            mp.kind = MAP_BLUE;
+            mp.M = M;
+            mp.scr_len = L;
+            mp.scr = A;
+            mp.chirp = c.chirp;
+            mp.fwd = io.fwd;
+            launch_map(c.a, true, src, mp, st);
+            // forward FFT_L with the chirp-spectrum product, backward FFT_L, in place in A
+            for (int pass = 0; pass < 2; ++pass) {
+                IODesc q = blank_io();
+                contig_side(q, false, A, ES, L, nl);
+                contig_side(q, true, A, ES, L, nl);
+                q.nlines = nl;
+                q.in_kind = IN_C;
+                q.out_kind = OUT_C;
+                q.cnt_in = q.cnt_out = (int)L;
+                q.fwd = pass == 0 ? 1 : 0;
+                if (pass == 0) {
+                    q.mul = c.chirpf;
+                    q.mul_a = 0;
+                    q.mul_b = 1;
+                    q.mul_conj = io.fwd ? 0 : 1;
+                }
+                run_complex(*c.sub, q, st);
+            }
+            IODesc h = io;
+            h.pre = PRE_NONE;
+            if (io.post == POST_SPLIT) {
+                char *C = (char *)scr.get(2, (size_t)(nl * M * ES));
+                IODesc g = blank_io();
+                contig_side(g, true, C, ES, M, nl);
+                g.nlines = nl;
+                g.out_kind = OUT_C;
+                g.cnt_out = (int)M;
+                MapDesc mb = mp;
+                launch_map(c.a, false, g, mb, st);
+                MapDesc ms{};
+                ms.kind = MAP_SPLIT_EVEN;
+                ms.M = M;
+                ms.scr_len = M;
+                ms.scr = C;
+                ms.rtw = c.rtw;
+                launch_map(c.a, false, h, ms, st);
+            } else {
+                launch_map(c.a, false, h, mp, st);
+            }
+        }
+    }
+}
+
 // contiguous batch of complex lines of length M (used for table building)
 static void run_core_on_device(const Core &c, const void *in, void *out, long long batch, int fwd, double fct,
                                cudaStream_t st)
 {
-    if (c.kind != 0) raise(IG_ETOOLARGE, "core kind not supported");
     IODesc io = blank_io();
     size_t sb = 2 * store_real_bytes(c.a);
     io.in = (const char *)in;
@@ -361,7 +657,7 @@ static void run_core_on_device(const Core &c, const void *in, void *out, long lo
     io.cnt_in = io.cnt_out = (int)c.M;
     io.fwd = fwd;
     io.fct = fct;
-    launch_smem(c.a, c.d, io, st);
+    run_complex(c, io, st);
 }
 
 // --------------------------------------------------------------------------
@@ -421,8 +717,12 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
         if (even && ln.es_in == sr) {
             io.in_kind = IN_C;  // contiguous reals read as complex pairs
             io.is = 2 * sr;
+        } else if (even) {
+            io.in_kind = IN_P;
+            io.is = 2 * ln.es_in;
+            io.ps_in = ln.es_in;
         } else {
-            io.in_kind = even ? IN_P : IN_R;
+            io.in_kind = IN_R;
         }
         io.cnt_in = (int)M;
         io.post = even ? POST_SPLIT : POST_NONE;
@@ -452,6 +752,8 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
                 io.os = 2 * sr;
             } else {
                 io.out_kind = OUT_P;
+                io.os = 2 * ln.es_out;
+                io.ps_out = ln.es_out;
             }
             io.cnt_out = (int)M;
         } else {
@@ -480,12 +782,11 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
         io.cnt_in = 1;
     }
     // coalescing mode: lines adjacent in memory and elements strided
-    long long ue_in = io.in_kind == IN_C ? 2 * sr : sr;
-    long long ue_out = (io.out_kind == OUT_C) ? 2 * sr : sr;
+    long long ue_in = (io.in_kind == IN_C || io.in_kind == IN_P) ? 2 * sr : sr;
+    long long ue_out = (io.out_kind == OUT_C || io.out_kind == OUT_P) ? 2 * sr : sr;
     io.cols_in = (ln.bn[0] > 1 && std::llabs(ln.bsi[0]) <= ue_in && std::llabs(io.is) > ue_in) ? 1 : 0;
     io.cols_out = (ln.bn[0] > 1 && std::llabs(ln.bso[0]) <= ue_out && std::llabs(io.os) > ue_out) ? 1 : 0;
-    if (core->kind != 0) raise(IG_ETOOLARGE, "multi-pass cores are not wired yet");
-    launch_smem(a, core->d, io, st);
+    run_complex(*core, io, st);
 }
 
 // --------------------------------------------------------------------------

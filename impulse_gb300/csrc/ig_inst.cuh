@@ -51,4 +51,22 @@ template <class Tag> cudaError_t Launch<Tag>::convert64(const void *in, void *ou
     return cudaGetLastError();
 }
 
+static inline unsigned map_grid(long long total)
+{
+    long long g = (total + 255) / 256;
+    return (unsigned)(g < 152LL * 32 ? (g > 0 ? g : 1) : 152LL * 32);
+}
+template <class Tag> cudaError_t Launch<Tag>::gather(const IODesc &io, const MapDesc &mp, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_gather<T><<<map_grid(io.nlines * mp.scr_len), 256, 0, st>>>(io, mp);
+    return cudaGetLastError();
+}
+template <class Tag> cudaError_t Launch<Tag>::scatter(const IODesc &io, const MapDesc &mp, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_scatter<T><<<map_grid(io.nlines * (long long)io.cnt_out), 256, 0, st>>>(io, mp);
+    return cudaGetLastError();
+}
+
 }  // namespace ig

@@ -196,8 +196,8 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
                     re = *reinterpret_cast<const S *>(base + u * io.is);
                     im = 0;
                 } else if (io.in_kind == IN_P) {
-                    re = *reinterpret_cast<const S *>(base + (2 * (long long)u) * io.is);
-                    im = *reinterpret_cast<const S *>(base + (2 * (long long)u + 1) * io.is);
+                    re = *reinterpret_cast<const S *>(base + u * io.is);
+                    im = *reinterpret_cast<const S *>(base + u * io.is + io.ps_in);
                 } else {  // IN_HC: unit 0 = (r0, 0); unit k = (r_{2k-1}, r_{2k}); even N: last = (r_{N-1}, 0)
                     if (u == 0) { re = *reinterpret_cast<const S *>(base); im = 0; }
                     else {
@@ -388,6 +388,11 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
                     cx<T> w = cmul(whi[hi], wlo[lo]);
                     z = io.fwd ? cmul(z, w) : cmulc(z, w);
                 }
+                if (io.mul) {
+                    const cx<T> *mt = reinterpret_cast<const cx<T> *>(io.mul);
+                    cx<T> w = mt[(l % io.bn[0]) * io.mul_a + (long long)u * io.mul_b];
+                    z = io.mul_conj ? cmulc(z, w) : cmul(z, w);
+                }
                 if (io.conj_out) z.i = -z.i;
                 // general_r2c stores the DC and Nyquist bins with a zero imaginary part
                 if (io.real_out && (u == 0 || (io.post == POST_SPLIT && u == M))) z.i = RealOps<T>::k(0.0);
@@ -399,8 +404,8 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
                 } else if (io.out_kind == OUT_R) {
                     *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
                 } else if (io.out_kind == OUT_P) {
-                    *reinterpret_cast<S *>(base + (2 * (long long)u) * io.os) = sc.apply(z.r, esc);
-                    *reinterpret_cast<S *>(base + (2 * (long long)u + 1) * io.os) = sc.apply(z.i, esc);
+                    *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
+                    *reinterpret_cast<S *>(base + u * io.os + io.ps_out) = sc.apply(z.i, esc);
                 } else {  // OUT_HC
                     if (u == 0) *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
                     else {
@@ -415,6 +420,179 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// elementwise line maps of the multi-pass paths
+// ---------------------------------------------------------------------------
+
+// double-float helpers with a shared power-of-two scale per small group of
+// values (exact), so that elementwise steps keep ~48-bit accuracy for any
+// finite magnitude without FP64 arithmetic
+template <class T> struct Loc {
+    int esc = 0;
+    __device__ void fit(double a, double b, double c = 0.0, double d = 0.0) {}
+    __device__ cx<T> in(double re, double im) const { return cx<T>{(T)re, (T)im}; }
+    __device__ double out(T v) const { return (double)v; }
+};
+template <> struct Loc<df> {
+    int esc = 0;
+    __device__ void fit(double a, double b, double c = 0.0, double d = 0.0)
+    {
+        int e = max(max(dexp(a), dexp(b)), max(dexp(c), dexp(d)));
+        esc = e > 0 ? 1023 - e : 0;
+    }
+    __device__ cx<df> in(double re, double im) const { return cx<df>{df_from_double(re, esc), df_from_double(im, esc)}; }
+    __device__ double out(df v) const { return df_to_double(v, esc); }
+};
+
+// read unit u of the user-facing input line at `base` (kinds of IODesc)
+template <class S, class S2>
+__device__ __forceinline__ void read_unit(const IODesc &io, const char *base, long long u, double &re, double &im)
+{
+    if (io.in_kind == IN_C) {
+        S2 z = *reinterpret_cast<const S2 *>(base + u * io.is);
+        re = z.x; im = z.y;
+    } else if (io.in_kind == IN_R) {
+        re = *reinterpret_cast<const S *>(base + u * io.is);
+        im = 0;
+    } else if (io.in_kind == IN_P) {
+        re = *reinterpret_cast<const S *>(base + u * io.is);
+        im = *reinterpret_cast<const S *>(base + u * io.is + io.ps_in);
+    } else {
+        if (u == 0) { re = *reinterpret_cast<const S *>(base); im = 0; }
+        else {
+            re = *reinterpret_cast<const S *>(base + (2 * u - 1) * io.is);
+            im = (2 * u < io.nreal) ? (double)*reinterpret_cast<const S *>(base + (2 * u) * io.is) : 0.0;
+        }
+    }
+    if (io.conj_in) im = -im;
+}
+
+// gather: user input -> scratch lines (one thread per scratch element)
+template <class T>
+__global__ void k_gather(const __grid_constant__ IODesc io, const __grid_constant__ MapDesc mp)
+{
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    const long long total = io.nlines * mp.scr_len;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        long long l = idx / mp.scr_len, u = idx - l * mp.scr_len;
+        const char *base = io.in + line_off(io, l, false);
+        S2 *dst = reinterpret_cast<S2 *>(mp.scr) + l * mp.scr_len + u;
+        double re = 0, im = 0;
+        if (mp.kind == MAP_HERM_EVEN) {
+            // Z[k] = (X[k] + conj(X[M-k])) + i e^{+2 pi i k/2M} (X[k] - conj(X[M-k])), k < M
+            if (u >= mp.M) continue;
+            double ar, ai, br, bi;
+            read_unit<S, S2>(io, base, u, ar, ai);
+            read_unit<S, S2>(io, base, mp.M - u, br, bi);
+            if (u == 0) ai = 0;
+            if (mp.M - u == mp.M || mp.M - u == 0) bi = 0;
+            Loc<T> lc;
+            lc.fit(ar, ai, br, bi);
+            cx<T> xa = lc.in(ar, ai), xb = lc.in(br, -bi);
+            cx<T> A = xa + xb, Bv = xa - xb;
+            cx<T> w = conjx(reinterpret_cast<const cx<T> *>(mp.rtw)[u]);
+            cx<T> tB = cmul(Bv, w);
+            cx<T> z = cx<T>{A.r - tB.i, A.i + tB.r};
+            S2 o;
+            o.x = (S)lc.out(z.r);
+            o.y = (S)lc.out(z.i);
+            *dst = o;
+            continue;
+        }
+        long long cnt = io.cnt_in;
+        if (u < mp.M) {
+            long long uu = u;
+            bool cj = false;
+            if (io.pre == PRE_HERM_ODD && u >= cnt) { uu = mp.M - u; cj = true; }
+            if (uu < cnt) {
+                read_unit<S, S2>(io, base, uu, re, im);
+                if (io.pre != PRE_NONE && uu == 0) im = 0;
+                if (cj) im = -im;
+            }
+        }
+        if (mp.kind == MAP_BLUE) {
+            if (u < mp.M) {
+                Loc<T> lc;
+                lc.fit(re, im);
+                cx<T> x = lc.in(re, im);
+                cx<T> c = reinterpret_cast<const cx<T> *>(mp.chirp)[u];
+                x = mp.fwd ? cmulc(x, c) : cmul(x, c);
+                re = lc.out(x.r);
+                im = lc.out(x.i);
+            } else {
+                re = im = 0;
+            }
+        }
+        S2 o;
+        o.x = (S)re;
+        o.y = (S)im;
+        *dst = o;
+    }
+}
+
+// scatter: scratch lines -> user output (one thread per output unit)
+template <class T>
+__global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_constant__ MapDesc mp)
+{
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    const long long cnt = io.cnt_out;
+    const long long total = io.nlines * cnt;
+    OutScale<T> sc;
+    sc.init(io.fct);
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        long long l = idx / cnt, u = idx - l * cnt;
+        char *base = io.out + line_off(io, l, true);
+        const S2 *src = reinterpret_cast<const S2 *>(mp.scr) + l * mp.scr_len;
+        cx<T> z;
+        Loc<T> lc;
+        if (mp.kind == MAP_SPLIT_EVEN) {
+            // X[k] = E_k + w^k O_k from Z[k], Z[M-k] (k <= M, Z[M] = Z[0])
+            long long M = mp.M;
+            S2 a = src[u % M], b = src[(M - u) % M];
+            lc.fit(a.x, a.y, b.x, b.y);
+            cx<T> za = lc.in(a.x, a.y), zb = conjx(lc.in(b.x, b.y));
+            constexpr T half = RealOps<T>::k(0.5);
+            cx<T> E = cscale(za + zb, half);
+            cx<T> D = cscale(za - zb, half);
+            cx<T> O = cx<T>{D.i, -D.r};
+            z = E + cmul(O, reinterpret_cast<const cx<T> *>(mp.rtw)[u]);
+        } else {
+            S2 a = src[u];
+            lc.fit(a.x, a.y);
+            z = lc.in(a.x, a.y);
+            if (mp.kind == MAP_BLUE) {
+                cx<T> c = reinterpret_cast<const cx<T> *>(mp.chirp)[u];
+                z = mp.fwd ? cmulc(z, c) : cmul(z, c);
+            }
+        }
+        if (io.conj_out) z.i = -z.i;
+        if (io.real_out && (u == 0 || (mp.kind == MAP_SPLIT_EVEN && u == mp.M))) z.i = RealOps<T>::k(0.0);
+        // OutScale folds the group's scale back in: esc of the output conversion
+        const int esc = lc.esc;
+        if (io.out_kind == OUT_C) {
+            S2 o;
+            o.x = sc.apply(z.r, esc);
+            o.y = sc.apply(z.i, esc);
+            *reinterpret_cast<S2 *>(base + u * io.os) = o;
+        } else if (io.out_kind == OUT_R) {
+            *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
+        } else if (io.out_kind == OUT_P) {
+            *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
+            *reinterpret_cast<S *>(base + u * io.os + io.ps_out) = sc.apply(z.i, esc);
+        } else {
+            if (u == 0) *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
+            else {
+                *reinterpret_cast<S *>(base + (2 * u - 1) * io.os) = sc.apply(z.r, esc);
+                if (2 * u < io.nreal) *reinterpret_cast<S *>(base + (2 * u) * io.os) = sc.apply(z.i, esc);
+            }
+        }
+    }
+}
 
 // ---------------------------------------------------------------------------
 // table builders (FP64, exact integer angle reduction, CUDA's sincospi)

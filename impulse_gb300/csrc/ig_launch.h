@@ -20,6 +20,8 @@ template <class Tag> struct Launch {
     static cudaError_t stage_tw(void *tw, int R, int ns);
     static cudaError_t roots(void *out, long long count, unsigned long long mult, unsigned long long D);
     static cudaError_t convert64(const void *in, void *out, long long n);
+    static cudaError_t gather(const IODesc &io, const MapDesc &mp, cudaStream_t st);
+    static cudaError_t scatter(const IODesc &io, const MapDesc &mp, cudaStream_t st);
 };
 
 // FP64 helpers for Bluestein tables (built in ig_inst_df.cu)

@@ -33,6 +33,7 @@ struct IODesc {
     const char *in;
     char *out;
     long long is, os;       // byte stride along the line (between storage units of the kind)
+    long long ps_in, ps_out;  // IN_P / OUT_P: bytes from a unit's real value to its second real
     long long nlines;
     long long bn[3];        // batch dims: line l -> (l % bn0, (l / bn0) % bn1, l / (bn0 bn1))
     long long bsi[3], bso[3];
@@ -50,6 +51,30 @@ struct IODesc {
     int tw4;
     long long tw4N, tw4S;
     const void *tw4hi, *tw4lo;
+    // pointwise product on output unit u of line l with tab[(l % bn0) * mul_a + u * mul_b]
+    // (conjugated when mul_conj); Bluestein's convolution step on a four-step core
+    const void *mul;
+    long long mul_a, mul_b;
+    int mul_conj;
+};
+
+// Elementwise line maps of the multi-pass paths (k_gather / k_scatter).
+// `ext` is the user-facing side (IODesc fields in/out, is/os, bn/bsi/bso,
+// kinds, conj, nreal); `scr` is a scratch array of contiguous complex lines.
+enum MapKind {
+    MAP_PLAIN = 0,      // unit u <-> scratch[u]
+    MAP_BLUE = 1,       // times chirp (Bluestein pre / post); gather zero-pads to scr_len
+    MAP_HERM_EVEN = 2,  // gather: halfcomplex X[0..M] -> Z[0..M) (inverse of the real split)
+    MAP_SPLIT_EVEN = 3, // scatter: Z[0..M) -> X[0..M] (real split), written as halfcomplex or half spectrum
+};
+struct MapDesc {
+    int kind;
+    long long M;        // complex units per line on the scratch side
+    long long scr_len;  // scratch line length (elements)
+    char *scr;          // scratch base (storage complex)
+    const void *chirp;  // cx<T>, MAP_BLUE
+    const void *rtw;    // cx<T> exp(-2 pi i k/2M), k <= M, real split
+    int fwd;            // Bluestein direction
 };
 
 

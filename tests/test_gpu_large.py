@@ -1,0 +1,63 @@
+"""GPU parity for lengths beyond one CTA's shared memory: four-step cores and
+Bluestein over a four-step core (lengths with a large prime factor)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-12
+
+
+def f32_tol(n):
+    return 1e-6 * max(1.0, np.log2(max(n, 2)))
+
+
+@pytest.mark.parametrize("n", [8191, 9973, 10000, 12288, 16384, 32768, 65521, 65536, 131072, 1 << 20])
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_cfft_large(engine, oracle_lib, n, dtype):
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(n)
+    b = 2 if n <= 131072 else 1
+    x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))).astype(dtype)
+    tol = F64_TOL if dtype == np.complex128 else f32_tol(n) * 2
+    for fwd in (True, False):
+        got = F.cfft_batch(x, forward=fwd, fct=0.5)
+        want = oracle_lib.cfft(x.astype(np.complex128), forward=fwd, fct=0.5)
+        assert oracle_lib.rel_l2(got, want) < tol, (n, fwd, oracle_lib.rel_l2(got, want))
+
+
+@pytest.mark.parametrize("n", [16382, 16386, 19998, 20000, 32768, 40960, 65521, 65536, 8191 * 3])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_rfft_halfcomplex_large(engine, oracle_lib, n, dtype):
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(n + 1)
+    x = rng.standard_normal((2, n)).astype(dtype)
+    tol = F64_TOL if dtype == np.float64 else f32_tol(n) * 2
+    hc = F.rfft_batch(x, forward=True, fct=1.0)
+    want = oracle_lib.rfft_hc(x.astype(np.float64), forward=True)
+    assert oracle_lib.rel_l2(hc, want) < tol, (n, oracle_lib.rel_l2(hc, want))
+    back = F.rfft_batch(hc, forward=False, fct=1.0 / n)
+    assert oracle_lib.rel_l2(back, x.astype(np.float64)) < 2 * tol, n
+
+
+@pytest.mark.parametrize("shape,axes", [((3, 40000), [1]), ((2, 3, 65521), [2]), ((20000, 3), [0]),
+                                        ((4, 16384), [0, 1])])
+def test_r2c_c2r_large(engine, oracle_lib, shape, axes):
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(sum(shape))
+    x = rng.uniform(-1, 1, shape)
+    for fwd in (True, False):
+        got = F.r2c(x, axes, forward=fwd)
+        want = oracle_lib.r2c(x, axes, forward=fwd)
+        assert oracle_lib.rel_l2(got, want) < F64_TOL, (shape, axes, fwd)
+        back = F.c2r(got, shape, axes, forward=fwd, fct=0.5)
+        want_b = oracle_lib.c2r(want, shape, axes, forward=fwd, fct=0.5)
+        assert oracle_lib.rel_l2(back, want_b) < F64_TOL, (shape, axes, fwd)
+
+
+def test_c2c_large_strided_axis(engine, oracle_lib):
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, (32768, 4)) + 1j * rng.uniform(-1, 1, (32768, 4))
+    got = F.c2c(x, [0], True, 1.0)
+    assert oracle_lib.rel_l2(got, oracle_lib.c2c(x, [0])) < F64_TOL
