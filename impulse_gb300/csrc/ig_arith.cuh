@@ -169,7 +169,14 @@ IGD df df_from_double(double x, int escale = 0)
     int el = e - 1023 - 52 + 127;  // biased exponent of the scale factor
     float l = 0.0f;
     if (el >= 1 && r) {
-        float lf = (float)r;  // rounded to 24 bits
+        // int -> float without a conversion instruction (those issue on
+        // GB300's narrow FP64 pipe): two exact magic-number conversions of
+        // 15-bit pieces, joined by one correctly rounded FMA
+        int32_t rh = r >> 15;                 // |rh| <= 2^13
+        int32_t rl = r & 0x7fff;              // 0 .. 32767
+        float fh = IG_FSUB(u2f(0x4B400000u + (uint32_t)rh), 12582912.0f);
+        float fl = IG_FSUB(u2f(0x4B000000u + (uint32_t)rl), 8388608.0f);
+        float lf = IG_FMA(fh, 32768.0f, fl);
         l = IG_FMUL(lf, u2f((uint32_t)el << 23));
         if (sign) l = -l;
     }
@@ -235,6 +242,9 @@ IGD double df_to_double(df v, int escale = 0)
     if (ed <= 0) return u2d(sgn);
     return u2d(sgn | ((uint64_t)ed << 52) | (M & 0xfffffffffffffull));
 }
+
+// sign flip of a double through its bit pattern (no FP64 instruction)
+IGD double dneg(double x) { return u2d(d2u(x) ^ 0x8000000000000000ull); }
 
 // ---------------------------------------------------------------------------
 // generic real helpers: constants, scale by power of two

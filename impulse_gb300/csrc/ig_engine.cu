@@ -186,16 +186,107 @@ static constexpr int kMaxThreads = 512;
 // smem slots a core of Stockham length L needs per line
 static long long smem_slots(long long L, long long M) { return std::max(L, M + 1); }
 
+static int elems_per_thread(long long L) { return L <= 4096 ? 8 : 16; }
+
 static bool fits_smem(Arith a, long long L, long long M)
 {
-    long long tpl = (L + kE - 1) / kE;
+    long long tpl = (L + kEMax - 1) / kEMax;
     if (tpl > kMaxThreads) return false;
-    return smem_slots(L, M) * (long long)slot_bytes(a) <= (long long)max_smem();
+    long long slots = smem_slots(L, M);
+    slots += slots >> 3;  // worst-case padding
+    return slots * (long long)slot_bytes(a) <= (long long)max_smem();
 }
 
 struct Exec;
 static void run_core_on_device(const Core &c, const void *in, void *out, long long batch, int fwd, double fct,
                                cudaStream_t st);
+
+static FastDiv make_fdiv(unsigned d)
+{
+    int lg = 0;
+    while ((1ull << lg) < d) ++lg;
+    FastDiv f;
+    f.s = 31 + lg;
+    f.m = (unsigned)(((1ull << f.s) + d - 1) / d);
+    return f;
+}
+
+// line-number decomposition of the kernels uses 32-bit fast division
+static void set_line_divs(IODesc &io)
+{
+    if (io.nlines >= (1LL << 31) || io.bn[0] >= (1LL << 31) || io.bn[1] >= (1LL << 31))
+        raise(IG_ETOOLARGE, "more than 2^31 lines in one launch");
+    io.fb0 = make_fdiv((unsigned)std::max<long long>(1, io.bn[0]));
+    io.fb1 = make_fdiv((unsigned)std::max<long long>(1, io.bn[1]));
+}
+
+// shared-memory wavefronts of one warp-wide access (quarter-warp phases for
+// 16-byte slots, half-warp phases for 8-byte slots)
+static int wavefronts(const int *addr, int n, int slot)
+{
+    const int group = slot == 16 ? 8 : 16, nslot = group;
+    int tot = 0;
+    for (int q = 0; q < n; q += group) {
+        int cnt[16] = {0}, worst = 0;
+        for (int a = q; a < std::min(n, q + group); ++a) {
+            bool dup = false;
+            for (int b = q; b < a; ++b) dup |= addr[b] == addr[a];
+            if (dup) continue;
+            int c = ++cnt[addr[a] % nslot];
+            worst = std::max(worst, c);
+        }
+        tot += worst;
+    }
+    return tot;
+}
+
+// pick the padding shift (i -> i + (i >> pad)) with the fewest simulated
+// shared-memory wavefronts over the stages of the first warp
+static int choose_pad(const CoreDesc &d, int slot)
+{
+    const int L = d.L;
+    const int tpl = (L + d.E - 1) / d.E;
+    int best_pad = 31;
+    long long best = -1;
+    for (int pad : {31, 5, 4, 3}) {
+        long long cost = 0;
+        for (int s = 0; s < d.nst; ++s) {
+            const int R = d.st[s].R, ns = d.st[s].ns, nr = L / R;
+            int la[32], sa[32];
+            for (int w = 0; w < std::min(tpl, 64); w += 32) {
+                int n = 0;
+                for (int l = 0; l < 32; ++l) {
+                    int j = w + l;
+                    if (j >= nr || j >= tpl) break;
+                    ++n;
+                }
+                if (!n) continue;
+                for (int m = 0; m < R; ++m) {
+                    for (int l = 0; l < n; ++l) {
+                        int j = w + l;
+                        int a = j + m * nr, b = (j / ns) * ns * R + (j % ns) + m * ns;
+                        la[l] = a + (a >> pad);
+                        sa[l] = b + (b >> pad);
+                    }
+                    cost += wavefronts(la, n, slot) + wavefronts(sa, n, slot);
+                }
+            }
+        }
+        if (best < 0 || cost < best) {
+            best = cost;
+            best_pad = pad;
+        }
+    }
+    return best_pad;
+}
+
+static void finish_layout(Core &c, long long L, long long M)
+{
+    c.d.E = elems_per_thread(L);
+    c.d.pad = choose_pad(c.d, (int)slot_bytes(c.a));
+    long long last = std::max(L, M + 1) - 1;
+    c.d.LS = (int)(last + (last >> c.d.pad) + 1);
+}
 
 static void build_stockham(Core &c, long long L, const std::vector<int> &rad)
 {
@@ -207,6 +298,7 @@ static void build_stockham(Core &c, long long L, const std::vector<int> &rad)
         c.d.st[s].R = rad[s];
         c.d.st[s].ns = (int)ns;
         c.d.st[s].tw = (int)off;
+        c.d.st[s].fns = make_fdiv((unsigned)ns);
         off += ns * (rad[s] - 1);
         ns *= rad[s];
     }
@@ -255,8 +347,8 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
     if (smooth && fits_smem(a, M, M)) {
         c->kind = 0;
         build_stockham(*c, M, rad);
-        c->d.LS = (int)smem_slots(M, M);
         c->d.blue = 0;
+        finish_layout(*c, M, M);
     } else if (!smooth) {
         long long L = good_size_gpu(2 * M - 1);
         std::vector<int> radL;
@@ -265,7 +357,7 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
             c->kind = 0;
             c->d.blue = 1;
             build_stockham(*c, L, radL);
-            c->d.LS = (int)smem_slots(L, M);
+            finish_layout(*c, L, M);
             void *ch, *chf;
             build_chirp(*c, M, L, ch, chf);
             c->d.chirp = ch;
@@ -329,7 +421,7 @@ static std::shared_ptr<Core> get_core(Arith a, long long M, bool real_tw)
 static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
 {
     if (io.nlines <= 0) return;
-    const long long tpl = (d.L + kE - 1) / kE;
+    const long long tpl = (d.L + d.E - 1) / d.E;
     const long long line_bytes = (long long)d.LS * (long long)slot_bytes(a);
     const int smax = max_smem();
     long long lpc = std::max<long long>(1, 256 / tpl);
@@ -342,6 +434,7 @@ static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
     lpc = std::min<long long>(lpc, std::max<long long>(1, io.nlines));
     io.lpc = (int)lpc;
     io.tpl = (int)tpl;
+    set_line_divs(io);
     size_t smem = (size_t)(lpc * line_bytes);
     static std::once_flag once[3];
     std::call_once(once[a], [&] {
@@ -393,8 +486,10 @@ static Scratch &scratch_for(cudaStream_t st)
     return *p;
 }
 
-static void launch_map(Arith a, bool gather, const IODesc &io, const MapDesc &mp, cudaStream_t st)
+static void launch_map(Arith a, bool gather, const IODesc &io_in, const MapDesc &mp, cudaStream_t st)
 {
+    IODesc io = io_in;
+    set_line_divs(io);
     cudaError_t e;
     if (gather)
         e = a == A_F32 ? Launch<TagF32>::gather(io, mp, st)
@@ -463,6 +558,7 @@ static void run_fourstep(const Core &c, const IODesc &io, char *B, cudaStream_t 
     p1.tw4 = 1;
     p1.tw4N = M;
     p1.tw4S = N2;
+    p1.fdS = make_fdiv((unsigned)N2);
     p1.tw4hi = c.whi;
     p1.tw4lo = c.wlo;
     p1.cols_in = 1;

@@ -14,7 +14,8 @@ template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const 
 {
     using T = typename TagType<Tag>::T;
     long long grid = (io.nlines + io.lpc - 1) / io.lpc;
-    k_fft_smem<T><<<(unsigned)grid, (unsigned)(io.lpc * io.tpl), smem, st>>>(d, io);
+    if (d.E == 8) k_fft_smem<T, 8><<<(unsigned)grid, (unsigned)(io.lpc * io.tpl), smem, st>>>(d, io);
+    else k_fft_smem<T, 16><<<(unsigned)grid, (unsigned)(io.lpc * io.tpl), smem, st>>>(d, io);
     return cudaGetLastError();
 }
 template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
@@ -22,9 +23,14 @@ template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
     using T = typename TagType<Tag>::T;
     // the dynamic limit excludes the kernel's static shared memory
     cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, k_fft_smem<T>);
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_fft_smem<T, 8>);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_fft_smem<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_fft_smem<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bytes - (int)fa.sharedSizeBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncGetAttributes(&fa, k_fft_smem<T, 16>);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_fft_smem<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 bytes - (int)fa.sharedSizeBytes);
 }
 template <class Tag> cudaError_t Launch<Tag>::stage_tw(void *tw, int R, int ns)

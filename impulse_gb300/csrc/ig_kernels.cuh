@@ -44,14 +44,26 @@ template <> struct Traits<df> {
     static constexpr bool kRaw = true;  // prologue stages raw doubles, first reader converts
 };
 
+__device__ __forceinline__ unsigned fdiv(unsigned n, FastDiv f)
+{
+    return (unsigned)(((unsigned long long)n * f.m) >> f.s);
+}
+
+// byte offset of line l: l -> (l mod bn0, (l / bn0) mod bn1, l / (bn0 bn1))
 __device__ __forceinline__ long long line_off(const IODesc &io, long long l, bool out)
 {
-    long long i0 = l % io.bn[0];
-    long long r = l / io.bn[0];
-    long long i1 = r % io.bn[1];
-    long long i2 = r / io.bn[1];
-    return out ? i0 * io.bso[0] + i1 * io.bso[1] + i2 * io.bso[2]
-               : i0 * io.bsi[0] + i1 * io.bsi[1] + i2 * io.bsi[2];
+    const unsigned lu = (unsigned)l;
+    const unsigned q0 = fdiv(lu, io.fb0);
+    const unsigned i0 = lu - q0 * (unsigned)io.bn[0];
+    const unsigned q1 = fdiv(q0, io.fb1);
+    const unsigned i1 = q0 - q1 * (unsigned)io.bn[1];
+    return out ? (long long)i0 * io.bso[0] + (long long)i1 * io.bso[1] + (long long)q1 * io.bso[2]
+               : (long long)i0 * io.bsi[0] + (long long)i1 * io.bsi[1] + (long long)q1 * io.bsi[2];
+}
+__device__ __forceinline__ int line_i0(const IODesc &io, long long l)
+{
+    const unsigned lu = (unsigned)l;
+    return (int)(lu - fdiv(lu, io.fb0) * (unsigned)io.bn[0]);
 }
 
 __device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
@@ -67,13 +79,20 @@ template <class T, bool RAW> __device__ __forceinline__ cx<T> sload(const cx<T> 
     }
 }
 
-// one Stockham stage of radix R in shared memory, in place through registers
-template <class T, int R, bool FWD>
-__device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int nl, int tpl)
+// padded shared-memory slot of element i
+__device__ __forceinline__ int sp(int i, int pad) { return i + (i >> pad); }
+
+// One Stockham stage of radix R in shared memory, in place through
+// registers.  Butterfly j (j < L/R) of a line reads x[j + m L/R], twiddles
+// input m by w^(m k) (k = j mod ns, w = exp(-+2 pi i/(ns R))), runs a radix-R
+// DFT and writes y[(j / ns) ns R + k + m ns].  All reads of a stage precede
+// the barrier and all writes follow it.
+template <class T, int E, int R>
+__device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int nl, int tpl, int g, int t)
 {
-    constexpr int NB = (kE + R - 1) / R;
-    const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
-    const int L = P.L, nr = L / R, ns = P.st[si].ns;
+    constexpr int NB = (E + R - 1) / R;
+    const int nr = P.L / R, ns = P.st[si].ns, pad = P.pad;
+    const FastDiv fns = P.st[si].fns;
     const cx<T> *tw = reinterpret_cast<const cx<T> *>(P.tw) + P.st[si].tw;
     cx<T> *line = sm + (size_t)g * P.LS;
     cx<T> v[NB][R];
@@ -83,52 +102,52 @@ __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int 
         int j = t + i * tpl;
         jj[i] = (g < nl && j < nr) ? j : -1;
         if (jj[i] >= 0) {
-            int k = j % ns;
 #pragma unroll
-            for (int m = 0; m < R; ++m) v[i][m] = line[j + m * nr];
-            if (k) {
-#pragma unroll
-                for (int m = 1; m < R; ++m) {
-                    cx<T> w = tw[k * (R - 1) + m - 1];
-                    v[i][m] = twmul<FWD>(v[i][m], w);
-                }
-            }
+            for (int m = 0; m < R; ++m) v[i][m] = line[sp(j + m * nr, pad)];
         }
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
         if (jj[i] >= 0) {
-            int j = jj[i], k = j % ns;
-            dft<R, FWD>(v[i]);
-            int base = (j / ns) * ns * R + k;
+            const int j = jj[i];
+            const int q = (int)fdiv((unsigned)j, fns), k = j - q * ns;
+            if (k) {
+                const cx<T> *twk = tw + k * (R - 1) - 1;
 #pragma unroll
-            for (int m = 0; m < R; ++m) line[base + m * ns] = v[i][m];
+                for (int m = 1; m < R; ++m) v[i][m] = cmul(v[i][m], twk[m]);
+            }
+            dft<R, true>(v[i]);
+            const int base = q * ns * R + k;
+#pragma unroll
+            for (int m = 0; m < R; ++m) line[sp(base + m * ns, pad)] = v[i][m];
         }
+        // keep the next butterfly's twiddle loads below this one's stores, so
+        // that only one butterfly's twiddles are live at a time
+        asm volatile("" ::: "memory");
     }
     __syncthreads();
 }
 
-template <class T, bool FWD>
-__device__ __forceinline__ void stage_dispatch(cx<T> *sm, const CoreDesc &P, int si, int nl, int tpl)
+// Forward stages only: a backward transform runs them on conjugated data
+// (IFFT(x) = conj(FFT(conj(x)))), with the conjugations folded into the
+// prologue, the epilogue and the Bluestein steps.
+template <class T, int E>
+__device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl, int tpl, int g, int t)
 {
-    switch (P.st[si].R) {
-    case 2: stage<T, 2, FWD>(sm, P, si, nl, tpl); break;
-    case 3: stage<T, 3, FWD>(sm, P, si, nl, tpl); break;
-    case 4: stage<T, 4, FWD>(sm, P, si, nl, tpl); break;
-    case 5: stage<T, 5, FWD>(sm, P, si, nl, tpl); break;
-    case 7: stage<T, 7, FWD>(sm, P, si, nl, tpl); break;
-    case 8: stage<T, 8, FWD>(sm, P, si, nl, tpl); break;
-    case 11: stage<T, 11, FWD>(sm, P, si, nl, tpl); break;
-    case 16: stage<T, 16, FWD>(sm, P, si, nl, tpl); break;
-    default: break;
+    for (int s = 0; s < P.nst; ++s) {
+        switch (P.st[s].R) {
+        case 2: stage<T, E, 2>(sm, P, s, nl, tpl, g, t); break;
+        case 3: stage<T, E, 3>(sm, P, s, nl, tpl, g, t); break;
+        case 4: stage<T, E, 4>(sm, P, s, nl, tpl, g, t); break;
+        case 5: stage<T, E, 5>(sm, P, s, nl, tpl, g, t); break;
+        case 7: stage<T, E, 7>(sm, P, s, nl, tpl, g, t); break;
+        case 8: stage<T, E, 8>(sm, P, s, nl, tpl, g, t); break;
+        case 11: stage<T, E, 11>(sm, P, s, nl, tpl, g, t); break;
+        case 16: stage<T, E, 16>(sm, P, s, nl, tpl, g, t); break;
+        default: break;
+        }
     }
-}
-
-template <class T, bool FWD>
-__device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl, int tpl)
-{
-    for (int s = 0; s < P.nst; ++s) stage_dispatch<T, FWD>(sm, P, s, nl, tpl);
 }
 
 // scale helper: multiply by fct and store with the per-line exponent
@@ -158,130 +177,137 @@ template <> struct OutScale<df> {
     __device__ double apply(df v, int esc) const { return df_to_double(v * m, esc - e); }
 };
 
-template <class T>
+// load one storage unit of an input line (kinds of IODesc), as raw storage values
+template <class S, class S2>
+__device__ __forceinline__ void load_unit(const IODesc &io, const char *base, int u, S &re, S &im)
+{
+    if (io.in_kind == IN_C) {
+        S2 z = *reinterpret_cast<const S2 *>(base + (long long)u * io.is);
+        re = z.x;
+        im = z.y;
+    } else if (io.in_kind == IN_R) {
+        re = *reinterpret_cast<const S *>(base + (long long)u * io.is);
+        im = S(0);
+    } else if (io.in_kind == IN_P) {
+        const char *p = base + (long long)u * io.is;
+        re = *reinterpret_cast<const S *>(p);
+        im = *reinterpret_cast<const S *>(p + io.ps_in);
+    } else {  // IN_HC: unit 0 = (r0, 0); unit k = (r_{2k-1}, r_{2k}); even N: last = (r_{N-1}, 0)
+        if (u == 0) {
+            re = *reinterpret_cast<const S *>(base);
+            im = S(0);
+        } else {
+            re = *reinterpret_cast<const S *>(base + (2 * (long long)u - 1) * io.is);
+            im = (2 * (long long)u < io.nreal) ? *reinterpret_cast<const S *>(base + (2 * (long long)u) * io.is) : S(0);
+        }
+    }
+}
+__device__ __forceinline__ float negs(float x) { return -x; }
+__device__ __forceinline__ double negs(double x) { return dneg(x); }
+
+template <class T, int E>
 __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
 {
     using S = typename Traits<T>::S;
     using S2 = typename Traits<T>::S2;
-    constexpr bool RAW = Traits<T>::kRaw;
+    constexpr bool RAW = Traits<T>::kRaw;  // double-float: per-line range check and scaling
     extern __shared__ __align__(16) unsigned char smraw[];
     cx<T> *sm = reinterpret_cast<cx<T> *>(smraw);
     __shared__ int s_esc[kMaxLinesPerCta];
+    __shared__ int s_emax[kMaxLinesPerCta];
+    __shared__ int s_rescale;
 
-    const int lpc = io.lpc, tpl = io.tpl;
+    const int lpc = io.lpc, tpl = io.tpl, pad = P.pad;
     const long long line0 = (long long)blockIdx.x * lpc;
     const int nl = (int)min((long long)lpc, io.nlines - line0);
     const int M = P.M;
+    // backward Stockham cores run the forward stages on conjugated data
+    const bool cc = !io.fwd && !P.blue;
+    // core mapping: line g, lane t of the line
+    const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
+    cx<T> *myline = sm + (size_t)(g < nl ? g : 0) * P.LS;
 
-    if (RAW && threadIdx.x < lpc) s_esc[threadIdx.x] = 0;
-    if (RAW) __syncthreads();
+    if (RAW) {
+        if ((int)threadIdx.x < lpc) { s_esc[threadIdx.x] = 0; s_emax[threadIdx.x] = 0; }
+        if (threadIdx.x == 0) s_rescale = 0;
+        __syncthreads();
+    }
 
-    // ---- prologue: HBM -> shared memory ---------------------------------
+    // ---- prologue: HBM -> shared memory, converting to the arithmetic type.
+    // Double-float lines whose largest element lies far from 1 are loaded a
+    // second time with an exact power-of-two scale.
     {
-        // each thread walks units of one line: rows mode (g, t) = (tid / tpl, tid % tpl),
-        // cols mode (g, t) = (tid % lpc, tid / lpc)
-        int g, t;
-        if (io.cols_in) { g = threadIdx.x % lpc; t = threadIdx.x / lpc; }
-        else { g = threadIdx.x / tpl; t = threadIdx.x - g * tpl; }
-        int emax = 0;
-        if (g < nl && t < tpl) {
-            const char *base = io.in + line_off(io, line0 + g, false);
-            cx<T> *line = sm + (size_t)g * P.LS;
-            for (int u = t; u < io.cnt_in; u += tpl) {
-                S re, im;
-                if (io.in_kind == IN_C) {
-                    S2 z = *reinterpret_cast<const S2 *>(base + u * io.is);
-                    re = z.x; im = z.y;
-                } else if (io.in_kind == IN_R) {
-                    re = *reinterpret_cast<const S *>(base + u * io.is);
-                    im = 0;
-                } else if (io.in_kind == IN_P) {
-                    re = *reinterpret_cast<const S *>(base + u * io.is);
-                    im = *reinterpret_cast<const S *>(base + u * io.is + io.ps_in);
-                } else {  // IN_HC: unit 0 = (r0, 0); unit k = (r_{2k-1}, r_{2k}); even N: last = (r_{N-1}, 0)
-                    if (u == 0) { re = *reinterpret_cast<const S *>(base); im = 0; }
-                    else {
-                        re = *reinterpret_cast<const S *>(base + (2 * (long long)u - 1) * io.is);
-                        long long ii = 2 * (long long)u;
-                        im = (ii < io.nreal) ? *reinterpret_cast<const S *>(base + ii * io.is) : (S)0;
+        int gi, ti;
+        if (io.cols_in) { gi = threadIdx.x % lpc; ti = threadIdx.x / lpc; }
+        else { gi = g; ti = t; }
+        const bool act = gi < nl && ti < tpl;
+        const char *base = act ? io.in + line_off(io, line0 + gi, false) : nullptr;
+        cx<T> *line = sm + (size_t)(act ? gi : 0) * P.LS;
+        for (int attempt = 0; attempt < (RAW ? 2 : 1); ++attempt) {
+            const int esc = (RAW && act) ? s_esc[gi] : 0;
+            int emax = 0;
+            if (act) {
+                for (int u = ti; u < io.cnt_in; u += tpl) {
+                    S re, im;
+                    load_unit<S, S2>(io, base, u, re, im);
+                    if (io.conj_in) im = negs(im);
+                    // general_c2r reads only the real part of the DC and Nyquist bins
+                    if (io.pre != PRE_NONE && (u == 0 || (io.pre == PRE_HERM_EVEN && u == M))) im = S(0);
+                    if constexpr (RAW) {
+                        int e1 = dexp(re), e2 = dexp(im);
+                        e1 = e1 == 0x7ff ? 0 : e1;
+                        e2 = e2 == 0x7ff ? 0 : e2;
+                        emax = max(emax, max(e1, e2));
                     }
-                }
-                if (io.conj_in) im = -im;
-                // general_c2r reads only the real part of the DC and Nyquist bins
-                if (io.pre != PRE_NONE && (u == 0 || (io.pre == PRE_HERM_EVEN && u == M))) im = 0;
-                if constexpr (RAW) {
-                    emax = max(emax, max(dexp(re), dexp(im)));
-                    *reinterpret_cast<double2 *>(line + u) = make_double2(re, im);
-                    if (io.pre == PRE_HERM_ODD && u > 0)
-                        *reinterpret_cast<double2 *>(line + (M - u)) = make_double2(re, -im);
-                } else {
-                    line[u] = cx<T>{(T)re, (T)im};
-                    if (io.pre == PRE_HERM_ODD && u > 0) line[M - u] = cx<T>{(T)re, (T)(-im)};
+                    cx<T> z{Store<T>::in(re, esc), Store<T>::in(im, esc)};
+                    const bool cz = cc && io.pre != PRE_HERM_EVEN;
+                    line[sp(u, pad)] = cz ? conjx(z) : z;
+                    if (io.pre == PRE_HERM_ODD && u > 0) line[sp(M - u, pad)] = cz ? z : conjx(z);
                 }
             }
-        }
-        if constexpr (RAW) {
-            // per-line exponent: scale the largest element of the line to [1, 2)
-            if (g < nl && t < tpl && emax > 0) atomicMax(&s_esc[g], emax);
+            if constexpr (!RAW) break;
+            if (attempt == 1) break;
+            if (act && emax > 0) atomicMax(&s_emax[gi], emax);
+            __syncthreads();
+            if ((int)threadIdx.x < nl) {
+                int em = s_emax[threadIdx.x];
+                // safe window: largest element within 2^+-40 (all-zero lines are safe)
+                if (em != 0 && (em > 1023 + 40 || em < 1023 - 40)) {
+                    s_esc[threadIdx.x] = 1023 - em;
+                    s_rescale = 1;
+                }
+            }
+            __syncthreads();
+            if (!s_rescale) break;
         }
     }
     __syncthreads();
-    if constexpr (RAW) {
-        if ((int)threadIdx.x < lpc) {
-            int em = s_esc[threadIdx.x];
-            s_esc[threadIdx.x] = em > 0 ? 1023 - em : 0;
-        }
-        __syncthreads();
-        // raw doubles -> double-float, scaled by the line's power of two
-        for (int idx = threadIdx.x; idx < nl * P.LS; idx += blockDim.x) {
-            int l = idx / P.LS;
-            sm[idx] = sload<T, true>(sm + idx, s_esc[l]);
-        }
-        __syncthreads();
-    }
 
-    // ---- pre-processing ---------------------------------------------------
-    const int g = threadIdx.x / tpl, t = threadIdx.x - (threadIdx.x / tpl) * tpl;
-    cx<T> *myline = sm + (size_t)(g < lpc ? g : 0) * P.LS;
-    if (io.pre == PRE_HERM_EVEN) {
-        // X[0..M] (X[M] Nyquist) -> Z[k] = (X[k] + conj(X[M-k])) + i e^{+2 pi i k/2M} (X[k] - conj(X[M-k]))
+    // ---- pre-processing: Hermitian half spectrum -> packed complex input ----
+    if (io.pre == PRE_HERM_EVEN && g < nl) {
+        // X[0..M] (X[M] Nyquist) -> Z[k] = (X[k] + conj(X[M-k])) + i e^{+2 pi i k/2M} (X[k] - conj(X[M-k])).
+        // Each thread owns the slot pair (k, M-k): no barrier between its reads and writes.
         const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
-        constexpr int NP = kE / 2 + 1;
-        cx<T> a[NP], b[NP];
-        int kk[NP];
-#pragma unroll
-        for (int i = 0; i < NP; ++i) {
-            int k = t + i * tpl;
-            kk[i] = (g < nl && k <= M / 2) ? k : -1;
-            if (kk[i] >= 0) {
-                a[i] = myline[k];
-                b[i] = myline[M - k];
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < NP; ++i) {
-            int k = kk[i];
-            if (k < 0) continue;
-            // Z[k] from (X[k], X[M-k]); Z[M-k] from (X[M-k], X[k])
+        for (int k = t; k <= M / 2; k += tpl) {
+            const int k2 = M - k;
+            cx<T> a = myline[sp(k, pad)], b = myline[sp(k2, pad)];
             {
-                cx<T> xa = a[i], xb = conjx(b[i]);
-                cx<T> A = xa + xb, Bv = xa - xb;
-                cx<T> w = conjx(rtw[k]);          // e^{+2 pi i k / N}
-                cx<T> tB = cmul(Bv, w);
-                myline[k] = cx<T>{A.r - tB.i, A.i + tB.r};
+                cx<T> xb = conjx(b);
+                cx<T> A = a + xb, Bv = a - xb;
+                cx<T> tB = cmulc(Bv, rtw[k]);
+                cx<T> z{A.r - tB.i, A.i + tB.r};
+                myline[sp(k, pad)] = cc ? conjx(z) : z;  // conjugated for a backward Stockham core
             }
-            int k2 = M - k;
             if (k > 0 && k2 != k) {
-                cx<T> xa = b[i], xb = conjx(a[i]);
-                cx<T> A = xa + xb, Bv = xa - xb;
-                cx<T> w = conjx(rtw[k2]);
-                cx<T> tB = cmul(Bv, w);
-                myline[k2] = cx<T>{A.r - tB.i, A.i + tB.r};
+                cx<T> xb = conjx(a);
+                cx<T> A = b + xb, Bv = b - xb;
+                cx<T> tB = cmulc(Bv, rtw[k2]);
+                cx<T> z{A.r - tB.i, A.i + tB.r};
+                myline[sp(k2, pad)] = cc ? conjx(z) : z;
             }
         }
-        __syncthreads();
     }
+    if (io.pre == PRE_HERM_EVEN) __syncthreads();
 
     // ---- core ---------------------------------------------------------------
     // Stockham: one pass in the transform's direction.  Bluestein (fftblue_fft,
@@ -293,83 +319,63 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
         const int L = P.L;
         const int npass = P.blue ? 2 : 1;
         for (int pass = 0; pass < npass; ++pass) {
-            if (P.blue && pass == 0) {
-                for (int idx = threadIdx.x; idx < nl * L; idx += blockDim.x) {
-                    int l = idx / L, u = idx - l * L;
-                    cx<T> *ln = sm + (size_t)l * P.LS;
-                    if (u < M) ln[u] = io.fwd ? cmulc(ln[u], ch[u]) : cmul(ln[u], ch[u]);
-                    else ln[u] = cx<T>{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
+            if (P.blue && g < nl) {
+                if (pass == 0) {
+                    for (int u = t; u < L; u += tpl) {
+                        cx<T> z = cx<T>{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
+                        if (u < M) z = io.fwd ? cmulc(myline[sp(u, pad)], ch[u]) : cmul(myline[sp(u, pad)], ch[u]);
+                        myline[sp(u, pad)] = z;
+                    }
+                } else {
+                    // backward FFT_L as conj(FFT_L(conj(.)))
+                    for (int u = t; u < L; u += tpl) {
+                        cx<T> z = io.fwd ? cmul(myline[sp(u, pad)], chf[u]) : cmulc(myline[sp(u, pad)], chf[u]);
+                        myline[sp(u, pad)] = conjx(z);
+                    }
                 }
-                __syncthreads();
-            } else if (P.blue) {
-                for (int idx = threadIdx.x; idx < nl * L; idx += blockDim.x) {
-                    int l = idx / L, u = idx - l * L;
-                    cx<T> *ln = sm + (size_t)l * P.LS;
-                    ln[u] = io.fwd ? cmul(ln[u], chf[u]) : cmulc(ln[u], chf[u]);
-                }
-                __syncthreads();
             }
-            const bool fwd = P.blue ? (pass == 0) : (io.fwd != 0);
-            if (fwd) run_stages<T, true>(sm, P, nl, tpl);
-            else run_stages<T, false>(sm, P, nl, tpl);
+            if (P.blue) __syncthreads();
+            run_stages<T, E>(sm, P, nl, tpl, g, t);
         }
         if (P.blue) {
-            for (int idx = threadIdx.x; idx < nl * M; idx += blockDim.x) {
-                int l = idx / M, u = idx - l * M;
-                cx<T> *ln = sm + (size_t)l * P.LS;
-                ln[u] = io.fwd ? cmulc(ln[u], ch[u]) : cmul(ln[u], ch[u]);
-            }
+            if (g < nl)
+                for (int u = t; u < M; u += tpl) {
+                    cx<T> z = conjx(myline[sp(u, pad)]);
+                    myline[sp(u, pad)] = io.fwd ? cmulc(z, ch[u]) : cmul(z, ch[u]);
+                }
             __syncthreads();
         }
     }
 
-    // ---- post-processing ----------------------------------------------------
-    if (io.post == POST_SPLIT) {
+    // ---- post-processing: real split ------------------------------------------
+    if (io.post == POST_SPLIT && g < nl) {
         // Z = FFT_M(x_even + i x_odd) -> X[k] = E_k + w^k O_k, k = 0..M,
-        // E_k = (Z[k] + conj(Z[M-k]))/2, O_k = -i (Z[k] - conj(Z[M-k]))/2, w = e^{-2 pi i/2M}
+        // E_k = (Z[k] + conj(Z[M-k]))/2, O_k = -i (Z[k] - conj(Z[M-k]))/2, w = e^{-2 pi i/2M};
+        // thread-owned slot pairs (k, M-k), slot M receives X[M]
         const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
-        constexpr int NP = kE / 2 + 1;
-        cx<T> a[NP], b[NP];
-        int kk[NP];
         constexpr T half = RealOps<T>::k(0.5);
-#pragma unroll
-        for (int i = 0; i < NP; ++i) {
-            int k = t + i * tpl;
-            kk[i] = (g < nl && k <= M / 2) ? k : -1;
-            if (kk[i] >= 0) {
-                a[i] = myline[k];
-                b[i] = myline[k == 0 ? 0 : M - k];
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < NP; ++i) {
-            int k = kk[i];
-            if (k < 0) continue;
+        for (int k = t; k <= M / 2; k += tpl) {
+            const int k2 = M - k;
+            cx<T> a = myline[sp(k, pad)], b = myline[sp(k == 0 ? 0 : k2, pad)];
             {
-                cx<T> za = a[i], zb = conjx(b[i]);
-                cx<T> E = cscale(za + zb, half);
-                cx<T> D = cscale(za - zb, half);
-                cx<T> O = cx<T>{D.i, -D.r};  // -i D
-                myline[k] = E + cmul(O, rtw[k]);
+                cx<T> zb = conjx(b);
+                cx<T> E = cscale(a + zb, half), D = cscale(a - zb, half);
+                myline[sp(k, pad)] = E + cmul(cx<T>{D.i, -D.r}, rtw[k]);
             }
-            int k2 = M - k;  // k = 0 -> slot M (Nyquist)
             if (k2 != k) {
-                cx<T> za = b[i], zb = conjx(a[i]);
-                cx<T> E = cscale(za + zb, half);
-                cx<T> D = cscale(za - zb, half);
-                cx<T> O = cx<T>{D.i, -D.r};
-                myline[k2] = E + cmul(O, rtw[k2]);
+                cx<T> zb = conjx(a);
+                cx<T> E = cscale(b + zb, half), D = cscale(b - zb, half);
+                myline[sp(k2, pad)] = E + cmul(cx<T>{D.i, -D.r}, rtw[k2]);
             }
         }
-        __syncthreads();
     }
+    if (io.post == POST_SPLIT) __syncthreads();
 
     // ---- epilogue: shared memory -> HBM ---------------------------------------
     {
         int g2, t2;
         if (io.cols_out) { g2 = threadIdx.x % lpc; t2 = threadIdx.x / lpc; }
-        else { g2 = threadIdx.x / tpl; t2 = threadIdx.x - g2 * tpl; }
+        else { g2 = g; t2 = t; }
         if (g2 < nl && t2 < tpl) {
             OutScale<T> sc;
             sc.init(io.fct);
@@ -377,20 +383,24 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
             const long long l = line0 + g2;
             char *base = io.out + line_off(io, l, true);
             const cx<T> *line = sm + (size_t)g2 * P.LS;
-            long long n2 = io.tw4 ? (l % io.bn[0]) : 0;
+            const int i0l = (io.tw4 || io.mul) ? line_i0(io, l) : 0;
+            const int n2 = io.tw4 ? i0l : 0;
+            const int ml = io.mul ? (int)(i0l * io.mul_a) : 0;
             const cx<T> *whi = reinterpret_cast<const cx<T> *>(io.tw4hi);
             const cx<T> *wlo = reinterpret_cast<const cx<T> *>(io.tw4lo);
+            const cx<T> *mt = reinterpret_cast<const cx<T> *>(io.mul);
             for (int u = t2; u < io.cnt_out; u += tpl) {
-                cx<T> z = line[u];
+                cx<T> z = line[sp(u, pad)];
+                if (cc) z.i = -z.i;
                 if (io.tw4) {
-                    long long tt = (n2 * u) % io.tw4N;
-                    long long hi = tt / io.tw4S, lo = tt - hi * io.tw4S;
+                    // t = n2 u < M: w^t = w_hi[t / S] * w_lo[t mod S]
+                    const unsigned tt = (unsigned)n2 * (unsigned)u;
+                    const unsigned hi = fdiv(tt, io.fdS), lo = tt - hi * (unsigned)io.tw4S;
                     cx<T> w = cmul(whi[hi], wlo[lo]);
                     z = io.fwd ? cmul(z, w) : cmulc(z, w);
                 }
                 if (io.mul) {
-                    const cx<T> *mt = reinterpret_cast<const cx<T> *>(io.mul);
-                    cx<T> w = mt[(l % io.bn[0]) * io.mul_a + (long long)u * io.mul_b];
+                    cx<T> w = mt[ml + (long long)u * io.mul_b];
                     z = io.mul_conj ? cmulc(z, w) : cmul(z, w);
                 }
                 if (io.conj_out) z.i = -z.i;
@@ -400,26 +410,25 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
                     S2 o;
                     o.x = sc.apply(z.r, esc);
                     o.y = sc.apply(z.i, esc);
-                    *reinterpret_cast<S2 *>(base + u * io.os) = o;
+                    *reinterpret_cast<S2 *>(base + (long long)u * io.os) = o;
                 } else if (io.out_kind == OUT_R) {
-                    *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
+                    *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, esc);
                 } else if (io.out_kind == OUT_P) {
-                    *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
-                    *reinterpret_cast<S *>(base + u * io.os + io.ps_out) = sc.apply(z.i, esc);
+                    char *p = base + (long long)u * io.os;
+                    *reinterpret_cast<S *>(p) = sc.apply(z.r, esc);
+                    *reinterpret_cast<S *>(p + io.ps_out) = sc.apply(z.i, esc);
                 } else {  // OUT_HC
                     if (u == 0) *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
                     else {
                         *reinterpret_cast<S *>(base + (2 * (long long)u - 1) * io.os) = sc.apply(z.r, esc);
-                        long long ii = 2 * (long long)u;
-                        if (ii < io.nreal)
-                            *reinterpret_cast<S *>(base + ii * io.os) = sc.apply(z.i, esc);
+                        if (2 * (long long)u < io.nreal)
+                            *reinterpret_cast<S *>(base + (2 * (long long)u) * io.os) = sc.apply(z.i, esc);
                     }
                 }
             }
         }
     }
 }
-
 
 // ---------------------------------------------------------------------------
 // elementwise line maps of the multi-pass paths

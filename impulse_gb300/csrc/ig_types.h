@@ -3,12 +3,20 @@
 
 namespace ig {
 
+// q = n / d for 0 <= n < 2^31 as (n * m) >> s, m = ceil(2^s / d), s = 31 + ceil(log2 d):
+// the error term n (m - 2^s/d) / 2^s stays below 1/d, so the quotient is exact
+struct FastDiv {
+    unsigned m;
+    int s;
+};
+
 constexpr int kMaxStages = 24;
 constexpr int kMaxLinesPerCta = 128;
-constexpr int kE = 16;  // complex elements per thread in the core
+constexpr int kEMax = 16;  // largest complex-elements-per-thread variant of the core kernel
 
 struct StageDesc {
     int R, ns, tw;  // radix, product of previous radices, twiddle offset (cx units)
+    FastDiv fns;    // division by ns
 };
 
 enum InKind { IN_C = 0, IN_R = 1, IN_P = 2, IN_HC = 3 };
@@ -21,6 +29,8 @@ struct CoreDesc {
     int L;    // Stockham length run in shared memory (M, or n2 for Bluestein)
     int LS;   // shared-memory complex slots per line (>= max(L, M + 1))
     int blue; // 1: Bluestein core
+    int pad;  // shared-memory padding: slot i is stored at i + (i >> pad)
+    int E;    // complex elements per thread (kernel variant 8 or 16): L / E threads per line
     int nst;
     StageDesc st[kMaxStages];
     const void *tw;     // cx<T> stage twiddles, forward sign
@@ -37,6 +47,7 @@ struct IODesc {
     long long nlines;
     long long bn[3];        // batch dims: line l -> (l % bn0, (l / bn0) % bn1, l / (bn0 bn1))
     long long bsi[3], bso[3];
+    FastDiv fb0, fb1;       // division by bn[0], bn[1] (line numbers are < 2^31)
     int in_kind, out_kind, pre, post;
     int cnt_in, cnt_out;    // storage units per line
     int conj_in, conj_out;
@@ -50,6 +61,7 @@ struct IODesc {
     // t = ((l % bn0) * u) mod tw4N, value w_hi[t / tw4S] * w_lo[t % tw4S]
     int tw4;
     long long tw4N, tw4S;
+    FastDiv fdS;            // division by tw4S
     const void *tw4hi, *tw4lo;
     // pointwise product on output unit u of line l with tab[(l % bn0) * mul_a + u * mul_b]
     // (conjugated when mul_conj); Bluestein's convolution step on a four-step core
