@@ -48,6 +48,7 @@ SIGNATURES = {
     "ig_rfft_exec_batch": (C.c_int, [_vp, _vp, _sz, _sz, C.c_int, C.c_double]),
     "ig_cfft_exec_device": (C.c_int, [_vp, _vp, _vp, _sz, _sz, _sz, C.c_int, C.c_double, _vp]),
     "ig_rfft_exec_device": (C.c_int, [_vp, _vp, _vp, _sz, _sz, _sz, C.c_int, C.c_double, _vp]),
+    "ig_cfft_exec_device_noalloc": (C.c_int, [_vp, _vp, _vp, _sz, _sz, _sz, C.c_int, C.c_double, _vp]),
     "ig_cfft_uses_bluestein": (C.c_int, [_vp, C.POINTER(_sz)]),
     "ig_rfft_uses_bluestein": (C.c_int, [_vp, C.POINTER(_sz)]),
     "ig_c2c": (C.c_int, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz, C.POINTER(_sz),

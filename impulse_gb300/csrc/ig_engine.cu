@@ -1166,6 +1166,80 @@ int ig_cfft_exec_device(ig_cfft_plan plan, const void *in, void *out, size_t bat
     });
 }
 
+// ---- allocation-free complex execution ------------------------------------
+// Some callers cannot allocate device memory at call time: code that runs
+// while a stream is being captured into a CUDA graph, under a memory pool
+// that forbids growth, or in a real-time loop that must not block in the
+// allocator.  ig_cfft_exec_device_noalloc serves them: its four-step scratch
+// is this file-scope device array instead of the cached per-stream
+// workspace.  Every GPU that loads the library holds the array until the
+// process exits.
+#define IG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+#define IG_NOALLOC_MAX_DEVICES 64
+static __device__ __align__(256) unsigned char g_noalloc_scratch[IG_NOALLOC_SCRATCH_BYTES];
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[IG_NOALLOC_MAX_DEVICES];
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is looked up
+// once per device (with that device current) and cached.
+static void *noalloc_scratch()
+{
+    int dev = device_id();
+    if (dev < 0 || dev >= IG_NOALLOC_MAX_DEVICES) raise(IG_EINVAL, "device index beyond the no-allocation table");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        ck(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-allocation scratch)");
+        g_noalloc_ptr[dev] = p;
+    }
+    return g_noalloc_ptr[dev];
+}
+
+// Same transform as ig_cfft_exec_device, with no device-memory allocation:
+// single-CTA plans need no scratch, four-step plans use the static array
+// (at most IG_NOALLOC_SCRATCH_BYTES = batch * length * complex size).  Plans
+// that run Bluestein over a four-step core are rejected.  The first call on
+// a device looks up the array's address there; make that first call before
+// any stream capture.  All calls share the array and it keeps the previous
+// call's contents (this path writes every scratch element before reading
+// it, so nothing needs clearing); calls that overlap on the GPU race.
+int ig_cfft_exec_device_noalloc(ig_cfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in,
+                                size_t dist_out, int forward, double fct, void *stream)
+{
+    return guarded([&] {
+        if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        const Core &c = *plan->core;
+        const long long es = 2 * (long long)store_real_bytes(plan->a);
+        if (c.kind == 2)
+            raise(IG_EINVAL, "no-allocation execution does not cover Bluestein over a multi-pass core");
+        if (batch == 0) return;
+        char *scr = nullptr;
+        if (c.kind == 1) {
+            unsigned long long need = (unsigned long long)batch * (unsigned long long)c.M * (unsigned long long)es;
+            if (need > IG_NOALLOC_SCRATCH_BYTES)
+                raise(IG_ETOOLARGE, "batch * length * element size exceeds the 64 MiB no-allocation scratch");
+            scr = (char *)noalloc_scratch();
+        }
+        IODesc io = blank_io();
+        io.in = (const char *)in;
+        io.out = (char *)out;
+        io.is = io.os = es;
+        io.nlines = (long long)batch;
+        io.bn[0] = (long long)batch;
+        io.bsi[0] = (long long)dist_in * es;
+        io.bso[0] = (long long)dist_out * es;
+        io.in_kind = IN_C;
+        io.out_kind = OUT_C;
+        io.cnt_in = io.cnt_out = (int)c.M;
+        io.nreal = c.M;
+        io.fwd = forward;
+        io.fct = fct;
+        if (c.kind == 0) launch_smem(c.a, c.d, io, as_stream(stream));
+        else run_fourstep(c, io, scr, as_stream(stream));
+    });
+}
+
 int ig_rfft_exec_device(ig_rfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in, size_t dist_out,
                         int forward, double fct, void *stream)
 {

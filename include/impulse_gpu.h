@@ -102,6 +102,19 @@ int ig_cfft_exec_device(ig_cfft_plan plan, const void *in, void *out, size_t bat
 int ig_rfft_exec_device(ig_rfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in,
                         size_t dist_out, int forward, double fct, void *stream);
 
+/* Allocation-free variant of ig_cfft_exec_device.  No counterpart in the
+ * reference (PocketFFT mallocs its scratch on every call).  For callers that
+ * must not allocate device memory while they run -- during CUDA-graph stream
+ * capture, under a fixed memory pool, in a real-time loop -- this call uses
+ * a static device array of 64 MiB (held by every GPU that loads the library)
+ * instead of the engine's cached workspace.  Limit: batch * length * complex
+ * element size <= 64 MiB for plans longer than one CTA; plans running
+ * Bluestein over a multi-pass core are rejected (IG_EINVAL).  The first call
+ * on each device looks the array up there and should precede any stream
+ * capture.  Calls share the array; calls that overlap on the GPU race. */
+int ig_cfft_exec_device_noalloc(ig_cfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in,
+                                size_t dist_out, int forward, double fct, void *stream);
+
 /* Plan introspection: 1 when the plan runs Bluestein; the padded length. */
 int ig_cfft_uses_bluestein(ig_cfft_plan plan, size_t *n2);
 int ig_rfft_uses_bluestein(ig_rfft_plan plan, size_t *n2);
