@@ -77,6 +77,20 @@ def batch_for(n):
     return max(1, int(round(TOTAL_REALS / n)))
 
 
+def aggregate(ms_local, bytes_local, world, device=None):
+    """Max step time over ranks and the whole-job throughput (weak scaling:
+    every rank processes the full workload on its own GPU; no data-path
+    collective)."""
+    ms = float(ms_local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * bytes_local / (ms / 1e3) / 1e9
+
+
 # --------------------------------------------------------------------------
 # clocks sampled during the timed region
 # --------------------------------------------------------------------------
@@ -238,12 +252,7 @@ def run_ours(args, rank, world):
         return ms, launches, per_ms
 
     def max_over_ranks(v):
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([v], dtype=torch.float64, device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            return float(t.item())
-        return v
+        return aggregate(v, 0.0, world, dev)[0]
 
     result = {}
     items64 = make("f64")
@@ -252,7 +261,7 @@ def run_ours(args, rank, world):
     clk.start()
     ms64, launches, per_ms = timed(items64, args.steps, args.warmup, per_length=True)
     clocks = clk.stop()
-    ms64 = max_over_ranks(ms64)
+    ms64, _ = aggregate(ms64, bytes64, world, dev)
     step_ms = ms64 / args.steps
     value = world * bytes64 / (step_ms / 1e3) / 1e9
 
