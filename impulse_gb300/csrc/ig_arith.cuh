@@ -91,17 +91,23 @@ struct df {
 // compile-time split of a double constant into a double-float
 constexpr df df_const(double c) { return df{(float)c, (float)(c - (double)(float)c)}; }
 
-// Knuth TwoSum + Fast2Sum renormalisation ("sloppy" double-float add: the
-// error bound is relative to |a| + |b|, which is what a normwise FFT error
-// analysis needs).
+// Knuth TwoSum of the high parts, low parts added in float ("sloppy"
+// double-float add: the error bound is relative to |a| + |b|, which is what a
+// normwise FFT error analysis needs).  The result is left unnormalised (the
+// low part may reach a few ulps of the high part); butterflies renormalise
+// their outputs once with df_renorm.  Products accept unnormalised inputs.
 IGD df operator+(df a, df b)
 {
     float s = IG_FADD(a.h, b.h);
     float bb = IG_FSUB(s, a.h);
     float e = IG_FADD(IG_FSUB(a.h, IG_FSUB(s, bb)), IG_FSUB(b.h, bb));
-    e = IG_FADD(e, IG_FADD(a.l, b.l));
-    float h = IG_FADD(s, e);
-    return df{h, IG_FSUB(e, IG_FSUB(h, s))};
+    return df{s, IG_FADD(e, IG_FADD(a.l, b.l))};
+}
+// Dekker's Fast2Sum: |l| is a few ulps of h at most, or h == 0
+IGD df df_renorm(df a)
+{
+    float h = IG_FADD(a.h, a.l);
+    return df{h, IG_FSUB(a.l, IG_FSUB(h, a.h))};
 }
 IGD df operator-(df a) { return df{-a.h, -a.l}; }
 IGD df operator-(df a, df b) { return a + df{-b.h, -b.l}; }
@@ -289,6 +295,14 @@ template <bool FWD, class R> IGD cx<R> rot(cx<R> a)
     return cx<R>{-a.i, a.r};
 }
 template <class R> IGD cx<R> cscale(cx<R> a, R s) { return cx<R>{a.r * s, a.i * s}; }
+// exact halving
+IGD cx<float> chalf(cx<float> a) { return cx<float>{a.r * 0.5f, a.i * 0.5f}; }
+IGD cx<double> chalf(cx<double> a) { return cx<double>{a.r * 0.5, a.i * 0.5}; }
+IGD cx<df> chalf(cx<df> a) { return cx<df>{df_scale2(a.r, 0.5f), df_scale2(a.i, 0.5f)}; }
+// renormalise a double-float complex (no-op for float / double)
+IGD cx<float> crenorm(cx<float> a) { return a; }
+IGD cx<double> crenorm(cx<double> a) { return a; }
+IGD cx<df> crenorm(cx<df> a) { return cx<df>{df_renorm(a.r), df_renorm(a.i)}; }
 template <class R> IGD cx<R> conjx(cx<R> a) { return cx<R>{a.r, -a.i}; }
 
 // ---------------------------------------------------------------------------
@@ -297,7 +311,13 @@ template <class R> IGD cx<R> conjx(cx<R> a) { return cx<R>{a.r, -a.i}; }
 template <class R> struct Store;
 template <> struct Store<float> {
     using real = float;
-    IGD static float in(float x, int) { return x; }
+    // x * 2^es (exact; es is clamped to the normal exponent range)
+    IGD static float in(float x, int es)
+    {
+        if (!es) return x;
+        int e = es < -126 ? -126 : (es > 127 ? 127 : es);
+        return IG_FMUL(x, u2f((uint32_t)(127 + e) << 23));
+    }
     IGD static float out(float x, int) { return x; }
 };
 template <> struct Store<double> {

@@ -877,6 +877,22 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
         io.post = POST_NONE;
         io.cnt_in = 1;
     }
+    // odd real lengths on a single-CTA core: two real lines per complex line
+    if (N > 1 && N % 2 == 1 && op != OP_C2C && ln.bn[0] >= 2 && core->kind == 0) {
+        io.pair = 1;
+        io.pair_n0 = ln.bn[0];
+        io.pair_in = ln.bsi[0];
+        io.pair_out = ln.bso[0];
+        io.bn[0] = (ln.bn[0] + 1) / 2;
+        io.bsi[0] = 2 * ln.bsi[0];
+        io.bso[0] = 2 * ln.bso[0];
+        io.nlines = io.bn[0] * io.bn[1] * io.bn[2];
+        if (op == OP_R2HC || op == OP_R2C) {
+            io.post = POST_PAIR;
+        } else {
+            io.pre = PRE_HERM_ODD;  // both half spectra completed to Z in the prologue
+        }
+    }
     // coalescing mode: lines adjacent in memory and elements strided
     long long ue_in = (io.in_kind == IN_C || io.in_kind == IN_P) ? 2 * sr : sr;
     long long ue_out = (io.out_kind == OUT_C || io.out_kind == OUT_P) ? 2 * sr : sr;

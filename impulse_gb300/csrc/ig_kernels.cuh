@@ -120,7 +120,7 @@ __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int 
             dft<R, true>(v[i]);
             const int base = q * ns * R + k;
 #pragma unroll
-            for (int m = 0; m < R; ++m) line[sp(base + m * ns, pad)] = v[i][m];
+            for (int m = 0; m < R; ++m) line[sp(base + m * ns, pad)] = crenorm(v[i][m]);
         }
         // keep the next butterfly's twiddle loads below this one's stores, so
         // that only one butterfly's twiddles are live at a time
@@ -152,10 +152,15 @@ __device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl,
 
 // scale helper: multiply by fct and store with the per-line exponent
 template <class T> struct OutScale;
+__device__ __forceinline__ float fpow2(int e)  // 2^e, e in [-126, 127]
+{
+    return __uint_as_float((unsigned)(127 + max(-126, min(127, e))) << 23);
+}
+__device__ __forceinline__ int fexp(float x) { return (int)((__float_as_uint(x) >> 23) & 0xff); }
 template <> struct OutScale<float> {
     float f;
     __device__ void init(double fct) { f = (float)fct; }
-    __device__ float apply(float v, int) const { return v * f; }
+    __device__ float apply(float v, int esc) const { return esc ? v * (f * fpow2(-esc)) : v * f; }
 };
 template <> struct OutScale<double> {
     double f;
@@ -205,6 +210,30 @@ __device__ __forceinline__ void load_unit(const IODesc &io, const char *base, in
 __device__ __forceinline__ float negs(float x) { return -x; }
 __device__ __forceinline__ double negs(double x) { return dneg(x); }
 
+// write unit u of an output line (kinds of IODesc) with the output scale
+template <class T, class S, class S2>
+__device__ __forceinline__ void store_unit(const IODesc &io, char *base, int u, cx<T> z, const OutScale<T> &sc, int esc)
+{
+    if (io.out_kind == OUT_C) {
+        S2 o;
+        o.x = sc.apply(z.r, esc);
+        o.y = sc.apply(z.i, esc);
+        *reinterpret_cast<S2 *>(base + (long long)u * io.os) = o;
+    } else if (io.out_kind == OUT_R) {
+        *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, esc);
+    } else if (io.out_kind == OUT_P) {
+        char *p = base + (long long)u * io.os;
+        *reinterpret_cast<S *>(p) = sc.apply(z.r, esc);
+        *reinterpret_cast<S *>(p + io.ps_out) = sc.apply(z.i, esc);
+    } else {  // OUT_HC
+        if (u == 0) *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
+        else {
+            *reinterpret_cast<S *>(base + (2 * (long long)u - 1) * io.os) = sc.apply(z.r, esc);
+            if (2 * (long long)u < io.nreal) *reinterpret_cast<S *>(base + (2 * (long long)u) * io.os) = sc.apply(z.i, esc);
+        }
+    }
+}
+
 template <class T, int E>
 __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
 {
@@ -213,8 +242,8 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
     constexpr bool RAW = Traits<T>::kRaw;  // double-float: per-line range check and scaling
     extern __shared__ __align__(16) unsigned char smraw[];
     cx<T> *sm = reinterpret_cast<cx<T> *>(smraw);
-    __shared__ int s_esc[kMaxLinesPerCta];
-    __shared__ int s_emax[kMaxLinesPerCta];
+    __shared__ int s_esc[2 * kMaxLinesPerCta];   // per real sub-line: 2 g (+1 for line b of a pair)
+    __shared__ int s_emax[2 * kMaxLinesPerCta];
     __shared__ int s_rescale;
 
     const int lpc = io.lpc, tpl = io.tpl, pad = P.pad;
@@ -227,53 +256,89 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
     const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
     cx<T> *myline = sm + (size_t)(g < nl ? g : 0) * P.LS;
 
-    if (RAW) {
-        if ((int)threadIdx.x < lpc) { s_esc[threadIdx.x] = 0; s_emax[threadIdx.x] = 0; }
+    // range scaling: double-float lines always, FP32 lines when two real lines share one complex line
+    const bool paired = io.pair != 0;
+    const bool scaled = RAW || paired;
+    if (scaled) {
+        for (int i = threadIdx.x; i < 2 * lpc; i += blockDim.x) { s_esc[i] = 0; s_emax[i] = 0; }
         if (threadIdx.x == 0) s_rescale = 0;
         __syncthreads();
     }
 
     // ---- prologue: HBM -> shared memory, converting to the arithmetic type.
-    // Double-float lines whose largest element lies far from 1 are loaded a
-    // second time with an exact power-of-two scale.
+    // Lines whose largest element lies far from 1 (double-float), or the two
+    // real lines of a pair whose magnitudes differ (so that each keeps its own
+    // relative accuracy), are loaded a second time with exact power-of-two
+    // scales, one per real line.
     {
         int gi, ti;
         if (io.cols_in) { gi = threadIdx.x % lpc; ti = threadIdx.x / lpc; }
         else { gi = g; ti = t; }
         const bool act = gi < nl && ti < tpl;
         const char *base = act ? io.in + line_off(io, line0 + gi, false) : nullptr;
+        const bool has_b = act && paired && (2LL * line_i0(io, line0 + gi) + 1 < io.pair_n0);
+        const char *base_b = base + io.pair_in;
         cx<T> *line = sm + (size_t)(act ? gi : 0) * P.LS;
-        for (int attempt = 0; attempt < (RAW ? 2 : 1); ++attempt) {
-            const int esc = (RAW && act) ? s_esc[gi] : 0;
-            int emax = 0;
+        for (int attempt = 0; attempt < (scaled ? 2 : 1); ++attempt) {
+            const int esc = (scaled && act) ? s_esc[2 * gi] : 0;
+            const int escb = (scaled && act) ? s_esc[2 * gi + 1] : 0;
+            int emax = 0, emaxb = 0;
             if (act) {
                 for (int u = ti; u < io.cnt_in; u += tpl) {
-                    S re, im;
+                    S re, im, rb = S(0), ib = S(0);
                     load_unit<S, S2>(io, base, u, re, im);
-                    if (io.conj_in) im = negs(im);
+                    if (has_b) load_unit<S, S2>(io, base_b, u, rb, ib);
+                    if (io.conj_in) { im = negs(im); ib = negs(ib); }
                     // general_c2r reads only the real part of the DC and Nyquist bins
-                    if (io.pre != PRE_NONE && (u == 0 || (io.pre == PRE_HERM_EVEN && u == M))) im = S(0);
-                    if constexpr (RAW) {
-                        int e1 = dexp(re), e2 = dexp(im);
-                        e1 = e1 == 0x7ff ? 0 : e1;
-                        e2 = e2 == 0x7ff ? 0 : e2;
-                        emax = max(emax, max(e1, e2));
+                    if (io.pre != PRE_NONE && (u == 0 || (io.pre == PRE_HERM_EVEN && u == M))) { im = S(0); ib = S(0); }
+                    if (scaled) {
+                        if constexpr (RAW) {
+                            int e1 = dexp(re), e2 = dexp(im), e3 = dexp(rb), e4 = dexp(ib);
+                            emax = max(emax, max(e1 == 0x7ff ? 0 : e1, e2 == 0x7ff ? 0 : e2));
+                            emaxb = max(emaxb, max(e3 == 0x7ff ? 0 : e3, e4 == 0x7ff ? 0 : e4));
+                        } else {
+                            int e1 = fexp((float)re), e2 = fexp((float)im), e3 = fexp((float)rb), e4 = fexp((float)ib);
+                            emax = max(emax, max(e1 == 0xff ? 0 : e1, e2 == 0xff ? 0 : e2));
+                            emaxb = max(emaxb, max(e3 == 0xff ? 0 : e3, e4 == 0xff ? 0 : e4));
+                        }
                     }
-                    cx<T> z{Store<T>::in(re, esc), Store<T>::in(im, esc)};
-                    const bool cz = cc && io.pre != PRE_HERM_EVEN;
-                    line[sp(u, pad)] = cz ? conjx(z) : z;
-                    if (io.pre == PRE_HERM_ODD && u > 0) line[sp(M - u, pad)] = cz ? z : conjx(z);
+                    if (!paired) {
+                        cx<T> z{Store<T>::in(re, esc), Store<T>::in(im, esc)};
+                        const bool cz = cc && io.pre != PRE_HERM_EVEN;
+                        line[sp(u, pad)] = cz ? conjx(z) : z;
+                        if (io.pre == PRE_HERM_ODD && u > 0) line[sp(M - u, pad)] = cz ? z : conjx(z);
+                    } else {
+                        // Z = A + i B: real lines -> (a, b); half spectra -> Z[u] = A + iB,
+                        // Z[M-u] = conj(A) + i conj(B)
+                        cx<T> A{Store<T>::in(re, esc), Store<T>::in(im, esc)};
+                        cx<T> B{Store<T>::in(rb, escb), Store<T>::in(ib, escb)};
+                        cx<T> z = cx<T>{A.r - B.i, A.i + B.r};
+                        line[sp(u, pad)] = cc ? conjx(z) : z;
+                        if (io.in_kind != IN_R && u > 0) {
+                            cx<T> zm = cx<T>{A.r + B.i, B.r - A.i};
+                            line[sp(M - u, pad)] = cc ? conjx(zm) : zm;
+                        }
+                    }
                 }
             }
-            if constexpr (!RAW) break;
-            if (attempt == 1) break;
-            if (act && emax > 0) atomicMax(&s_emax[gi], emax);
+            if (!scaled || attempt == 1) break;
+            if (act && emax > 0) atomicMax(&s_emax[2 * gi], emax);
+            if (act && emaxb > 0) atomicMax(&s_emax[2 * gi + 1], emaxb);
             __syncthreads();
-            if ((int)threadIdx.x < nl) {
-                int em = s_emax[threadIdx.x];
-                // safe window: largest element within 2^+-40 (all-zero lines are safe)
-                if (em != 0 && (em > 1023 + 40 || em < 1023 - 40)) {
-                    s_esc[threadIdx.x] = 1023 - em;
+            for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+                const int ea = s_emax[2 * l], eb = s_emax[2 * l + 1];
+                if (RAW) {
+                    // safe window: largest element within 2^+-40 (all-zero lines are safe)
+                    if (ea != 0 && (ea > 1023 + 40 || ea < 1023 - 40)) { s_esc[2 * l] = 1023 - ea; s_rescale = 1; }
+                    if (paired && eb != 0 && (eb > 1023 + 40 || eb < 1023 - 40)) { s_esc[2 * l + 1] = 1023 - eb; s_rescale = 1; }
+                    if (paired && ea != 0 && eb != 0 && abs(ea - eb) > 8) {
+                        s_esc[2 * l] = 1023 - ea;
+                        s_esc[2 * l + 1] = 1023 - eb;
+                        s_rescale = 1;
+                    }
+                } else if (paired && ea != 0 && eb != 0 && (abs(ea - eb) > 8 || abs(ea - 127) > 40 || abs(eb - 127) > 40)) {
+                    s_esc[2 * l] = 127 - ea;
+                    s_esc[2 * l + 1] = 127 - eb;
                     s_rescale = 1;
                 }
             }
@@ -353,23 +418,34 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
         // E_k = (Z[k] + conj(Z[M-k]))/2, O_k = -i (Z[k] - conj(Z[M-k]))/2, w = e^{-2 pi i/2M};
         // thread-owned slot pairs (k, M-k), slot M receives X[M]
         const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
-        constexpr T half = RealOps<T>::k(0.5);
         for (int k = t; k <= M / 2; k += tpl) {
             const int k2 = M - k;
             cx<T> a = myline[sp(k, pad)], b = myline[sp(k == 0 ? 0 : k2, pad)];
             {
                 cx<T> zb = conjx(b);
-                cx<T> E = cscale(a + zb, half), D = cscale(a - zb, half);
-                myline[sp(k, pad)] = E + cmul(cx<T>{D.i, -D.r}, rtw[k]);
+                cx<T> E = chalf(a + zb), D = chalf(a - zb);
+                myline[sp(k, pad)] = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k]));
             }
             if (k2 != k) {
                 cx<T> zb = conjx(a);
-                cx<T> E = cscale(b + zb, half), D = cscale(b - zb, half);
-                myline[sp(k2, pad)] = E + cmul(cx<T>{D.i, -D.r}, rtw[k2]);
+                cx<T> E = chalf(b + zb), D = chalf(b - zb);
+                myline[sp(k2, pad)] = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k2]));
             }
         }
     }
     if (io.post == POST_SPLIT) __syncthreads();
+    if (io.post == POST_PAIR && g < nl) {
+        // Z = FFT(a + i b) -> A[k] = (Z[k] + conj(Z[M-k]))/2 at slot k,
+        // B[k] = -i (Z[k] - conj(Z[M-k]))/2 at slot M-k; slot 0 keeps (A[0], B[0])
+        for (int k = 1 + t; 2 * k < M + 1; k += tpl) {
+            const int k2 = M - k;
+            cx<T> a = myline[sp(k, pad)], b = conjx(myline[sp(k2, pad)]);
+            cx<T> A = chalf(a + b), D = chalf(a - b);
+            myline[sp(k, pad)] = crenorm(A);
+            myline[sp(k2, pad)] = crenorm(cx<T>{D.i, -D.r});
+        }
+    }
+    if (io.post == POST_PAIR) __syncthreads();
 
     // ---- epilogue: shared memory -> HBM ---------------------------------------
     {
@@ -379,17 +455,36 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
         if (g2 < nl && t2 < tpl) {
             OutScale<T> sc;
             sc.init(io.fct);
-            const int esc = RAW ? s_esc[g2] : 0;
+            const int esc = scaled ? s_esc[2 * g2] : 0;
+            const int escb = scaled ? s_esc[2 * g2 + 1] : 0;
             const long long l = line0 + g2;
             char *base = io.out + line_off(io, l, true);
             const cx<T> *line = sm + (size_t)g2 * P.LS;
-            const int i0l = (io.tw4 || io.mul) ? line_i0(io, l) : 0;
+            const int i0l = (io.tw4 || io.mul || paired) ? line_i0(io, l) : 0;
+            const bool has_b = paired && (2LL * i0l + 1 < io.pair_n0);
             const int n2 = io.tw4 ? i0l : 0;
             const int ml = io.mul ? (int)(i0l * io.mul_a) : 0;
             const cx<T> *whi = reinterpret_cast<const cx<T> *>(io.tw4hi);
             const cx<T> *wlo = reinterpret_cast<const cx<T> *>(io.tw4lo);
             const cx<T> *mt = reinterpret_cast<const cx<T> *>(io.mul);
+            const cx<T> z0 = paired ? line[0] : cx<T>{};
+            constexpr T zero = RealOps<T>::k(0.0);
             for (int u = t2; u < io.cnt_out; u += tpl) {
+                if (paired) {
+                    if (io.out_kind == OUT_R) {
+                        cx<T> z = line[sp(u, pad)];
+                        if (cc) z.i = -z.i;
+                        *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, esc);
+                        if (has_b) *reinterpret_cast<S *>(base + io.pair_out + (long long)u * io.os) = sc.apply(z.i, escb);
+                    } else {
+                        cx<T> za = u == 0 ? cx<T>{z0.r, zero} : line[sp(u, pad)];
+                        cx<T> zb = u == 0 ? cx<T>{z0.i, zero} : line[sp(M - u, pad)];
+                        if (io.conj_out) { za.i = -za.i; zb.i = -zb.i; }
+                        store_unit<T, S, S2>(io, base, u, za, sc, esc);
+                        if (has_b) store_unit<T, S, S2>(io, base + io.pair_out, u, zb, sc, escb);
+                    }
+                    continue;
+                }
                 cx<T> z = line[sp(u, pad)];
                 if (cc) z.i = -z.i;
                 if (io.tw4) {
@@ -405,26 +500,8 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
                 }
                 if (io.conj_out) z.i = -z.i;
                 // general_r2c stores the DC and Nyquist bins with a zero imaginary part
-                if (io.real_out && (u == 0 || (io.post == POST_SPLIT && u == M))) z.i = RealOps<T>::k(0.0);
-                if (io.out_kind == OUT_C) {
-                    S2 o;
-                    o.x = sc.apply(z.r, esc);
-                    o.y = sc.apply(z.i, esc);
-                    *reinterpret_cast<S2 *>(base + (long long)u * io.os) = o;
-                } else if (io.out_kind == OUT_R) {
-                    *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, esc);
-                } else if (io.out_kind == OUT_P) {
-                    char *p = base + (long long)u * io.os;
-                    *reinterpret_cast<S *>(p) = sc.apply(z.r, esc);
-                    *reinterpret_cast<S *>(p + io.ps_out) = sc.apply(z.i, esc);
-                } else {  // OUT_HC
-                    if (u == 0) *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
-                    else {
-                        *reinterpret_cast<S *>(base + (2 * (long long)u - 1) * io.os) = sc.apply(z.r, esc);
-                        if (2 * (long long)u < io.nreal)
-                            *reinterpret_cast<S *>(base + (2 * (long long)u) * io.os) = sc.apply(z.i, esc);
-                    }
-                }
+                if (io.real_out && (u == 0 || (io.post == POST_SPLIT && u == M))) z.i = zero;
+                store_unit<T, S, S2>(io, base, u, z, sc, esc);
             }
         }
     }
@@ -565,9 +642,8 @@ __global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_consta
             S2 a = src[u % M], b = src[(M - u) % M];
             lc.fit(a.x, a.y, b.x, b.y);
             cx<T> za = lc.in(a.x, a.y), zb = conjx(lc.in(b.x, b.y));
-            constexpr T half = RealOps<T>::k(0.5);
-            cx<T> E = cscale(za + zb, half);
-            cx<T> D = cscale(za - zb, half);
+            cx<T> E = chalf(za + zb);
+            cx<T> D = chalf(za - zb);
             cx<T> O = cx<T>{D.i, -D.r};
             z = E + cmul(O, reinterpret_cast<const cx<T> *>(mp.rtw)[u]);
         } else {

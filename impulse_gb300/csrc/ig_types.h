@@ -22,7 +22,7 @@ struct StageDesc {
 enum InKind { IN_C = 0, IN_R = 1, IN_P = 2, IN_HC = 3 };
 enum OutKind { OUT_C = 0, OUT_R = 1, OUT_P = 2, OUT_HC = 3 };
 enum PreKind { PRE_NONE = 0, PRE_HERM_EVEN = 1, PRE_HERM_ODD = 2 };
-enum PostKind { POST_NONE = 0, POST_SPLIT = 1 };
+enum PostKind { POST_NONE = 0, POST_SPLIT = 1, POST_PAIR = 2 };
 
 struct CoreDesc {
     int M;    // logical complex length of the core transform
@@ -52,6 +52,11 @@ struct IODesc {
     int cnt_in, cnt_out;    // storage units per line
     int conj_in, conj_out;
     int real_out;           // output is the spectrum of real data (zero DC / Nyquist imaginary parts)
+    // two real lines per complex line (odd real lengths): line l of the
+    // kernel covers real lines a (at the line's offset) and b (at +pair_in /
+    // +pair_out); b is absent when 2 * (l mod bn0) + 1 >= pair_n0
+    int pair;
+    long long pair_in, pair_out, pair_n0;
     int cols_in, cols_out;  // 1: consecutive threads walk consecutive lines
     int lpc, tpl;           // lines per CTA, threads per line
     long long nreal;        // real length N for halfcomplex units

@@ -82,3 +82,29 @@ def test_cpp_readme_r2c(engine):
     F.apply(F.FFTDesc([0], True), F.DataDesc(dOut, [5]), F.DataDesc(dIn, [5]))
     want = [4.5, 2.081559480312316 - 1.651098762732523j, -1.831559480312316 + 1.608220406444071j, 0, 0]
     assert np.allclose(dOut, want, atol=1e-14)
+
+
+@pytest.mark.parametrize("n", [5, 101, 1009, 2205, 6075])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_odd_lengths_paired_lines_keep_own_accuracy(engine, oracle_lib, n, dtype):
+    """Odd real lengths run two lines per complex transform; each line keeps its
+    own relative accuracy even when the two lines differ by many orders."""
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(n)
+    scales = np.array([1.0, 1e-9, 1e6, 1e-30 if dtype == np.float32 else 1e-250, 3.0])[:, None]
+    x = (rng.standard_normal((5, n)) * scales).astype(dtype)
+    tol = 1e-12 if dtype == np.float64 else 1e-6 * np.log2(n) * 2
+    hc = F.rfft_batch(x, forward=True)
+    back = F.rfft_batch(hc, forward=False, fct=1.0 / n)
+    for i in range(5):
+        want = oracle_lib.rfft_hc(x[i].astype(np.float64), True)
+        assert oracle_lib.rel_l2(hc[i], want) < tol, (n, i)
+        assert oracle_lib.rel_l2(back[i], x[i].astype(np.float64)) < 2 * tol, (n, i)
+    # N-d r2c / c2r over an odd last axis pairs lines too
+    y = rng.uniform(-1, 1, (7, n)).astype(dtype)
+    got = F.r2c(y, [1], forward=False)
+    want = oracle_lib.r2c(y.astype(np.float64), [1], forward=False)
+    assert oracle_lib.rel_l2(got, want) < tol
+    back2 = F.c2r(got, (7, n), [1], forward=True, fct=1.0 / n)
+    want2 = oracle_lib.c2r(want, (7, n), [1], forward=True, fct=1.0 / n)
+    assert oracle_lib.rel_l2(back2, want2) < 2 * tol
