@@ -63,6 +63,15 @@ SIGNATURES = {
                                 C.POINTER(_sz), C.c_int, _vp, _vp, C.c_double, _vp]),
     "ig_c2r_device": (C.c_int, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,
                                 C.POINTER(_sz), C.c_int, _vp, _vp, C.c_double, _vp]),
+    "ig_r2c_adjoint_device": (C.c_int, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,
+                                        C.POINTER(_sz), C.c_int, _vp, _vp, C.c_double, _vp]),
+    "ig_c2r_adjoint_device": (C.c_int, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,
+                                        C.POINTER(_sz), C.c_int, _vp, _vp, C.c_double, _vp]),
+    "ig_fftconv_create": (_vp, [C.c_int, _sz, _sz, _sz, _sz, _sz, _sz, _sz, C.c_int]),
+    "ig_fftconv_destroy": (None, [_vp]),
+    "ig_fftconv_padded_size": (C.c_int, [_vp, C.POINTER(_sz), C.POINTER(_sz)]),
+    "ig_fftconv_forward": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "ig_fftconv_backward": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ig_set_f64_arith": (C.c_int, [C.c_int]),
     "ig_release_caches": (None, []),
     "ig_launch_count": (C.c_ulonglong, [C.c_int]),

@@ -1448,6 +1448,268 @@ static void host_nd(int kind, int dtype, size_t ndim, const size_t *shape, const
     ck(cudaMemcpy((char *)out + olo, dout + olo, obytes, cudaMemcpyDeviceToHost), "D2H copy");
 }
 
+// ---- adjoints of the real transforms ------------------------------------------
+static void launch_half_weight(Arith a, void *x, long long lines, long long n_half, long long nreal, double w,
+                               int drop_im, cudaStream_t st)
+{
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::half_weight(x, lines, n_half, nreal, w, drop_im, st)
+                  : a == A_DF  ? Launch<TagDF>::half_weight(x, lines, n_half, nreal, w, drop_im, st)
+                               : Launch<TagF64>::half_weight(x, lines, n_half, nreal, w, drop_im, st);
+    ck(e, "Hermitian weighting");
+    count_launch();
+}
+
+// adjoint of r2c(axes, forward): halve the inner bins of the last axis (the
+// Hermitian weighting), then c2r(axes, !forward), which reads only the real
+// parts of the DC / Nyquist bins after its c2c over the other axes.  g has the half-spectrum
+// shape; x is real with shape_in.
+int ig_r2c_adjoint_device(int dtype, size_t ndim, const size_t *shape_in, const ptrdiff_t *stride_g,
+                          const ptrdiff_t *stride_x, size_t naxes, const size_t *axes, int forward, const void *g,
+                          void *x, double fct, void *stream)
+{
+    return guarded([&] {
+        if (ndim >= 1 && shape_in && prod(ndim, shape_in) == 0) return;
+        nd_checks(dtype, ndim, shape_in, stride_g, stride_x, naxes, axes, g, x, false);
+        if (naxes == 0) return;
+        Arith a = arith_for(dtype);
+        cudaStream_t st = as_stream(stream);
+        size_t last = axes[naxes - 1];
+        std::vector<size_t> sh(shape_in, shape_in + ndim);
+        sh[last] = shape_in[last] / 2 + 1;
+        const size_t ce = 2 * store_real_bytes(a);
+        // contiguous copy with the last axis innermost-of-the-copy: c2c the strided input into it
+        std::vector<ptrdiff_t> sc(ndim);
+        sc[ndim - 1] = (ptrdiff_t)ce;
+        for (size_t d = ndim - 1; d-- > 0;) sc[d] = sc[d + 1] * (ptrdiff_t)sh[d + 1];
+        DevBuf tmp(prod(ndim, sh.data()) * ce);
+        // identity copy through a zero-axis c2c is not available: copy line by line with the gather map
+        for_lines(ndim, sh.data(), stride_g, sc.data(), last, (const char *)g, (char *)tmp.p, [&](const Lines &ln) {
+            IODesc io = blank_io();
+            io.in = ln.in;
+            io.out = ln.out;
+            io.is = ln.es_in;
+            io.os = ln.es_out;
+            io.nlines = ln.nlines;
+            for (int i = 0; i < 3; ++i) { io.bn[i] = ln.bn[i]; io.bsi[i] = ln.bsi[i]; io.bso[i] = ln.bso[i]; }
+            io.in_kind = IN_C;
+            io.out_kind = OUT_C;
+            io.cnt_in = io.cnt_out = (int)sh[last];
+            io.nreal = (long long)shape_in[last];
+            MapDesc mp{};
+            mp.kind = MAP_PLAIN;
+            mp.M = (long long)sh[last];
+            mp.scr_len = (long long)sh[last];
+            // gather writes scratch line l at l * scr_len: the copy is contiguous in line order
+            mp.scr = ln.out;
+            launch_map(a, true, io, mp, st);
+        });
+        // the gather above wrote lines in the engine's line order, which for a
+        // contiguous destination whose last axis is innermost is the array order
+        long long nh = (long long)sh[last];
+        // DC / Nyquist imaginary parts are kept: the c2c over the other axes
+        // mixes them into real values; c2r drops them after that step
+        launch_half_weight(a, tmp.p, (long long)(prod(ndim, sh.data()) / sh[last]), nh, (long long)shape_in[last], 0.5,
+                           0, st);
+        nd_c2r_device(a, ndim, shape_in, sc.data(), stride_x, naxes, axes, forward ? 0 : 1, tmp.p, x, fct, st);
+        ck(cudaStreamSynchronize(st), "r2c adjoint");
+    });
+}
+
+// adjoint of c2r(axes, forward): r2c(axes, !forward), then double the inner
+// bins of the last axis.  y is real with shape_out; g has the half-spectrum shape.
+int ig_c2r_adjoint_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *stride_y,
+                          const ptrdiff_t *stride_g, size_t naxes, const size_t *axes, int forward, const void *y,
+                          void *g, double fct, void *stream)
+{
+    return guarded([&] {
+        if (ndim >= 1 && shape_out && prod(ndim, shape_out) == 0) return;
+        nd_checks(dtype, ndim, shape_out, stride_y, stride_g, naxes, axes, y, g, false);
+        if (naxes == 0) return;
+        Arith a = arith_for(dtype);
+        cudaStream_t st = as_stream(stream);
+        size_t last = axes[naxes - 1];
+        nd_r2c_device(a, ndim, shape_out, stride_y, stride_g, naxes, axes, forward ? 0 : 1, y, g, fct, st);
+        std::vector<size_t> sh(shape_out, shape_out + ndim);
+        sh[last] = shape_out[last] / 2 + 1;
+        // weighting along the last axis of a possibly strided array: one launch per line set
+        const long long es = 2 * (long long)store_real_bytes(a);
+        bool contiguous_last = stride_g[last] == es;
+        if (!contiguous_last) raise(IG_EINVAL, "c2r adjoint needs a unit-stride last axis in the spectrum");
+        for_lines(ndim, sh.data(), stride_g, stride_g, last, (const char *)g, (char *)g, [&](const Lines &ln) {
+            // lines here are rows of sh[last] contiguous bins; weight each row set
+            for (long long i1 = 0; i1 < ln.bn[1] * ln.bn[2]; ++i1) {
+                long long i1a = i1 % ln.bn[1], i2 = i1 / ln.bn[1];
+                char *base = ln.out + i1a * ln.bso[1] + i2 * ln.bso[2];
+                if (ln.bso[0] == (long long)sh[last] * es || ln.bn[0] == 1)
+                    launch_half_weight(a, base, ln.bn[0], (long long)sh[last], (long long)shape_out[last], 2.0, 0, st);
+                else
+                    for (long long i0 = 0; i0 < ln.bn[0]; ++i0)
+                        launch_half_weight(a, base + i0 * ln.bso[0], 1, (long long)sh[last], (long long)shape_out[last],
+                                           2.0, 0, st);
+            }
+        });
+    });
+}
+
+// ---- differentiable FFT convolution --------------------------------------------
+struct ig_fftconv_i {
+    Arith a;
+    int dtype;
+    long long B, H, W, NF, K, P0, P1;
+    int recompute;
+    std::unique_ptr<DevBuf> xpad, kpad, FX, FK, FG, Z, zpad;
+    bool have_spectra = false;
+};
+
+static void conv_r2c2d(Arith a, long long nb, long long P0, long long P1, const void *in, void *out, cudaStream_t st)
+{
+    const size_t sr = store_real_bytes(a), ce = 2 * sr;
+    size_t shape[3] = {(size_t)nb, (size_t)P0, (size_t)P1};
+    ptrdiff_t si[3] = {(ptrdiff_t)(P0 * P1 * sr), (ptrdiff_t)(P1 * sr), (ptrdiff_t)sr};
+    ptrdiff_t so[3] = {(ptrdiff_t)(P0 * (P1 / 2 + 1) * ce), (ptrdiff_t)((P1 / 2 + 1) * ce), (ptrdiff_t)ce};
+    size_t axes[2] = {1, 2};
+    nd_r2c_device(a, 3, shape, si, so, 2, axes, 1, in, out, 1.0, st);
+}
+static void conv_c2r2d(Arith a, long long nb, long long P0, long long P1, const void *in, void *out, cudaStream_t st)
+{
+    const size_t sr = store_real_bytes(a), ce = 2 * sr;
+    size_t shape[3] = {(size_t)nb, (size_t)P0, (size_t)P1};
+    ptrdiff_t si[3] = {(ptrdiff_t)(P0 * (P1 / 2 + 1) * ce), (ptrdiff_t)((P1 / 2 + 1) * ce), (ptrdiff_t)ce};
+    ptrdiff_t so[3] = {(ptrdiff_t)(P0 * P1 * sr), (ptrdiff_t)(P1 * sr), (ptrdiff_t)sr};
+    size_t axes[2] = {1, 2};
+    nd_c2r_device(a, 3, shape, si, so, 2, axes, 0, in, out, 1.0 / ((double)P0 * (double)P1), st);
+}
+static void conv_pad(Arith a, const void *in, void *out, long long B, long long H, long long W, long long P0,
+                     long long P1, long long r0, long long c0, cudaStream_t st)
+{
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::pad2d(in, out, B, H, W, P0, P1, r0, c0, st)
+                  : a == A_DF  ? Launch<TagDF>::pad2d(in, out, B, H, W, P0, P1, r0, c0, st)
+                               : Launch<TagF64>::pad2d(in, out, B, H, W, P0, P1, r0, c0, st);
+    ck(e, "pad");
+    count_launch();
+}
+static void conv_crop(Arith a, const void *in, void *out, long long B, long long H, long long W, long long P0,
+                      long long P1, long long r0, long long c0, cudaStream_t st)
+{
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::crop2d(in, out, B, H, W, P0, P1, r0, c0, st)
+                  : a == A_DF  ? Launch<TagDF>::crop2d(in, out, B, H, W, P0, P1, r0, c0, st)
+                               : Launch<TagF64>::crop2d(in, out, B, H, W, P0, P1, r0, c0, st);
+    ck(e, "crop");
+    count_launch();
+}
+static void conv_mul(Arith a, const void *x, const void *f, void *out, long long B, long long nf, long long n, int mode,
+                     cudaStream_t st)
+{
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::spec_mul(x, f, out, B, nf, n, mode, st)
+                  : a == A_DF  ? Launch<TagDF>::spec_mul(x, f, out, B, nf, n, mode, st)
+                               : Launch<TagF64>::spec_mul(x, f, out, B, nf, n, mode, st);
+    ck(e, "spectrum product");
+    count_launch();
+}
+
+static void conv_spectra(ig_fftconv_i &c, const void *x, const void *k, cudaStream_t st)
+{
+    conv_pad(c.a, x, c.xpad->p, c.B, c.H, c.W, c.P0, c.P1, 0, 0, st);
+    conv_r2c2d(c.a, c.B, c.P0, c.P1, c.xpad->p, c.FX->p, st);
+    conv_pad(c.a, k, c.kpad->p, c.NF, c.K, c.K, c.P0, c.P1, 0, 0, st);
+    conv_r2c2d(c.a, c.NF, c.P0, c.P1, c.kpad->p, c.FK->p, st);
+}
+
+ig_fftconv ig_fftconv_create(int dtype, size_t batch, size_t height, size_t width, size_t nfilters, size_t ksize,
+                             size_t pad_rows, size_t pad_cols, int recompute)
+{
+    ig_fftconv c = nullptr;
+    guarded([&] {
+        if (dtype != IG_F64 && dtype != IG_F32) raise(IG_EINVAL, "bad dtype");
+        if (!batch || !height || !width || !ksize) raise(IG_EZERO_LEN, "zero-length FFT requested");
+        if (ksize % 2 == 0) raise(IG_EINVAL, "filter size must be odd ('same' convolution)");
+        if (nfilters != 1 && nfilters != batch) raise(IG_EINVAL, "nfilters must be 1 or the batch size");
+        auto o = std::make_unique<ig_fftconv_i>();
+        o->a = arith_for(dtype);
+        o->dtype = dtype;
+        o->B = (long long)batch;
+        o->H = (long long)height;
+        o->W = (long long)width;
+        o->NF = (long long)nfilters;
+        o->K = (long long)ksize;
+        long long need0 = o->H + o->K - 1, need1 = o->W + o->K - 1;
+        o->P0 = pad_rows ? (long long)pad_rows : good_size_gpu(need0);
+        o->P1 = pad_cols ? (long long)pad_cols : good_size_gpu(need1);
+        if (o->P0 < need0 || o->P1 < need1) raise(IG_EINVAL, "padded size smaller than height/width + ksize - 1");
+        o->recompute = recompute;
+        const size_t sr = store_real_bytes(o->a), ce = 2 * sr;
+        const size_t half = (size_t)(o->P0 * (o->P1 / 2 + 1));
+        o->xpad.reset(new DevBuf(o->B * o->P0 * o->P1 * sr));
+        o->kpad.reset(new DevBuf(o->NF * o->P0 * o->P1 * sr));
+        o->FX.reset(new DevBuf(o->B * half * ce));
+        o->FK.reset(new DevBuf(o->NF * half * ce));
+        o->FG.reset(new DevBuf(o->B * half * ce));
+        o->Z.reset(new DevBuf(o->B * half * ce));
+        o->zpad.reset(new DevBuf(o->B * o->P0 * o->P1 * sr));
+        c = o.release();
+    });
+    return c;
+}
+
+void ig_fftconv_destroy(ig_fftconv c) { delete c; }
+
+int ig_fftconv_padded_size(ig_fftconv c, size_t *rows, size_t *cols)
+{
+    if (!c) return IG_EINVAL;
+    if (rows) *rows = (size_t)c->P0;
+    if (cols) *cols = (size_t)c->P1;
+    return IG_OK;
+}
+
+// y = crop_c(c2r(r2c(pad x) * r2c(pad k))) / (P0 P1), c = (K - 1) / 2  ('same' convolution)
+int ig_fftconv_forward(ig_fftconv c, const void *x, const void *k, void *y, void *stream)
+{
+    return guarded([&] {
+        if (!c || !x || !k || !y) raise(IG_EINVAL, "null argument");
+        cudaStream_t st = as_stream(stream);
+        conv_spectra(*c, x, k, st);
+        const long long n = c->P0 * (c->P1 / 2 + 1);
+        conv_mul(c->a, c->FX->p, c->FK->p, c->Z->p, c->B, c->NF, n, 0, st);
+        conv_c2r2d(c->a, c->B, c->P0, c->P1, c->Z->p, c->zpad->p, st);
+        const long long off = (c->K - 1) / 2;
+        conv_crop(c->a, c->zpad->p, y, c->B, c->H, c->W, c->P0, c->P1, off, off, st);
+        c->have_spectra = !c->recompute;
+    });
+}
+
+// gx = crop_0(c2r(r2c(pad_c gy) * conj(r2c(pad k)))) / (P0 P1)
+// gk = crop_0(sum_b c2r(r2c(pad_c gy_b) * conj(r2c(pad x_b)))) / (P0 P1)  (per image when nfilters == batch)
+// The spectra of x and k are recomputed unless the object keeps them.
+int ig_fftconv_backward(ig_fftconv c, const void *x, const void *k, const void *gy, void *gx, void *gk, void *stream)
+{
+    return guarded([&] {
+        if (!c || !x || !k || !gy) raise(IG_EINVAL, "null argument");
+        cudaStream_t st = as_stream(stream);
+        if (!c->have_spectra) conv_spectra(*c, x, k, st);
+        const long long off = (c->K - 1) / 2;
+        const long long n = c->P0 * (c->P1 / 2 + 1);
+        conv_pad(c->a, gy, c->zpad->p, c->B, c->H, c->W, c->P0, c->P1, off, off, st);
+        conv_r2c2d(c->a, c->B, c->P0, c->P1, c->zpad->p, c->FG->p, st);
+        if (gx) {
+            conv_mul(c->a, c->FG->p, c->FK->p, c->Z->p, c->B, c->NF, n, 1, st);
+            conv_c2r2d(c->a, c->B, c->P0, c->P1, c->Z->p, c->zpad->p, st);
+            conv_crop(c->a, c->zpad->p, gx, c->B, c->H, c->W, c->P0, c->P1, 0, 0, st);
+        }
+        if (gk) {
+            if (c->NF == 1) {
+                conv_mul(c->a, c->FG->p, c->FX->p, c->Z->p, c->B, c->B, n, 2, st);
+                conv_c2r2d(c->a, 1, c->P0, c->P1, c->Z->p, c->zpad->p, st);
+                conv_crop(c->a, c->zpad->p, gk, 1, c->K, c->K, c->P0, c->P1, 0, 0, st);
+            } else {
+                conv_mul(c->a, c->FG->p, c->FX->p, c->Z->p, c->B, c->B, n, 1, st);
+                conv_c2r2d(c->a, c->B, c->P0, c->P1, c->Z->p, c->zpad->p, st);
+                conv_crop(c->a, c->zpad->p, gk, c->B, c->K, c->K, c->P0, c->P1, 0, 0, st);
+            }
+        }
+        if (c->recompute) c->have_spectra = false;
+    });
+}
+
 int ig_c2c(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
            const size_t *axes, int forward, const void *in, void *out, double fct, size_t nthreads)
 {

@@ -75,4 +75,41 @@ template <class Tag> cudaError_t Launch<Tag>::scatter(const IODesc &io, const Ma
     return cudaGetLastError();
 }
 
+template <class Tag>
+cudaError_t Launch<Tag>::pad2d(const void *in, void *out, long long B, long long H, long long W, long long P0,
+                               long long P1, long long r0, long long c0, cudaStream_t st)
+{
+    using S = typename Traits<typename TagType<Tag>::T>::S;
+    k_pad2d<S><<<map_grid(B * P0 * P1), 256, 0, st>>>((const S *)in, (S *)out, B, H, W, P0, P1, r0, c0);
+    return cudaGetLastError();
+}
+template <class Tag>
+cudaError_t Launch<Tag>::crop2d(const void *in, void *out, long long B, long long H, long long W, long long P0,
+                                long long P1, long long r0, long long c0, cudaStream_t st)
+{
+    using S = typename Traits<typename TagType<Tag>::T>::S;
+    k_crop2d<S><<<map_grid(B * H * W), 256, 0, st>>>((const S *)in, (S *)out, B, H, W, P0, P1, r0, c0);
+    return cudaGetLastError();
+}
+template <class Tag>
+cudaError_t Launch<Tag>::spec_mul(const void *a, const void *f, void *out, long long B, long long nf, long long n,
+                                  int mode, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    using S2 = typename Traits<T>::S2;
+    k_spec_mul<T><<<map_grid(mode == 2 ? n : B * n), 256, 0, st>>>((const S2 *)a, (const S2 *)f, (S2 *)out, B, nf, n,
+                                                                    mode);
+    return cudaGetLastError();
+}
+template <class Tag>
+cudaError_t Launch<Tag>::half_weight(void *x, long long lines, long long n_half, long long nreal, double w,
+                                     int drop_im, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    k_half_weight<T><<<map_grid(lines * n_half), 256, 0, st>>>((S2 *)x, lines, n_half, nreal, (S)w, drop_im);
+    return cudaGetLastError();
+}
+
 }  // namespace ig

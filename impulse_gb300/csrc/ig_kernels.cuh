@@ -531,6 +531,16 @@ template <> struct Loc<df> {
     __device__ double out(df v) const { return df_to_double(v, esc); }
 };
 
+// conversions with an explicit power-of-two exponent (double-float) or plain casts
+template <class T> struct Loc2 {
+    __device__ static T in(double v) { return (T)v; }
+    __device__ static double out(T v, int) { return (double)v; }
+};
+template <> struct Loc2<df> {
+    __device__ static df in(double v) { return df_from_double(v, 0); }
+    __device__ static double out(df v, int esc) { return df_to_double(v, esc); }
+};
+
 // read unit u of the user-facing input line at `base` (kinds of IODesc)
 template <class S, class S2>
 __device__ __forceinline__ void read_unit(const IODesc &io, const char *base, long long u, double &re, double &im)
@@ -675,6 +685,103 @@ __global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_consta
                 *reinterpret_cast<S *>(base + (2 * u - 1) * io.os) = sc.apply(z.r, esc);
                 if (2 * u < io.nreal) *reinterpret_cast<S *>(base + (2 * u) * io.os) = sc.apply(z.i, esc);
             }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FFT-convolution helpers (elementwise; storage type S, arithmetic T)
+// ---------------------------------------------------------------------------
+
+// out[b, i, j] (P0 x P1) = in[b, i - r0, j - c0] inside the H x W source, else 0
+template <class S>
+__global__ void k_pad2d(const S *__restrict__ in, S *__restrict__ out, long long B, long long H, long long W,
+                        long long P0, long long P1, long long r0, long long c0)
+{
+    const long long total = B * P0 * P1;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        long long j = idx % P1, r = idx / P1, i = r % P0, b = r / P0;
+        long long si = i - r0, sj = j - c0;
+        out[idx] = (si >= 0 && si < H && sj >= 0 && sj < W) ? in[(b * H + si) * W + sj] : S(0);
+    }
+}
+
+// out[b, i, j] (H x W) = in[b, i + r0, j + c0] of a P0 x P1 source
+template <class S>
+__global__ void k_crop2d(const S *__restrict__ in, S *__restrict__ out, long long B, long long H, long long W,
+                         long long P0, long long P1, long long r0, long long c0)
+{
+    const long long total = B * H * W;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        long long j = idx % W, r = idx / W, i = r % H, b = r / H;
+        out[idx] = in[(b * P0 + i + r0) * P1 + j + c0];
+    }
+}
+
+// spectrum products: mode 0: out[b,e] = a[b,e] * f[b % nf, e];  mode 1: * conj(f)
+// mode 2: out[e] = sum_b a[b,e] * conj(f[b,e])   (gradient of a shared filter)
+template <class T>
+__global__ void k_spec_mul(const typename Traits<T>::S2 *__restrict__ a, const typename Traits<T>::S2 *__restrict__ f,
+                           typename Traits<T>::S2 *__restrict__ out, long long B, long long nf, long long n, int mode)
+{
+    using S2 = typename Traits<T>::S2;
+    using S = typename Traits<T>::S;
+    const long long total = mode == 2 ? n : B * n;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        if (mode == 2) {
+            cx<T> acc{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
+            // accumulate with a common scale: the largest operand exponents of each product
+            for (long long b = 0; b < B; ++b) {
+                S2 x = a[b * n + idx], y = f[b * n + idx];
+                Loc<T> la, lf;
+                la.fit(x.x, x.y);
+                lf.fit(y.x, y.y);
+                cx<T> p = cmulc(la.in(x.x, x.y), lf.in(y.x, y.y));
+                // bring each product back to true scale before summing
+                const double qr = Loc2<T>::out(p.r, la.esc + lf.esc), qi = Loc2<T>::out(p.i, la.esc + lf.esc);
+                acc = crenorm(acc + cx<T>{Loc2<T>::in(qr), Loc2<T>::in(qi)});
+            }
+            S2 o;
+            o.x = (S)Loc2<T>::out(acc.r, 0);
+            o.y = (S)Loc2<T>::out(acc.i, 0);
+            out[idx] = o;
+        } else {
+            long long b = idx / n, e = idx - b * n;
+            S2 x = a[idx], y = f[(b % nf) * n + e];
+            Loc<T> la, lf;
+            la.fit(x.x, x.y);
+            lf.fit(y.x, y.y);
+            cx<T> xx = la.in(x.x, x.y), yy = lf.in(y.x, y.y);
+            cx<T> p = mode == 1 ? cmulc(xx, yy) : cmul(xx, yy);
+            S2 o;
+            o.x = (S)Loc2<T>::out(p.r, la.esc + lf.esc);
+            o.y = (S)Loc2<T>::out(p.i, la.esc + lf.esc);
+            out[idx] = o;
+        }
+    }
+}
+
+// Hermitian weighting of half spectra (n_half bins per line, real length nreal):
+// bins 1 .. ceil(nreal/2)-1 are multiplied by w; DC (and Nyquist for even
+// nreal) keep their real part and lose the imaginary part when drop_im
+template <class T>
+__global__ void k_half_weight(typename Traits<T>::S2 *__restrict__ x, long long lines, long long n_half,
+                              long long nreal, typename Traits<T>::S w, int drop_im)
+{
+    using S = typename Traits<T>::S;
+    const long long total = lines * n_half;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        long long k = idx % n_half;
+        bool edge = k == 0 || (nreal % 2 == 0 && k == nreal / 2);
+        if (edge) {
+            if (drop_im) x[idx].y = S(0);
+        } else {
+            x[idx].x *= w;  // w is 2 or 1/2: exact
+            x[idx].y *= w;
         }
     }
 }

@@ -22,6 +22,15 @@ template <class Tag> struct Launch {
     static cudaError_t convert64(const void *in, void *out, long long n);
     static cudaError_t gather(const IODesc &io, const MapDesc &mp, cudaStream_t st);
     static cudaError_t scatter(const IODesc &io, const MapDesc &mp, cudaStream_t st);
+    // FFT convolution helpers on the storage type of the arithmetic
+    static cudaError_t pad2d(const void *in, void *out, long long B, long long H, long long W, long long P0,
+                             long long P1, long long r0, long long c0, cudaStream_t st);
+    static cudaError_t crop2d(const void *in, void *out, long long B, long long H, long long W, long long P0,
+                              long long P1, long long r0, long long c0, cudaStream_t st);
+    static cudaError_t spec_mul(const void *a, const void *f, void *out, long long B, long long nf, long long n,
+                                int mode, cudaStream_t st);
+    static cudaError_t half_weight(void *x, long long lines, long long n_half, long long nreal, double w,
+                                   int drop_im, cudaStream_t st);
 };
 
 // FP64 helpers for Bluestein tables (built in ig_inst_df.cu)

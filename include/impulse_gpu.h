@@ -147,6 +147,40 @@ int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff
                   const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int forward,
                   const void *data_in, void *data_out, double fct, void *stream);
 
+/* ---- adjoints of the real transforms --------------------------------------
+ * Gradients of a real loss through r2c / c2r (device pointers).  With g the
+ * gradient with respect to (Re X, Im X) packed as complex:
+ *   adjoint of r2c(axes, forward): x_bar = c2r(axes, !forward) of g with the
+ *     inner bins of the last axis halved;
+ *   adjoint of c2r(axes, forward): g_bar = r2c(axes, !forward) of y_bar with
+ *     the inner bins of the last axis doubled (the Hermitian 2x weighting).
+ * No counterpart in the reference (PocketFFT has no adjoints); shapes and
+ * byte strides follow pocketfft::r2c / c2r (pocketfft_hdronly.h:3334, 3366). */
+int ig_r2c_adjoint_device(int dtype, size_t ndim, const size_t *shape_in, const ptrdiff_t *stride_g,
+                          const ptrdiff_t *stride_x, size_t naxes, const size_t *axes, int forward, const void *g,
+                          void *x, double fct, void *stream);
+int ig_c2r_adjoint_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *stride_y,
+                          const ptrdiff_t *stride_g, size_t naxes, const size_t *axes, int forward, const void *y,
+                          void *g, double fct, void *stream);
+
+/* ---- differentiable FFT convolution -----------------------------------------
+ * 'same' 2-D convolution of `batch` real H x W images with odd K x K filters
+ * (one shared filter or one per image), zero padded to pad_rows x pad_cols
+ * (0 = smallest 2^a3^b5^c7^d11^e >= size + K - 1) and computed as
+ * c2r(r2c(x) * r2c(k)).  forward(x, k) -> y; backward(x, k, gy) -> gx, gk
+ * (either may be NULL).  With recompute = 1 the backward recomputes the
+ * spectra of x and k instead of keeping them from the forward.  Contiguous
+ * row-major device arrays: x, y, gy, gx [batch][H][W]; k, gk [nfilters][K][K].
+ * No counterpart in the reference (impulse convolves directly, signal.nim:594). */
+typedef struct ig_fftconv_i *ig_fftconv;
+ig_fftconv ig_fftconv_create(int dtype, size_t batch, size_t height, size_t width, size_t nfilters, size_t ksize,
+                             size_t pad_rows, size_t pad_cols, int recompute);
+void ig_fftconv_destroy(ig_fftconv conv);
+int ig_fftconv_padded_size(ig_fftconv conv, size_t *rows, size_t *cols);
+int ig_fftconv_forward(ig_fftconv conv, const void *x, const void *k, void *y, void *stream);
+int ig_fftconv_backward(ig_fftconv conv, const void *x, const void *k, const void *gy, void *gx, void *gk,
+                        void *stream);
+
 /* ---- engine control ------------------------------------------------------ */
 /* Select the arithmetic used for IG_F64 data: 0 = double-float (default;
  * FP32-pair butterflies, ~48-bit significand, for GB300's narrow FP64
