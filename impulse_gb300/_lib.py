@@ -72,6 +72,12 @@ SIGNATURES = {
     "ig_fftconv_padded_size": (C.c_int, [_vp, C.POINTER(_sz), C.POINTER(_sz)]),
     "ig_fftconv_forward": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "ig_fftconv_backward": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ig_make_multi_plan": (_vp, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_sz), C.c_int, C.c_double]),
+    "ig_destroy_multi_plan": (None, [_vp]),
+    "ig_multi_info": (C.c_int, [_vp, C.POINTER(_sz), C.POINTER(_sz), C.POINTER(_sz)]),
+    "ig_multi_exec_device": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "ig_multi_exec_graph": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "ig_multi_exec_loop_device": (C.c_int, [_vp, _vp, _vp, _vp]),
     "ig_set_f64_arith": (C.c_int, [C.c_int]),
     "ig_release_caches": (None, []),
     "ig_launch_count": (C.c_ulonglong, [C.c_int]),

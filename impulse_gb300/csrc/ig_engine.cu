@@ -526,13 +526,23 @@ static void contig_side(IODesc &io, bool out, char *base, long long es, long lon
 // twiddle, then row FFTs of length N2 written transposed).  io describes
 // the user-facing sides with kinds IN_C/IN_R/IN_P and OUT_C/OUT_R/OUT_P and
 // at most two batch dims; `B` is a scratch of nlines * M complex elements.
+static void fourstep_passes(const Core &c, const IODesc &io, char *B, IODesc &p1, IODesc &p2);
+
 static void run_fourstep(const Core &c, const IODesc &io, char *B, cudaStream_t st)
+{
+    IODesc p1, p2;
+    fourstep_passes(c, io, B, p1, p2);
+    launch_smem(c.a, c.c1->d, p1, st);
+    launch_smem(c.a, c.c2->d, p2, st);
+}
+
+static void fourstep_passes(const Core &c, const IODesc &io, char *B, IODesc &p1, IODesc &p2)
 {
     const long long N1 = c.N1, N2 = c.N2, M = c.M;
     const long long ES = 2 * (long long)store_real_bytes(c.a);
     const long long nl = io.nlines;
     // pass 1: columns
-    IODesc p1 = io;
+    p1 = io;
     const long long ub_in = io.is;  // bytes between units
     p1.nlines = nl * N2;
     p1.bn[0] = N2;
@@ -563,9 +573,8 @@ static void run_fourstep(const Core &c, const IODesc &io, char *B, cudaStream_t 
     p1.tw4lo = c.wlo;
     p1.cols_in = 1;
     p1.cols_out = 1;
-    launch_smem(c.a, c.c1->d, p1, st);
     // pass 2: rows, transposed write
-    IODesc p2 = io;
+    p2 = io;
     const long long ub_out = io.os;
     p2.in = B;
     p2.in_kind = IN_C;
@@ -592,7 +601,6 @@ static void run_fourstep(const Core &c, const IODesc &io, char *B, cudaStream_t 
         p2.mul_a = 1;
         p2.mul_b = N1;
     }
-    launch_smem(c.a, c.c2->d, p2, st);
 }
 
 // Run a complex core of any kind.  io: user-facing sides, kinds, pre/post,
@@ -1707,6 +1715,298 @@ int ig_fftconv_backward(ig_fftconv c, const void *x, const void *k, const void *
             }
         }
         if (c->recompute) c->have_spectra = false;
+    });
+}
+
+// ---- batched transforms of uneven lengths ---------------------------------------
+// Transforms whose length fits one CTA are grouped by length (lines at
+// arbitrary offsets through per-line offset tables); four-step transforms
+// contribute a column-pass group and a row-pass group; all run through the
+// persistent work-list kernel in two launches (phase 0: single-CTA groups and
+// column passes; phase 1: row passes).  Lengths needing Bluestein over a
+// multi-pass core run on the general path.  The whole sequence can be
+// captured once into a CUDA graph.
+struct MultiPhase {
+    std::vector<WorkGroup> groups;
+    std::vector<long long> prefix;
+    std::unique_ptr<DevBuf> d_groups, d_prefix;
+    unsigned long long total = 0;
+    size_t smem = 0;
+};
+
+struct ig_multi_plan_i {
+    Arith a;
+    int dtype, fwd;
+    double fct;
+    std::vector<long long> len, off;
+    std::vector<std::shared_ptr<Core>> cores;
+    MultiPhase ph[2];
+    std::vector<std::unique_ptr<DevBuf>> tables;
+    std::vector<long long> general;
+    std::unique_ptr<DevBuf> scratch, counter;
+    size_t n_wl = 0, n_4s = 0;
+    cudaGraphExec_t gexec = nullptr;
+    const void *g_in = nullptr;
+    void *g_out = nullptr;
+    cudaStream_t g_st = nullptr;
+    ~ig_multi_plan_i()
+    {
+        if (gexec) cudaGraphExecDestroy(gexec);
+    }
+};
+
+static const int kWorklistThreads = 512;
+
+static void worklist_fit(Arith a, WorkGroup &g, size_t phase_smem)
+{
+    g.P.E = 16;
+    const long long tpl = (g.P.L + 15) / 16;
+    const long long line_bytes = (long long)g.P.LS * (long long)slot_bytes(a);
+    long long lpc = std::min<long long>(kMaxLinesPerCta, kWorklistThreads / tpl);
+    lpc = std::min<long long>(lpc, std::max<long long>(1, (long long)phase_smem / line_bytes));
+    lpc = std::max<long long>(1, std::min<long long>(lpc, g.io.nlines));
+    g.io.lpc = (int)lpc;
+    g.io.tpl = (int)tpl;
+    set_line_divs(g.io);
+}
+
+static void finish_phase(Arith a, MultiPhase &ph)
+{
+    if (ph.groups.empty()) return;
+    size_t smem = 0;
+    for (auto &g : ph.groups) smem = std::max(smem, (size_t)g.P.LS * slot_bytes(a));
+    smem = std::max<size_t>(smem, std::min<size_t>((size_t)max_smem(), 96 * 1024));
+    smem = std::min<size_t>(smem, (size_t)max_smem());
+    ph.smem = smem;
+    ph.prefix.clear();
+    unsigned long long tot = 0;
+    for (auto &g : ph.groups) {
+        worklist_fit(a, g, smem);
+        ph.prefix.push_back((long long)tot);
+        tot += (unsigned long long)((g.io.nlines + g.io.lpc - 1) / g.io.lpc);
+    }
+    ph.total = tot;
+    ph.d_groups.reset(new DevBuf(ph.groups.size() * sizeof(WorkGroup)));
+    ph.d_prefix.reset(new DevBuf(ph.prefix.size() * sizeof(long long)));
+    ck(cudaMemcpy(ph.d_groups->p, ph.groups.data(), ph.groups.size() * sizeof(WorkGroup), cudaMemcpyHostToDevice),
+       "work list upload");
+    ck(cudaMemcpy(ph.d_prefix->p, ph.prefix.data(), ph.prefix.size() * sizeof(long long), cudaMemcpyHostToDevice),
+       "work list upload");
+}
+
+static void multi_launch(ig_multi_plan_i &m, const void *in, void *out, cudaStream_t st)
+{
+    const int smcount = [] {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device_id());
+        return v > 0 ? v : 1;
+    }();
+    ck(cudaMemsetAsync(m.counter->p, 0, 2 * sizeof(unsigned long long), st), "work list counter");
+    for (int k = 0; k < 2; ++k) {
+        MultiPhase &ph = m.ph[k];
+        if (!ph.total) continue;
+        int grid = (int)std::min<unsigned long long>((unsigned long long)smcount, ph.total);
+        unsigned long long *ctr = (unsigned long long *)m.counter->p + k;
+        void *scr = m.scratch ? m.scratch->p : nullptr;
+        cudaError_t e =
+            m.a == A_F32 ? Launch<TagF32>::fft_worklist((const WorkGroup *)ph.d_groups->p,
+                                                        (const long long *)ph.d_prefix->p, (int)ph.groups.size(),
+                                                        ph.total, ctr, in, out, scr, grid, ph.smem, st)
+          : m.a == A_DF  ? Launch<TagDF>::fft_worklist((const WorkGroup *)ph.d_groups->p,
+                                                       (const long long *)ph.d_prefix->p, (int)ph.groups.size(),
+                                                       ph.total, ctr, in, out, scr, grid, ph.smem, st)
+                         : Launch<TagF64>::fft_worklist((const WorkGroup *)ph.d_groups->p,
+                                                        (const long long *)ph.d_prefix->p, (int)ph.groups.size(),
+                                                        ph.total, ctr, in, out, scr, grid, ph.smem, st);
+        ck(e, "work list launch");
+        count_launch();
+    }
+    const long long es = 2 * (long long)store_real_bytes(m.a);
+    for (long long i : m.general) {
+        Lines ln = contiguous_lines((const char *)in + m.off[i] * es, (char *)out + m.off[i] * es, 1, m.len[i],
+                                    m.len[i], es, es);
+        exec_op(m.a, OP_C2C, m.len[i], ln, m.fwd, m.fct, st);
+    }
+}
+
+ig_multi_plan ig_make_multi_plan(int dtype, size_t count, const size_t *lengths, const size_t *offsets, int forward,
+                                 double fct)
+{
+    ig_multi_plan plan = nullptr;
+    guarded([&] {
+        if (dtype != IG_F64 && dtype != IG_F32) raise(IG_EINVAL, "bad dtype");
+        if (!count || !lengths) raise(IG_EINVAL, "empty transform list");
+        auto m = std::make_unique<ig_multi_plan_i>();
+        m->a = arith_for(dtype);
+        m->dtype = dtype;
+        m->fwd = forward;
+        m->fct = fct;
+        const long long es = 2 * (long long)store_real_bytes(m->a);
+        long long pos = 0;
+        for (size_t i = 0; i < count; ++i) {
+            if (!lengths[i]) raise(IG_EZERO_LEN, "zero-length FFT requested");
+            m->len.push_back((long long)lengths[i]);
+            m->off.push_back(offsets ? (long long)offsets[i] : pos);
+            pos += (long long)lengths[i];
+        }
+        // group single-CTA lengths; collect four-step and general transforms
+        std::map<long long, std::vector<long long>> by_len;
+        std::vector<long long> four;
+        for (size_t i = 0; i < count; ++i) {
+            auto c = get_core(m->a, m->len[i], false);
+            m->cores.push_back(c);
+            if (c->kind == 0) by_len[m->len[i]].push_back((long long)i);
+            else if (c->kind == 1) four.push_back((long long)i);
+            else m->general.push_back((long long)i);
+        }
+        for (auto &kv : by_len) {
+            const long long L = kv.first;
+            const auto &ids = kv.second;
+            std::vector<long long> lo(ids.size());
+            for (size_t j = 0; j < ids.size(); ++j) lo[j] = m->off[ids[j]] * es;
+            m->tables.emplace_back(new DevBuf(lo.size() * sizeof(long long)));
+            ck(cudaMemcpy(m->tables.back()->p, lo.data(), lo.size() * sizeof(long long), cudaMemcpyHostToDevice),
+               "offset table");
+            WorkGroup g;
+            memset(&g, 0, sizeof g);
+            g.P = m->cores[ids[0]]->d;
+            g.io = blank_io();
+            g.io.loff_in = g.io.loff_out = (const long long *)m->tables.back()->p;
+            g.io.nlines = (long long)ids.size();
+            g.io.bn[0] = g.io.nlines;
+            g.io.is = g.io.os = es;
+            g.io.in_kind = IN_C;
+            g.io.out_kind = OUT_C;
+            g.io.cnt_in = g.io.cnt_out = (int)L;
+            g.io.nreal = L;
+            g.io.fwd = forward;
+            g.io.fct = fct;
+            g.in_base = 0;
+            g.out_base = 1;
+            m->ph[0].groups.push_back(g);
+            m->n_wl += ids.size();
+        }
+        long long soff = 0;
+        for (long long i : four) soff += m->len[i];
+        if (soff) m->scratch.reset(new DevBuf((size_t)(soff * es)));
+        soff = 0;
+        for (long long i : four) {
+            const Core &c = *m->cores[i];
+            IODesc io = blank_io();
+            io.in = (const char *)(m->off[i] * es);  // offsets from the bases
+            io.out = (char *)(m->off[i] * es);
+            io.is = io.os = es;
+            io.nlines = 1;
+            io.bn[0] = 1;
+            io.bsi[0] = io.bso[0] = c.M * es;
+            io.in_kind = IN_C;
+            io.out_kind = OUT_C;
+            io.cnt_in = io.cnt_out = (int)c.M;
+            io.nreal = c.M;
+            io.fwd = forward;
+            io.fct = fct;
+            IODesc p1, p2;
+            fourstep_passes(c, io, (char *)(soff * es), p1, p2);
+            WorkGroup g1, g2;
+            memset(&g1, 0, sizeof g1);
+            memset(&g2, 0, sizeof g2);
+            g1.P = c.c1->d;
+            g1.io = p1;
+            g1.in_base = 0;
+            g1.out_base = 2;
+            g2.P = c.c2->d;
+            g2.io = p2;
+            g2.in_base = 2;
+            g2.out_base = 1;
+            m->ph[0].groups.push_back(g1);
+            m->ph[1].groups.push_back(g2);
+            soff += c.M;
+            ++m->n_4s;
+        }
+        finish_phase(m->a, m->ph[0]);
+        finish_phase(m->a, m->ph[1]);
+        m->counter.reset(new DevBuf(2 * sizeof(unsigned long long)));
+        int optin = max_smem() + 1024;
+        static std::once_flag once[3];
+        std::call_once(once[m->a], [&] {
+            cudaError_t e = m->a == A_F32 ? Launch<TagF32>::set_max_smem(optin)
+                          : m->a == A_DF  ? Launch<TagDF>::set_max_smem(optin)
+                                          : Launch<TagF64>::set_max_smem(optin);
+            ck(e, "cudaFuncSetAttribute");
+        });
+        plan = m.release();
+    });
+    return plan;
+}
+
+void ig_destroy_multi_plan(ig_multi_plan plan) { delete plan; }
+
+int ig_multi_info(ig_multi_plan plan, size_t *n_worklist, size_t *n_fourstep, size_t *n_general)
+{
+    if (!plan) return IG_EINVAL;
+    if (n_worklist) *n_worklist = plan->n_wl;
+    if (n_fourstep) *n_fourstep = plan->n_4s;
+    if (n_general) *n_general = plan->general.size();
+    return IG_OK;
+}
+
+int ig_multi_exec_device(ig_multi_plan plan, const void *in, void *out, void *stream)
+{
+    return guarded([&] {
+        if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        multi_launch(*plan, in, out, as_stream(stream));
+    });
+}
+
+// Capture the work-list sequence for (in, out) into a CUDA graph once, then
+// replay it.  The first call runs the sequence eagerly (sizing every
+// workspace) before capturing; `stream` must not be the legacy default stream.
+int ig_multi_exec_graph(ig_multi_plan plan, const void *in, void *out, void *stream)
+{
+    return guarded([&] {
+        if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        cudaStream_t st = as_stream(stream);
+        if (!st) raise(IG_EINVAL, "graph capture needs a created stream, not the default stream");
+        if (!plan->gexec || plan->g_in != in || plan->g_out != out || plan->g_st != st) {
+            if (plan->gexec) {
+                cudaGraphExecDestroy(plan->gexec);
+                plan->gexec = nullptr;
+            }
+            multi_launch(*plan, in, out, st);
+            ck(cudaStreamSynchronize(st), "eager run before capture");
+            cudaGraph_t graph = nullptr;
+            ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+            try {
+                multi_launch(*plan, in, out, st);
+            } catch (...) {
+                cudaStreamEndCapture(st, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                throw;
+            }
+            ck(cudaStreamEndCapture(st, &graph), "end capture");
+            cudaError_t e = cudaGraphInstantiate(&plan->gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            ck(e, "graph instantiate");
+            plan->g_in = in;
+            plan->g_out = out;
+            plan->g_st = st;
+        }
+        ck(cudaGraphLaunch(plan->gexec, st), "graph launch");
+        count_launch();
+    });
+}
+
+// Reference launch pattern: one call of the single-transform path per transform.
+int ig_multi_exec_loop_device(ig_multi_plan plan, const void *in, void *out, void *stream)
+{
+    return guarded([&] {
+        if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        const long long es = 2 * (long long)store_real_bytes(plan->a);
+        for (size_t i = 0; i < plan->len.size(); ++i) {
+            Lines ln = contiguous_lines((const char *)in + plan->off[i] * es, (char *)out + plan->off[i] * es, 1,
+                                        plan->len[i], plan->len[i], es, es);
+            exec_op(plan->a, OP_C2C, plan->len[i], ln, plan->fwd, plan->fct, as_stream(stream));
+        }
     });
 }
 

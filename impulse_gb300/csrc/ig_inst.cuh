@@ -30,8 +30,23 @@ template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
     if (e != cudaSuccess) return e;
     e = cudaFuncGetAttributes(&fa, k_fft_smem<T, 16>);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_fft_smem<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_fft_smem<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bytes - (int)fa.sharedSizeBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncGetAttributes(&fa, k_fft_worklist<T, 16>);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_fft_worklist<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 bytes - (int)fa.sharedSizeBytes);
+}
+template <class Tag>
+cudaError_t Launch<Tag>::fft_worklist(const WorkGroup *groups, const long long *prefix, int ngroups,
+                                      unsigned long long total, unsigned long long *counter, const void *in,
+                                      void *out, void *scr, int grid, size_t smem, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_fft_worklist<T, 16><<<grid, 512, smem, st>>>(groups, prefix, ngroups, total, counter, (const char *)in,
+                                                   (char *)out, (char *)scr);
+    return cudaGetLastError();
 }
 template <class Tag> cudaError_t Launch<Tag>::stage_tw(void *tw, int R, int ns)
 {

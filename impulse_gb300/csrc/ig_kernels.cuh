@@ -49,9 +49,11 @@ __device__ __forceinline__ unsigned fdiv(unsigned n, FastDiv f)
     return (unsigned)(((unsigned long long)n * f.m) >> f.s);
 }
 
-// byte offset of line l: l -> (l mod bn0, (l / bn0) mod bn1, l / (bn0 bn1))
+// byte offset of line l: from the offset tables when present, else
+// l -> (l mod bn0, (l / bn0) mod bn1, l / (bn0 bn1)) over the batch dims
 __device__ __forceinline__ long long line_off(const IODesc &io, long long l, bool out)
 {
+    if (out ? io.loff_out != nullptr : io.loff_in != nullptr) return out ? io.loff_out[l] : io.loff_in[l];
     const unsigned lu = (unsigned)l;
     const unsigned q0 = fdiv(lu, io.fb0);
     const unsigned i0 = lu - q0 * (unsigned)io.bn[0];
@@ -234,8 +236,13 @@ __device__ __forceinline__ void store_unit(const IODesc &io, char *base, int u, 
     }
 }
 
+// One block of lines: lines [blk * lpc, blk * lpc + lpc) of (P, io), with the
+// input / output base pointers given explicitly (the persistent work-list
+// kernel keeps its groups' pointers relative to per-launch bases).  Threads
+// beyond lpc * tpl take part only in the barriers.
 template <class T, int E>
-__global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
+__device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, long long blk, const char *in_base,
+                                          char *out_base)
 {
     using S = typename Traits<T>::S;
     using S2 = typename Traits<T>::S2;
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
     __shared__ int s_rescale;
 
     const int lpc = io.lpc, tpl = io.tpl, pad = P.pad;
-    const long long line0 = (long long)blockIdx.x * lpc;
+    const long long line0 = blk * lpc;
     const int nl = (int)min((long long)lpc, io.nlines - line0);
     const int M = P.M;
     // backward Stockham cores run the forward stages on conjugated data
@@ -275,7 +282,7 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
         if (io.cols_in) { gi = threadIdx.x % lpc; ti = threadIdx.x / lpc; }
         else { gi = g; ti = t; }
         const bool act = gi < nl && ti < tpl;
-        const char *base = act ? io.in + line_off(io, line0 + gi, false) : nullptr;
+        const char *base = act ? in_base + line_off(io, line0 + gi, false) : nullptr;
         const bool has_b = act && paired && (2LL * line_i0(io, line0 + gi) + 1 < io.pair_n0);
         const char *base_b = base + io.pair_in;
         cx<T> *line = sm + (size_t)(act ? gi : 0) * P.LS;
@@ -458,7 +465,7 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
             const int esc = scaled ? s_esc[2 * g2] : 0;
             const int escb = scaled ? s_esc[2 * g2 + 1] : 0;
             const long long l = line0 + g2;
-            char *base = io.out + line_off(io, l, true);
+            char *base = out_base + line_off(io, l, true);
             const cx<T> *line = sm + (size_t)g2 * P.LS;
             const int i0l = (io.tw4 || io.mul || paired) ? line_i0(io, l) : 0;
             const bool has_b = paired && (2LL * i0l + 1 < io.pair_n0);
@@ -504,6 +511,45 @@ __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ Cor
                 store_unit<T, S, S2>(io, base, u, z, sc, esc);
             }
         }
+    }
+}
+
+template <class T, int E>
+__global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
+{
+    fft_block<T, E>(P, io, blockIdx.x, io.in, io.out);
+}
+
+// Persistent kernel over a device work list: item w is block (w - prefix[g])
+// of group g (binary search on prefix).  Groups hold their own core and line
+// descriptors; their in/out pointers are byte offsets from one of three
+// bases (0: input, 1: output, 2: scratch).  Items are claimed with one
+// atomic per block; the counter is reset before every launch.
+template <class T, int E>
+__global__ void __launch_bounds__(512, 1) k_fft_worklist(const WorkGroup *__restrict__ groups,
+                                                         const long long *__restrict__ prefix, int ngroups,
+                                                         unsigned long long total, unsigned long long *counter,
+                                                         const char *in, char *out, char *scr)
+{
+    __shared__ unsigned long long s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1ull);
+        __syncthreads();
+        const unsigned long long w = s_item;
+        __syncthreads();
+        if (w >= total) break;
+        int lo = 0, hi = ngroups - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if ((unsigned long long)prefix[mid] <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        const WorkGroup &G = groups[lo];
+        const char *ib = G.in_base == 0 ? in : G.in_base == 1 ? (const char *)out : (const char *)scr;
+        char *ob = G.out_base == 1 ? out : G.out_base == 2 ? scr : (char *)in;
+        fft_block<T, E>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]), ib + (size_t)G.io.in,
+                        ob + (size_t)G.io.out);
+        __syncthreads();
     }
 }
 

@@ -17,6 +17,9 @@ template <class Tag> struct Launch {
     // k_fft_smem with `lpc` lines of `tpl` threads per CTA and `smem` bytes
     static cudaError_t fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
     static cudaError_t set_max_smem(int bytes);
+    static cudaError_t fft_worklist(const WorkGroup *groups, const long long *prefix, int ngroups,
+                                    unsigned long long total, unsigned long long *counter, const void *in, void *out,
+                                    void *scr, int grid, size_t smem, cudaStream_t st);
     static cudaError_t stage_tw(void *tw, int R, int ns);
     static cudaError_t roots(void *out, long long count, unsigned long long mult, unsigned long long D);
     static cudaError_t convert64(const void *in, void *out, long long n);

@@ -73,6 +73,17 @@ struct IODesc {
     const void *mul;
     long long mul_a, mul_b;
     int mul_conj;
+    // per-line byte offsets (device arrays) replacing the batch dims when set
+    const long long *loff_in, *loff_out;
+};
+
+// one group of the persistent work list: a core, a line set, its block count;
+// io.in / io.out are byte offsets from base in_base / out_base
+// (0 input, 1 output, 2 scratch) of the launch
+struct WorkGroup {
+    CoreDesc P;
+    IODesc io;
+    int in_base, out_base;
 };
 
 // Elementwise line maps of the multi-pass paths (k_gather / k_scatter).

@@ -147,6 +147,27 @@ int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff
                   const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int forward,
                   const void *data_in, void *data_out, double fct, void *stream);
 
+/* ---- batched complex transforms of uneven lengths ---------------------------
+ * `count` complex transforms, transform i of lengths[i] at element offset
+ * offsets[i] (NULL = packed back to back) of the same layout in `in` and
+ * `out` (device pointers; may be equal).  The plan groups equal lengths that
+ * fit one CTA and runs them, with the column passes of longer four-step
+ * lengths, through one persistent work-list launch; a second launch runs the
+ * row passes; lengths needing Bluestein over a multi-pass core use the
+ * general path.  ig_multi_exec_graph captures that sequence into a CUDA graph
+ * on its first call for given pointers and replays it afterwards;
+ * ig_multi_exec_loop_device is the one-call-per-transform pattern, for
+ * comparison.  The reference transforms one line per call
+ * (pocketfft.nim:290-303). */
+typedef struct ig_multi_plan_i *ig_multi_plan;
+ig_multi_plan ig_make_multi_plan(int dtype, size_t count, const size_t *lengths, const size_t *offsets, int forward,
+                                 double fct);
+void ig_destroy_multi_plan(ig_multi_plan plan);
+int ig_multi_info(ig_multi_plan plan, size_t *n_worklist, size_t *n_fourstep, size_t *n_general);
+int ig_multi_exec_device(ig_multi_plan plan, const void *in, void *out, void *stream);
+int ig_multi_exec_graph(ig_multi_plan plan, const void *in, void *out, void *stream);
+int ig_multi_exec_loop_device(ig_multi_plan plan, const void *in, void *out, void *stream);
+
 /* ---- adjoints of the real transforms --------------------------------------
  * Gradients of a real loss through r2c / c2r (device pointers).  With g the
  * gradient with respect to (Re X, Im X) packed as complex:
