@@ -148,7 +148,7 @@ class ClockSampler:
 # --------------------------------------------------------------------------
 # CPU side: the reference's algorithm restated (oracle port) on host threads
 # --------------------------------------------------------------------------
-def cpu_sample_run(lengths, min_seconds=10.0, max_passes=50):
+def cpu_sample_run(lengths, min_seconds=10.0, max_passes=400):
     """Time the oracle's threaded halfcomplex transform on a bounded sample of the workload:
     each length at 1/64 of its batch.  Returns (GB/s, passes, seconds, sample description)."""
     from oracle import oracle as O  # CPU-baseline leg only
@@ -361,11 +361,142 @@ def run_ours(args, rank, world):
                  "bound_1e-6_log2N": all(e <= 1e-6 * math.log2(n) for n, e in errs)},
         "per_length_gbs": slow,
     }
+    if not args.no_extra:
+        result["uneven"] = run_uneven(lib, dev, world, args)
+        result["conv"] = run_conv(dev, args)
     if rank == 0 and world == 1 and not args.no_cpu:
         gbs, nth, sample, _ = cpu_sample_run(lengths, min_seconds=args.cpu_seconds)
         result["cpu_baseline"] = {"value": round(gbs, 3), "unit": "GB/s", "cores": nth, "kind": "port",
                                   "sample": sample}
     return result
+
+
+def run_uneven(lib, dev, world, args):
+    """20,000 complex transforms of uneven lengths (log-uniform, 90 % 7-smooth,
+    10 % prime, ~2^28 elements): FP32 through the captured work-list graph vs
+    the per-transform launch loop, and FP64 (double-float) through the graph."""
+    import torch
+    from impulse_gb300 import _lib as L
+    from impulse_gb300.batch import MultiFFT, uneven_lengths
+    lengths = uneven_lengths()
+    tot = sum(lengths)
+    s = torch.cuda.Stream(dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4)
+    out = {"transforms": len(lengths), "elements": tot}
+
+    def timed(plan, x, y, mode, reps):
+        with torch.cuda.stream(s):
+            for _ in range(2):
+                plan.run(x.data_ptr(), y.data_ptr(), s.cuda_stream, mode)
+            s.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                plan.run(x.data_ptr(), y.data_ptr(), s.cuda_stream, mode)
+            e1.record(s)
+            s.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    x32 = torch.complex(torch.randn(tot, generator=g, device=dev), torch.randn(tot, generator=g, device=dev))
+    y32 = torch.empty_like(x32)
+    t0 = time.perf_counter()
+    p32 = MultiFFT(lengths, L.IG_F32)
+    out["plan_s_fp32"] = round(time.perf_counter() - t0, 2)
+    out["paths"] = p32.info
+    ms32 = timed(p32, x32, y32, "graph", max(3, args.steps // 2))
+    ms32_loop = timed(p32, x32, y32, "loop", 2)
+    x64 = x32.to(torch.complex128)
+    y64 = torch.empty_like(x64)
+    p64 = MultiFFT(lengths, L.IG_F64)
+    ms64 = timed(p64, x64, y64, "graph", max(3, args.steps // 2))
+    err = float(torch.linalg.vector_norm(y32.to(torch.complex128) - y64) / torch.linalg.vector_norm(y64))
+    out.update({
+        "fp32_graph_ms": round(ms32, 3), "fp32_graph_gbs": round(2 * 8 * tot / (ms32 / 1e3) / 1e9, 1),
+        "fp32_loop_ms": round(ms32_loop, 3), "graph_vs_loop_speedup": round(ms32_loop / ms32, 2),
+        "fp64_graph_ms": round(ms64, 3), "fp64_graph_gbs": round(2 * 16 * tot / (ms64 / 1e3) / 1e9, 1),
+        "fp32_vs_fp64_speedup": round(ms64 / ms32, 3),
+        "rel_l2_fp32_vs_fp64": err, "bound_1e-6_log2_maxN": err <= 1e-6 * math.log2(max(lengths)),
+    })
+    del p32, p64, x32, y32, x64, y64
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_conv(dev, args):
+    """64 images 2048x2048 f32 convolved ('same') with 31x31 filters (one per
+    image), zero padded to 4096x4096: forward + backward (adjoints wrt image and
+    filter, spectra recomputed)."""
+    import torch
+    from impulse_gb300.fftconv import FFTConv2d
+    B, H, K, P = 64, 2048, 31, 4096
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    x = torch.rand((B, H, H), generator=g, device=dev)
+    k = torch.randn((B, K, K), generator=g, device=dev)
+    k = k / k.abs().sum(dim=(1, 2), keepdim=True)
+    gy = torch.randn((B, H, H), generator=g, device=dev)
+    op = FFTConv2d(B, H, H, K, B, torch.float32, recompute=True, pad=(P, P))
+    for _ in range(2):
+        op.forward(x, k)
+        op.backward(gy)
+    torch.cuda.synchronize()
+    reps = 3
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e2 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        op.forward(x, k)
+    e1.record()
+    for _ in range(reps):
+        op.backward(gy)
+    e2.record()
+    torch.cuda.synchronize()
+    fwd = e0.elapsed_time(e1) / reps
+    bwd = e1.elapsed_time(e2) / reps
+    io_bytes = 2 * 4 * B * H * H + 4 * B * K * K  # images in, result out, filters
+    del op, x, k, gy
+    torch.cuda.empty_cache()
+    return {"workload": "64 x 2048^2 f32, 31x31 filter per image, padded to 4096^2", "forward_ms": round(fwd, 2),
+            "backward_ms": round(bwd, 2), "images_per_s_fwd_bwd": round(B / ((fwd + bwd) / 1e3), 1),
+            "forward_io_gbs": round(io_bytes / (fwd / 1e3) / 1e9, 1)}
+
+
+PROFILE_CASES = {
+    # name: (kind, dtype, length, batch)
+    "rfft4096_f64": ("r", "f64", 4096, 16384),
+    "rfft4096_f32": ("r", "f32", 4096, 32768),
+    "c2c4096_f64": ("c", "f64", 4096, 8192),
+    "rfft2205_f64": ("r", "f64", 2205, 7609),
+    "rfft52272_f64": ("r", "f64", 52272, 321),
+    "rfft1009_f64": ("r", "f64", 1009, 16628),
+    "rfft65521_f64": ("r", "f64", 65521, 256),
+}
+
+
+def run_case(name):
+    """One launch sequence of a small named case, for profiler captures."""
+    import torch
+    from impulse_gb300 import _lib as L
+    kind, dt, n, b = PROFILE_CASES[name]
+    lib = L.load()
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    code = L.IG_F64 if dt == "f64" else L.IG_F32
+    if kind == "r":
+        x = torch.randn((b, n), device="cuda", dtype=torch.float64 if dt == "f64" else torch.float32)
+        plan = lib.ig_make_rfft_plan(n, code)
+        fn = lib.ig_rfft_exec_device
+    else:
+        x = torch.randn((b, n), device="cuda", dtype=torch.complex128 if dt == "f64" else torch.complex64)
+        plan = lib.ig_make_cfft_plan(n, code)
+        fn = lib.ig_cfft_exec_device
+    y = torch.empty_like(x)
+    torch.cuda.synchronize()
+    L.check(fn(plan, x.data_ptr(), y.data_ptr(), b, n, n, 1, 1.0, s))
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "ok": True}))
 
 
 def run_reference(args, rank, world):
@@ -417,7 +548,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-extra", action="store_true", help="skip the uneven-batch and convolution measurements")
+    ap.add_argument("--case", default=None, choices=sorted(PROFILE_CASES), help="run one small case once and exit")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":
