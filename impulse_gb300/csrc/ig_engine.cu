@@ -100,11 +100,16 @@ static int max_smem()
 // --------------------------------------------------------------------------
 // cores: complex transforms of one length
 // --------------------------------------------------------------------------
+// Radices for a Stockham length L.  Cores of up to 4096 points run 8
+// elements per thread, where a radix-16 stage would leave half the threads
+// idle, so they use radix 8 at most.
 static bool gpu_factor(long long L, std::vector<int> &rad)
 {
     rad.clear();
     long long n = L;
-    while (n % 16 == 0) { rad.push_back(16); n /= 16; }
+    const bool small = L <= 4096;
+    while (!small && n % 16 == 0) { rad.push_back(16); n /= 16; }
+    while (small && n % 8 == 0) { rad.push_back(8); n /= 8; }
     if (n % 8 == 0) { rad.push_back(8); n /= 8; }
     if (n % 4 == 0) { rad.push_back(4); n /= 4; }
     if (n % 2 == 0) { rad.push_back(2); n /= 2; }
@@ -283,6 +288,12 @@ static int choose_pad(const CoreDesc &d, int slot)
 static void finish_layout(Core &c, long long L, long long M)
 {
     c.d.E = elems_per_thread(L);
+    bool odd35 = false, odd711 = false;
+    for (int s = 0; s < c.d.nst; ++s) {
+        odd35 |= c.d.st[s].R == 3 || c.d.st[s].R == 5;
+        odd711 |= c.d.st[s].R == 7 || c.d.st[s].R == 11;
+    }
+    c.d.rs = odd711 ? RS_ALL : odd35 ? (c.d.E == 8 ? RS_P235 : RS_ALL) : RS_P2;
     c.d.pad = choose_pad(c.d, (int)slot_bytes(c.a));
     long long last = std::max(L, M + 1) - 1;
     c.d.LS = (int)(last + (last >> c.d.pad) + 1);

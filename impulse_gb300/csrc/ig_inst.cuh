@@ -13,30 +13,35 @@ template <> struct TagType<TagF64> { using T = double; };
 template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
     using T = typename TagType<Tag>::T;
-    long long grid = (io.nlines + io.lpc - 1) / io.lpc;
-    if (d.E == 8) k_fft_smem<T, 8><<<(unsigned)grid, (unsigned)(io.lpc * io.tpl), smem, st>>>(d, io);
-    else k_fft_smem<T, 16><<<(unsigned)grid, (unsigned)(io.lpc * io.tpl), smem, st>>>(d, io);
+    const unsigned grid = (unsigned)((io.nlines + io.lpc - 1) / io.lpc), blk = (unsigned)(io.lpc * io.tpl);
+    if (d.E == 8) {
+        if (d.rs == RS_P2) k_fft_smem<T, 8, RS_P2><<<grid, blk, smem, st>>>(d, io);
+        else if (d.rs == RS_P235) k_fft_smem<T, 8, RS_P235><<<grid, blk, smem, st>>>(d, io);
+        else k_fft_smem<T, 8, RS_ALL><<<grid, blk, smem, st>>>(d, io);
+    } else {
+        if (d.rs == RS_P2) k_fft_smem<T, 16, RS_P2><<<grid, blk, smem, st>>>(d, io);
+        else k_fft_smem<T, 16, RS_ALL><<<grid, blk, smem, st>>>(d, io);
+    }
     return cudaGetLastError();
+}
+template <class K> static cudaError_t set_smem_attr(K kernel, int bytes)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes - (int)fa.sharedSizeBytes);
 }
 template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
 {
     using T = typename TagType<Tag>::T;
-    // the dynamic limit excludes the kernel's static shared memory
-    cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, k_fft_smem<T, 8>);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_fft_smem<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             bytes - (int)fa.sharedSizeBytes);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncGetAttributes(&fa, k_fft_smem<T, 16>);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_fft_smem<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             bytes - (int)fa.sharedSizeBytes);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncGetAttributes(&fa, k_fft_worklist<T, 16>);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_fft_worklist<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                bytes - (int)fa.sharedSizeBytes);
+    // the dynamic limit excludes each kernel's static shared memory
+    cudaError_t e;
+    if ((e = set_smem_attr(k_fft_smem<T, 8, RS_P2>, bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_attr(k_fft_smem<T, 8, RS_P235>, bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_attr(k_fft_smem<T, 8, RS_ALL>, bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_attr(k_fft_smem<T, 16, RS_P2>, bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_attr(k_fft_smem<T, 16, RS_ALL>, bytes)) != cudaSuccess) return e;
+    return set_smem_attr(k_fft_worklist<T, 16>, bytes);
 }
 template <class Tag>
 cudaError_t Launch<Tag>::fft_worklist(const WorkGroup *groups, const long long *prefix, int ngroups,

@@ -131,22 +131,33 @@ __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int 
     __syncthreads();
 }
 
+// Radix classes: a kernel instantiation compiles only the radix cases of its
+// class, which keeps the register allocation of the whole kernel small
+// (the union of all radix cases spills).
+// radix 16 only in the 16-elements-per-thread variants (the planner caps
+// 8-element cores at radix 8)
+template <int E, int RS> __host__ __device__ constexpr bool rs_has(int R)
+{
+    return (R == 2 || R == 4 || R == 8) || (R == 16 && E == 16) || (RS >= RS_P235 && (R == 3 || R == 5)) ||
+           (RS == RS_ALL && (R == 7 || R == 11));
+}
+
 // Forward stages only: a backward transform runs them on conjugated data
 // (IFFT(x) = conj(FFT(conj(x)))), with the conjugations folded into the
 // prologue, the epilogue and the Bluestein steps.
-template <class T, int E>
+template <class T, int E, int RS>
 __device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl, int tpl, int g, int t)
 {
     for (int s = 0; s < P.nst; ++s) {
         switch (P.st[s].R) {
         case 2: stage<T, E, 2>(sm, P, s, nl, tpl, g, t); break;
-        case 3: stage<T, E, 3>(sm, P, s, nl, tpl, g, t); break;
         case 4: stage<T, E, 4>(sm, P, s, nl, tpl, g, t); break;
-        case 5: stage<T, E, 5>(sm, P, s, nl, tpl, g, t); break;
-        case 7: stage<T, E, 7>(sm, P, s, nl, tpl, g, t); break;
         case 8: stage<T, E, 8>(sm, P, s, nl, tpl, g, t); break;
-        case 11: stage<T, E, 11>(sm, P, s, nl, tpl, g, t); break;
-        case 16: stage<T, E, 16>(sm, P, s, nl, tpl, g, t); break;
+        case 16: if constexpr (rs_has<E, RS>(16)) stage<T, E, 16>(sm, P, s, nl, tpl, g, t); break;
+        case 3: if constexpr (rs_has<E, RS>(3)) stage<T, E, 3>(sm, P, s, nl, tpl, g, t); break;
+        case 5: if constexpr (rs_has<E, RS>(5)) stage<T, E, 5>(sm, P, s, nl, tpl, g, t); break;
+        case 7: if constexpr (rs_has<E, RS>(7)) stage<T, E, 7>(sm, P, s, nl, tpl, g, t); break;
+        case 11: if constexpr (rs_has<E, RS>(11)) stage<T, E, 11>(sm, P, s, nl, tpl, g, t); break;
         default: break;
         }
     }
@@ -240,7 +251,7 @@ __device__ __forceinline__ void store_unit(const IODesc &io, char *base, int u, 
 // input / output base pointers given explicitly (the persistent work-list
 // kernel keeps its groups' pointers relative to per-launch bases).  Threads
 // beyond lpc * tpl take part only in the barriers.
-template <class T, int E>
+template <class T, int E, int RS>
 __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, long long blk, const char *in_base,
                                           char *out_base)
 {
@@ -291,10 +302,24 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const int escb = (scaled && act) ? s_esc[2 * gi + 1] : 0;
             int emax = 0, emaxb = 0;
             if (act) {
-                for (int u = ti; u < io.cnt_in; u += tpl) {
-                    S re, im, rb = S(0), ib = S(0);
-                    load_unit<S, S2>(io, base, u, re, im);
-                    if (has_b) load_unit<S, S2>(io, base_b, u, rb, ib);
+                // chunks of 4 units: all loads of a chunk are issued before any is used
+                constexpr int CH = 4;
+                for (int u0 = ti; u0 < io.cnt_in; u0 += CH * tpl) {
+                S cre[CH], cim[CH], crb[CH], cib[CH];
+#pragma unroll
+                for (int c = 0; c < CH; ++c) {
+                    const int u = u0 + c * tpl;
+                    cre[c] = cim[c] = crb[c] = cib[c] = S(0);
+                    if (u < io.cnt_in) {
+                        load_unit<S, S2>(io, base, u, cre[c], cim[c]);
+                        if (has_b) load_unit<S, S2>(io, base_b, u, crb[c], cib[c]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < CH; ++c) {
+                    const int u = u0 + c * tpl;
+                    if (u >= io.cnt_in) break;
+                    S re = cre[c], im = cim[c], rb = crb[c], ib = cib[c];
                     if (io.conj_in) { im = negs(im); ib = negs(ib); }
                     // general_c2r reads only the real part of the DC and Nyquist bins
                     if (io.pre != PRE_NONE && (u == 0 || (io.pre == PRE_HERM_EVEN && u == M))) { im = S(0); ib = S(0); }
@@ -326,6 +351,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                             line[sp(M - u, pad)] = cc ? conjx(zm) : zm;
                         }
                     }
+                }
                 }
             }
             if (!scaled || attempt == 1) break;
@@ -407,7 +433,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 }
             }
             if (P.blue) __syncthreads();
-            run_stages<T, E>(sm, P, nl, tpl, g, t);
+            run_stages<T, E, RS>(sm, P, nl, tpl, g, t);
         }
         if (P.blue) {
             if (g < nl)
@@ -514,10 +540,10 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     }
 }
 
-template <class T, int E>
+template <class T, int E, int RS>
 __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
 {
-    fft_block<T, E>(P, io, blockIdx.x, io.in, io.out);
+    fft_block<T, E, RS>(P, io, blockIdx.x, io.in, io.out);
 }
 
 // Persistent kernel over a device work list: item w is block (w - prefix[g])
@@ -547,7 +573,7 @@ __global__ void __launch_bounds__(512, 1) k_fft_worklist(const WorkGroup *__rest
         const WorkGroup &G = groups[lo];
         const char *ib = G.in_base == 0 ? in : G.in_base == 1 ? (const char *)out : (const char *)scr;
         char *ob = G.out_base == 1 ? out : G.out_base == 2 ? scr : (char *)in;
-        fft_block<T, E>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]), ib + (size_t)G.io.in,
+        fft_block<T, E, RS_ALL>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]), ib + (size_t)G.io.in,
                         ob + (size_t)G.io.out);
         __syncthreads();
     }

@@ -19,6 +19,11 @@ struct StageDesc {
     FastDiv fns;    // division by ns
 };
 
+// radix classes of the kernel variants
+constexpr int RS_P2 = 0;   // 2, 4, 8, 16
+constexpr int RS_P235 = 1; // 2, 4, 8, 16, 3, 5
+constexpr int RS_ALL = 2;  // 2, 3, 4, 5, 7, 8, 11, 16
+
 enum InKind { IN_C = 0, IN_R = 1, IN_P = 2, IN_HC = 3 };
 enum OutKind { OUT_C = 0, OUT_R = 1, OUT_P = 2, OUT_HC = 3 };
 enum PreKind { PRE_NONE = 0, PRE_HERM_EVEN = 1, PRE_HERM_ODD = 2 };
@@ -31,6 +36,7 @@ struct CoreDesc {
     int blue; // 1: Bluestein core
     int pad;  // shared-memory padding: slot i is stored at i + (i >> pad)
     int E;    // complex elements per thread (kernel variant 8 or 16): L / E threads per line
+    int rs;   // radix class of the kernel variant (0: 2/4/8/16, 1: + 3/5, 2: all)
     int nst;
     StageDesc st[kMaxStages];
     const void *tw;     // cx<T> stage twiddles, forward sign
