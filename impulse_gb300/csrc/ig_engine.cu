@@ -477,7 +477,7 @@ static IODesc blank_io()
 // scratch for the multi-pass paths: per (device, stream), grow-only
 // --------------------------------------------------------------------------
 struct Scratch {
-    std::unique_ptr<DevBuf> buf[3];
+    std::unique_ptr<DevBuf> buf[4];
     void *get(int i, size_t bytes)
     {
         if (!buf[i] || buf[i]->bytes < bytes) {
@@ -515,6 +515,27 @@ static void launch_map(Arith a, bool gather, const IODesc &io_in, const MapDesc 
 }
 
 static void run_complex(const Core &c, const IODesc &io, cudaStream_t st);
+
+static void launch_pair_map(Arith a, int which, const IODesc &io_in, const MapDesc &mp, int *esc, cudaStream_t st)
+{
+    IODesc io = io_in;
+    set_line_divs(io);
+    cudaError_t e;
+    if (which == 0)
+        e = a == A_F32 ? Launch<TagF32>::line_exp(io, esc, st)
+          : a == A_DF  ? Launch<TagDF>::line_exp(io, esc, st)
+                       : Launch<TagF64>::line_exp(io, esc, st);
+    else if (which == 1)
+        e = a == A_F32 ? Launch<TagF32>::gather_pair(io, mp, esc, st)
+          : a == A_DF  ? Launch<TagDF>::gather_pair(io, mp, esc, st)
+                       : Launch<TagF64>::gather_pair(io, mp, esc, st);
+    else
+        e = a == A_F32 ? Launch<TagF32>::scatter_pair(io, mp, esc, st)
+          : a == A_DF  ? Launch<TagDF>::scatter_pair(io, mp, esc, st)
+                       : Launch<TagF64>::scatter_pair(io, mp, esc, st);
+    ck(e, "paired line map");
+    count_launch();
+}
 
 // contiguous scratch lines as an IODesc side
 static void contig_side(IODesc &io, bool out, char *base, long long es, long long len, long long nl)
@@ -634,6 +655,56 @@ static void run_complex(const Core &c, const IODesc &io_all, cudaStream_t st)
         const long long nl = io.nlines;
         const long long ES = 2 * (long long)store_real_bytes(c.a);
         Scratch &scr = scratch_for(st);
+        if (io.pair) {
+            // two real lines per complex line: per-line scales, paired gather,
+            // complex core on contiguous scratch, paired scatter
+            const long long L = c.kind == 2 ? c.n2 : c.M;
+            int *esc = (int *)scr.get(3, (size_t)(2 * nl * sizeof(int)));
+            char *A = (char *)scr.get(0, (size_t)(nl * L * ES));
+            MapDesc mp{};
+            mp.kind = c.kind == 2 ? MAP_BLUE : MAP_PLAIN;
+            mp.M = c.M;
+            mp.scr_len = L;
+            mp.scr = A;
+            mp.chirp = c.chirp;
+            mp.fwd = io.fwd;
+            launch_pair_map(c.a, 0, io, mp, esc, st);
+            launch_pair_map(c.a, 1, io, mp, esc, st);
+            if (c.kind == 1) {
+                char *B = (char *)scr.get(1, (size_t)(nl * L * ES));
+                IODesc q = blank_io();
+                contig_side(q, false, A, ES, L, nl);
+                contig_side(q, true, A, ES, L, nl);
+                q.nlines = nl;
+                q.in_kind = IN_C;
+                q.out_kind = OUT_C;
+                q.cnt_in = q.cnt_out = (int)L;
+                q.nreal = L;
+                q.fwd = io.fwd;
+                run_fourstep(c, q, B, st);
+            } else {
+                for (int pass = 0; pass < 2; ++pass) {
+                    IODesc q = blank_io();
+                    contig_side(q, false, A, ES, L, nl);
+                    contig_side(q, true, A, ES, L, nl);
+                    q.nlines = nl;
+                    q.in_kind = IN_C;
+                    q.out_kind = OUT_C;
+                    q.cnt_in = q.cnt_out = (int)L;
+                    q.nreal = L;
+                    q.fwd = pass == 0 ? 1 : 0;
+                    if (pass == 0) {
+                        q.mul = c.chirpf;
+                        q.mul_a = 0;
+                        q.mul_b = 1;
+                        q.mul_conj = io.fwd ? 0 : 1;
+                    }
+                    run_complex(*c.sub, q, st);
+                }
+            }
+            launch_pair_map(c.a, 2, io, mp, esc, st);
+            continue;
+        }
         if (c.kind == 1) {
             const long long M = c.M;
             bool gath = io.pre != PRE_NONE || io.in_kind == IN_HC;
@@ -897,7 +968,7 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
         io.cnt_in = 1;
     }
     // odd real lengths on a single-CTA core: two real lines per complex line
-    if (N > 1 && N % 2 == 1 && op != OP_C2C && ln.bn[0] >= 2 && core->kind == 0) {
+    if (N > 1 && N % 2 == 1 && op != OP_C2C && ln.bn[0] >= 2) {
         io.pair = 1;
         io.pair_n0 = ln.bn[0];
         io.pair_in = ln.bsi[0];

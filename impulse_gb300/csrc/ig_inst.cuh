@@ -95,6 +95,26 @@ template <class Tag> cudaError_t Launch<Tag>::scatter(const IODesc &io, const Ma
     return cudaGetLastError();
 }
 
+template <class Tag> cudaError_t Launch<Tag>::line_exp(const IODesc &io, int *esc, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_line_exp<T><<<(unsigned)io.nlines, 256, 0, st>>>(io, esc);
+    return cudaGetLastError();
+}
+template <class Tag>
+cudaError_t Launch<Tag>::gather_pair(const IODesc &io, const MapDesc &mp, const int *esc, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_gather_pair<T><<<map_grid(io.nlines * mp.scr_len), 256, 0, st>>>(io, mp, esc);
+    return cudaGetLastError();
+}
+template <class Tag>
+cudaError_t Launch<Tag>::scatter_pair(const IODesc &io, const MapDesc &mp, const int *esc, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_scatter_pair<T><<<map_grid(io.nlines * (long long)io.cnt_out), 256, 0, st>>>(io, mp, esc);
+    return cudaGetLastError();
+}
 template <class Tag>
 cudaError_t Launch<Tag>::pad2d(const void *in, void *out, long long B, long long H, long long W, long long P0,
                                long long P1, long long r0, long long c0, cudaStream_t st)

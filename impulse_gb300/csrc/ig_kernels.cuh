@@ -762,6 +762,142 @@ __global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_consta
 }
 
 // ---------------------------------------------------------------------------
+// two real lines per complex line on the multi-pass paths
+// ---------------------------------------------------------------------------
+
+// exponent scale of each real line of a pair: the largest element of every
+// line is brought to [1, 2) (double-float) or near 1 (FP32) by 2^esc, so that
+// both lines of a pair keep their own relative accuracy
+template <class T>
+__global__ void k_line_exp(const __grid_constant__ IODesc io, int *__restrict__ esc)
+{
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    __shared__ int s_e[2];
+    if (threadIdx.x < 2) s_e[threadIdx.x] = 0;
+    __syncthreads();
+    const long long l = blockIdx.x;
+    const char *base = io.in + line_off(io, l, false);
+    const bool has_b = 2LL * line_i0(io, l) + 1 < io.pair_n0;
+    int ea = 0, eb = 0;
+    for (int u = threadIdx.x; u < io.cnt_in; u += blockDim.x) {
+        S re, im, rb = S(0), ib = S(0);
+        load_unit<S, S2>(io, base, u, re, im);
+        if (has_b) load_unit<S, S2>(io, base + io.pair_in, u, rb, ib);
+        int e1, e2, e3, e4, inf;
+        if constexpr (sizeof(S) == 8) {
+            e1 = dexp((double)re); e2 = dexp((double)im); e3 = dexp((double)rb); e4 = dexp((double)ib); inf = 0x7ff;
+        } else {
+            e1 = fexp((float)re); e2 = fexp((float)im); e3 = fexp((float)rb); e4 = fexp((float)ib); inf = 0xff;
+        }
+        ea = max(ea, max(e1 == inf ? 0 : e1, e2 == inf ? 0 : e2));
+        eb = max(eb, max(e3 == inf ? 0 : e3, e4 == inf ? 0 : e4));
+    }
+    if (ea) atomicMax(&s_e[0], ea);
+    if (eb) atomicMax(&s_e[1], eb);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int bias = sizeof(S) == 8 ? 1023 : 127;
+        esc[2 * l] = s_e[0] ? bias - s_e[0] : 0;
+        esc[2 * l + 1] = s_e[1] ? bias - s_e[1] : 0;
+    }
+}
+
+// gather of pairs: Z[u] = 2^ea A[u] + i 2^eb B[u] for real lines; for half
+// spectra Z[u] = A + iB (u < cnt), Z[u] = conj(A[M-u]) + i conj(B[M-u]) above;
+// times the chirp for MAP_BLUE; zero padded to scr_len
+template <class T>
+__global__ void k_gather_pair(const __grid_constant__ IODesc io, const __grid_constant__ MapDesc mp,
+                              const int *__restrict__ esc)
+{
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    const long long total = io.nlines * mp.scr_len;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long l = idx / mp.scr_len, u = idx - l * mp.scr_len;
+        S2 *dst = reinterpret_cast<S2 *>(mp.scr) + idx;
+        cx<T> z{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
+        if (u < mp.M) {
+            const char *base = io.in + line_off(io, l, false);
+            const bool has_b = 2LL * line_i0(io, l) + 1 < io.pair_n0;
+            const int ea = esc[2 * l], eb = esc[2 * l + 1];
+            const bool mirror = io.in_kind != IN_R && u >= io.cnt_in;
+            const int uu = (int)(mirror ? mp.M - u : u);
+            S ar, ai, br = S(0), bi = S(0);
+            load_unit<S, S2>(io, base, uu, ar, ai);
+            if (has_b) load_unit<S, S2>(io, base + io.pair_in, uu, br, bi);
+            if (io.conj_in) { ai = negs(ai); bi = negs(bi); }
+            if (io.in_kind != IN_R && uu == 0) { ai = S(0); bi = S(0); }
+            cx<T> A{Store<T>::in(ar, ea), Store<T>::in(ai, ea)};
+            cx<T> B{Store<T>::in(br, eb), Store<T>::in(bi, eb)};
+            if (io.in_kind == IN_R) z = cx<T>{A.r, B.r};
+            else if (!mirror) z = cx<T>{A.r - B.i, A.i + B.r};
+            else z = cx<T>{A.r + B.i, B.r - A.i};
+            if (mp.kind == MAP_BLUE) {
+                cx<T> c = reinterpret_cast<const cx<T> *>(mp.chirp)[u];
+                z = mp.fwd ? cmulc(z, c) : cmul(z, c);
+            }
+        }
+        S2 o;
+        o.x = (S)Loc2<T>::out(crenorm(z).r, 0);
+        o.y = (S)Loc2<T>::out(crenorm(z).i, 0);
+        *dst = o;
+    }
+}
+
+// scatter of pairs: forward -> A[k] = (Z[k] + conj(Z[M-k]))/2 to line a,
+// B[k] = -i (Z[k] - conj(Z[M-k]))/2 to line b; backward (OUT_R) -> Re Z to a,
+// Im Z to b; chirp first for MAP_BLUE; each line unscaled by its own 2^-esc
+template <class T>
+__global__ void k_scatter_pair(const __grid_constant__ IODesc io, const __grid_constant__ MapDesc mp,
+                               const int *__restrict__ esc)
+{
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    const long long cnt = io.cnt_out;
+    const long long total = io.nlines * cnt;
+    OutScale<T> sc;
+    sc.init(io.fct);
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long l = idx / cnt;
+        const int u = (int)(idx - l * cnt);
+        char *base = io.out + line_off(io, l, true);
+        const bool has_b = 2LL * line_i0(io, l) + 1 < io.pair_n0;
+        const int ea = esc[2 * l], eb = esc[2 * l + 1];
+        const S2 *src = reinterpret_cast<const S2 *>(mp.scr) + l * mp.scr_len;
+        const cx<T> *ch = reinterpret_cast<const cx<T> *>(mp.chirp);
+        auto fetch = [&](long long k) {
+            S2 a = src[k];
+            cx<T> z{Loc2<T>::in(a.x), Loc2<T>::in(a.y)};
+            if (mp.kind == MAP_BLUE) z = mp.fwd ? cmulc(z, ch[k]) : cmul(z, ch[k]);
+            return z;
+        };
+        if (io.out_kind == OUT_R) {
+            cx<T> z = fetch(u);
+            *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, ea);
+            if (has_b) *reinterpret_cast<S *>(base + io.pair_out + (long long)u * io.os) = sc.apply(z.i, eb);
+            continue;
+        }
+        cx<T> za, zb;
+        const cx<T> z1 = fetch(u);
+        if (u == 0) {
+            za = cx<T>{z1.r, RealOps<T>::k(0.0)};
+            zb = cx<T>{z1.i, RealOps<T>::k(0.0)};
+        } else {
+            const cx<T> z2 = conjx(fetch(mp.M - u));
+            cx<T> A = chalf(z1 + z2), D = chalf(z1 - z2);
+            za = crenorm(A);
+            zb = crenorm(cx<T>{D.i, -D.r});
+        }
+        if (io.conj_out) { za.i = -za.i; zb.i = -zb.i; }
+        store_unit<T, S, S2>(io, base, u, za, sc, ea);
+        if (has_b) store_unit<T, S, S2>(io, base + io.pair_out, u, zb, sc, eb);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FFT-convolution helpers (elementwise; storage type S, arithmetic T)
 // ---------------------------------------------------------------------------
 

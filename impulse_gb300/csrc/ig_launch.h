@@ -25,6 +25,10 @@ template <class Tag> struct Launch {
     static cudaError_t convert64(const void *in, void *out, long long n);
     static cudaError_t gather(const IODesc &io, const MapDesc &mp, cudaStream_t st);
     static cudaError_t scatter(const IODesc &io, const MapDesc &mp, cudaStream_t st);
+    // two real lines per complex line on the multi-pass paths
+    static cudaError_t line_exp(const IODesc &io, int *esc, cudaStream_t st);
+    static cudaError_t gather_pair(const IODesc &io, const MapDesc &mp, const int *esc, cudaStream_t st);
+    static cudaError_t scatter_pair(const IODesc &io, const MapDesc &mp, const int *esc, cudaStream_t st);
     // FFT convolution helpers on the storage type of the arithmetic
     static cudaError_t pad2d(const void *in, void *out, long long B, long long H, long long W, long long P0,
                              long long P1, long long r0, long long c0, cudaStream_t st);

@@ -84,7 +84,7 @@ def test_cpp_readme_r2c(engine):
     assert np.allclose(dOut, want, atol=1e-14)
 
 
-@pytest.mark.parametrize("n", [5, 101, 1009, 2205, 6075])
+@pytest.mark.parametrize("n", [5, 101, 1009, 2205, 6075, 8191, 29403, 65521])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_odd_lengths_paired_lines_keep_own_accuracy(engine, oracle_lib, n, dtype):
     """Odd real lengths run two lines per complex transform; each line keeps its
