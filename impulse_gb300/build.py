@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libimpulse_gpu.so")
-UNITS = ["ig_engine.cu", "ig_inst_f32.cu", "ig_inst_df.cu", "ig_inst_f64.cu"]
+UNITS = ["ig_engine.cu", "ig_inst_f32.cu", "ig_inst_df.cu", "ig_inst_f64.cu", "ig_inst_f32_e8.cu",
+         "ig_inst_f32_e16.cu", "ig_inst_df_e8.cu", "ig_inst_df_e16.cu", "ig_inst_f64_e8.cu", "ig_inst_f64_e16.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden"]
@@ -58,7 +59,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(run, jobs))
     if force or jobs or not os.path.exists(LIB):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        # -z defs: an unresolved symbol is a link error, not a load-time failure
+        cmd = [nvcc, *ARCH, "-shared", "-Xlinker", "-z,defs", "-o", LIB, *objs, "-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

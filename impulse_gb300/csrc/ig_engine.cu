@@ -216,9 +216,46 @@ static FastDiv make_fdiv(unsigned d)
     return f;
 }
 
+// fct as the kernels consume it: FP32 value, and m * 2^e with m in [1, 2)
+// split into two floats for double-float
+static void set_fct_parts(IODesc &io)
+{
+    io.fct_f = (float)io.fct;
+    if (io.fct == 0.0 || !std::isfinite(io.fct)) {
+        io.fct_h = (float)io.fct;
+        io.fct_l = 0.0f;
+        io.fct_e = 0;
+        return;
+    }
+    int ex = 0;
+    double m = std::frexp(io.fct, &ex);  // fct = m 2^ex, |m| in [0.5, 1)
+    m *= 2.0;
+    ex -= 1;
+    io.fct_h = (float)m;
+    io.fct_l = (float)(m - (double)io.fct_h);
+    io.fct_e = ex;
+}
+
+// layout class of the kernel variant for a line descriptor (the specialised
+// variants compile the common layouts without per-element runtime checks)
+static int choose_layout(Arith a, const IODesc &io)
+{
+    if (a == A_F64) return LAY_GEN;
+    const bool plain = !io.conj_in && !io.conj_out && !io.real_out && io.pre == PRE_NONE;
+    if (io.tw4 || io.mul)
+        return (plain && !io.pair && io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C) ? LAY_TW
+                                                                                                          : LAY_GEN;
+    if (!plain) return LAY_GEN;
+    if (!io.pair && io.in_kind == IN_C && io.out_kind == OUT_C && io.post == POST_NONE) return LAY_C2C;
+    if (!io.pair && io.in_kind == IN_C && io.out_kind == OUT_HC && io.post == POST_SPLIT) return LAY_R2HC;
+    if (io.pair && io.in_kind == IN_R && io.out_kind == OUT_HC && io.post == POST_PAIR) return LAY_PR2HC;
+    return LAY_GEN;
+}
+
 // line-number decomposition of the kernels uses 32-bit fast division
 static void set_line_divs(IODesc &io)
 {
+    set_fct_parts(io);
     if (io.nlines >= (1LL << 31) || io.bn[0] >= (1LL << 31) || io.bn[1] >= (1LL << 31))
         raise(IG_ETOOLARGE, "more than 2^31 lines in one launch");
     io.fb0 = make_fdiv((unsigned)std::max<long long>(1, io.bn[0]));
@@ -446,6 +483,7 @@ static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
     io.lpc = (int)lpc;
     io.tpl = (int)tpl;
     set_line_divs(io);
+    io.lay = choose_layout(a, io);
     size_t smem = (size_t)(lpc * line_bytes);
     static std::once_flag once[3];
     std::call_once(once[a], [&] {

@@ -10,19 +10,15 @@ template <> struct TagType<TagF32> { using T = float; };
 template <> struct TagType<TagDF> { using T = df; };
 template <> struct TagType<TagF64> { using T = double; };
 
+// k_fft_smem variants of one (arithmetic, elements-per-thread) pair live in
+// their own translation unit (ig_inst_<arith>_e<E>.cu) to compile in parallel
+template <class T, int E> cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
+template <class T, int E> cudaError_t set_smem_E(int bytes);
+
 template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
     using T = typename TagType<Tag>::T;
-    const unsigned grid = (unsigned)((io.nlines + io.lpc - 1) / io.lpc), blk = (unsigned)(io.lpc * io.tpl);
-    if (d.E == 8) {
-        if (d.rs == RS_P2) k_fft_smem<T, 8, RS_P2><<<grid, blk, smem, st>>>(d, io);
-        else if (d.rs == RS_P235) k_fft_smem<T, 8, RS_P235><<<grid, blk, smem, st>>>(d, io);
-        else k_fft_smem<T, 8, RS_ALL><<<grid, blk, smem, st>>>(d, io);
-    } else {
-        if (d.rs == RS_P2) k_fft_smem<T, 16, RS_P2><<<grid, blk, smem, st>>>(d, io);
-        else k_fft_smem<T, 16, RS_ALL><<<grid, blk, smem, st>>>(d, io);
-    }
-    return cudaGetLastError();
+    return d.E == 8 ? launch_fft_E<T, 8>(d, io, smem, st) : launch_fft_E<T, 16>(d, io, smem, st);
 }
 template <class K> static cudaError_t set_smem_attr(K kernel, int bytes)
 {
@@ -36,11 +32,8 @@ template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
     using T = typename TagType<Tag>::T;
     // the dynamic limit excludes each kernel's static shared memory
     cudaError_t e;
-    if ((e = set_smem_attr(k_fft_smem<T, 8, RS_P2>, bytes)) != cudaSuccess) return e;
-    if ((e = set_smem_attr(k_fft_smem<T, 8, RS_P235>, bytes)) != cudaSuccess) return e;
-    if ((e = set_smem_attr(k_fft_smem<T, 8, RS_ALL>, bytes)) != cudaSuccess) return e;
-    if ((e = set_smem_attr(k_fft_smem<T, 16, RS_P2>, bytes)) != cudaSuccess) return e;
-    if ((e = set_smem_attr(k_fft_smem<T, 16, RS_ALL>, bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_E<T, 8>(bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_E<T, 16>(bytes)) != cudaSuccess) return e;
     return set_smem_attr(k_fft_worklist<T, 16>, bytes);
 }
 template <class Tag>

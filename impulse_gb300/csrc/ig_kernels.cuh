@@ -172,25 +172,23 @@ __device__ __forceinline__ float fpow2(int e)  // 2^e, e in [-126, 127]
 __device__ __forceinline__ int fexp(float x) { return (int)((__float_as_uint(x) >> 23) & 0xff); }
 template <> struct OutScale<float> {
     float f;
-    __device__ void init(double fct) { f = (float)fct; }
+    __device__ void init(const IODesc &io) { f = io.fct_f; }
     __device__ float apply(float v, int esc) const { return esc ? v * (f * fpow2(-esc)) : v * f; }
 };
 template <> struct OutScale<double> {
     double f;
-    __device__ void init(double fct) { f = fct; }
+    __device__ void init(const IODesc &io) { f = io.fct; }
     __device__ double apply(double v, int) const { return v * f; }
 };
 template <> struct OutScale<df> {
     df m;
     int e;
-    __device__ void init(double fct)
+    __device__ void init(const IODesc &io)
     {
-        // fct = m * 2^e with m in [1, 2): the exponent is folded into the
-        // integer output conversion, so no FP64 instruction is needed
-        if (fct == 0.0) { m = df{0.f, 0.f}; e = 0; return; }
-        int be = dexp(fct);
-        e = be - 1023;
-        m = df_from_double(fct, -e);
+        // fct = m * 2^e with m in [1, 2) (split on the host): the exponent is
+        // folded into the integer output conversion
+        m = df{io.fct_h, io.fct_l};
+        e = io.fct_e;
     }
     __device__ double apply(df v, int esc) const { return df_to_double(v * m, esc - e); }
 };
@@ -251,7 +249,7 @@ __device__ __forceinline__ void store_unit(const IODesc &io, char *base, int u, 
 // input / output base pointers given explicitly (the persistent work-list
 // kernel keeps its groups' pointers relative to per-launch bases).  Threads
 // beyond lpc * tpl take part only in the barriers.
-template <class T, int E, int RS>
+template <class T, int E, int RS, int LAY>
 __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, long long blk, const char *in_base,
                                           char *out_base)
 {
@@ -275,7 +273,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     cx<T> *myline = sm + (size_t)(g < nl ? g : 0) * P.LS;
 
     // range scaling: double-float lines always, FP32 lines when two real lines share one complex line
-    const bool paired = io.pair != 0;
+    const bool paired = LAY == LAY_PR2HC || (LAY == LAY_GEN && io.pair != 0);
     const bool scaled = RAW || paired;
     if (scaled) {
         for (int i = threadIdx.x; i < 2 * lpc; i += blockDim.x) { s_esc[i] = 0; s_emax[i] = 0; }
@@ -301,7 +299,63 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const int esc = (scaled && act) ? s_esc[2 * gi] : 0;
             const int escb = (scaled && act) ? s_esc[2 * gi + 1] : 0;
             int emax = 0, emaxb = 0;
-            if (act) {
+            if (act && (LAY == LAY_C2C || LAY == LAY_R2HC || LAY == LAY_TW)) {
+                // complex units, no conjugation / Hermitian steps / pairs
+                constexpr int CH = 4;
+                const int cnt = io.cnt_in;
+                const long long is = io.is;
+                for (int u0 = ti; u0 < cnt; u0 += CH * tpl) {
+                    S2 v[CH];
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        const int u = u0 + c * tpl;
+                        if (u < cnt) v[c] = *reinterpret_cast<const S2 *>(base + (long long)u * is);
+                    }
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        const int u = u0 + c * tpl;
+                        if (u >= cnt) break;
+                        if constexpr (RAW) {
+                            int e1 = dexp(v[c].x), e2 = dexp(v[c].y);
+                            emax = max(emax, max(e1 == 0x7ff ? 0 : e1, e2 == 0x7ff ? 0 : e2));
+                        }
+                        cx<T> z{Store<T>::in(v[c].x, esc), Store<T>::in(v[c].y, esc)};
+                        line[sp(u, pad)] = cc ? conjx(z) : z;
+                    }
+                }
+            } else if (act && LAY == LAY_PR2HC) {
+                // two real lines -> (a, b)
+                constexpr int CH = 4;
+                const int cnt = io.cnt_in;
+                const long long is = io.is;
+                for (int u0 = ti; u0 < cnt; u0 += CH * tpl) {
+                    S va[CH], vb[CH];
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        const int u = u0 + c * tpl;
+                        va[c] = vb[c] = S(0);
+                        if (u < cnt) {
+                            va[c] = *reinterpret_cast<const S *>(base + (long long)u * is);
+                            if (has_b) vb[c] = *reinterpret_cast<const S *>(base_b + (long long)u * is);
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        const int u = u0 + c * tpl;
+                        if (u >= cnt) break;
+                        if constexpr (RAW) {
+                            int e1 = dexp(va[c]), e2 = dexp(vb[c]);
+                            emax = max(emax, e1 == 0x7ff ? 0 : e1);
+                            emaxb = max(emaxb, e2 == 0x7ff ? 0 : e2);
+                        } else {
+                            int e1 = fexp(va[c]), e2 = fexp(vb[c]);
+                            emax = max(emax, e1 == 0xff ? 0 : e1);
+                            emaxb = max(emaxb, e2 == 0xff ? 0 : e2);
+                        }
+                        line[sp(u, pad)] = cx<T>{Store<T>::in(va[c], esc), Store<T>::in(vb[c], escb)};
+                    }
+                }
+            } else if (act) {
                 // chunks of 4 units: all loads of a chunk are issued before any is used
                 constexpr int CH = 4;
                 for (int u0 = ti; u0 < io.cnt_in; u0 += CH * tpl) {
@@ -382,7 +436,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     __syncthreads();
 
     // ---- pre-processing: Hermitian half spectrum -> packed complex input ----
-    if (io.pre == PRE_HERM_EVEN && g < nl) {
+    if (LAY == LAY_GEN && io.pre == PRE_HERM_EVEN && g < nl) {
         // X[0..M] (X[M] Nyquist) -> Z[k] = (X[k] + conj(X[M-k])) + i e^{+2 pi i k/2M} (X[k] - conj(X[M-k])).
         // Each thread owns the slot pair (k, M-k): no barrier between its reads and writes.
         const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
@@ -405,7 +459,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             }
         }
     }
-    if (io.pre == PRE_HERM_EVEN) __syncthreads();
+    if (LAY == LAY_GEN && io.pre == PRE_HERM_EVEN) __syncthreads();
 
     // ---- core ---------------------------------------------------------------
     // Stockham: one pass in the transform's direction.  Bluestein (fftblue_fft,
@@ -446,7 +500,9 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     }
 
     // ---- post-processing: real split ------------------------------------------
-    if (io.post == POST_SPLIT && g < nl) {
+    const bool post_split = LAY == LAY_R2HC || (LAY == LAY_GEN && io.post == POST_SPLIT);
+    const bool post_pair = LAY == LAY_PR2HC || (LAY == LAY_GEN && io.post == POST_PAIR);
+    if (post_split && g < nl) {
         // Z = FFT_M(x_even + i x_odd) -> X[k] = E_k + w^k O_k, k = 0..M,
         // E_k = (Z[k] + conj(Z[M-k]))/2, O_k = -i (Z[k] - conj(Z[M-k]))/2, w = e^{-2 pi i/2M};
         // thread-owned slot pairs (k, M-k), slot M receives X[M]
@@ -466,8 +522,8 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             }
         }
     }
-    if (io.post == POST_SPLIT) __syncthreads();
-    if (io.post == POST_PAIR && g < nl) {
+    if (post_split) __syncthreads();
+    if (post_pair && g < nl) {
         // Z = FFT(a + i b) -> A[k] = (Z[k] + conj(Z[M-k]))/2 at slot k,
         // B[k] = -i (Z[k] - conj(Z[M-k]))/2 at slot M-k; slot 0 keeps (A[0], B[0])
         for (int k = 1 + t; 2 * k < M + 1; k += tpl) {
@@ -478,7 +534,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             myline[sp(k2, pad)] = crenorm(cx<T>{D.i, -D.r});
         }
     }
-    if (io.post == POST_PAIR) __syncthreads();
+    if (post_pair) __syncthreads();
 
     // ---- epilogue: shared memory -> HBM ---------------------------------------
     {
@@ -487,7 +543,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         else { g2 = g; t2 = t; }
         if (g2 < nl && t2 < tpl) {
             OutScale<T> sc;
-            sc.init(io.fct);
+            sc.init(io);
             const int esc = scaled ? s_esc[2 * g2] : 0;
             const int escb = scaled ? s_esc[2 * g2 + 1] : 0;
             const long long l = line0 + g2;
@@ -502,6 +558,55 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const cx<T> *mt = reinterpret_cast<const cx<T> *>(io.mul);
             const cx<T> z0 = paired ? line[0] : cx<T>{};
             constexpr T zero = RealOps<T>::k(0.0);
+            if constexpr (LAY == LAY_C2C) {
+                const int cnt = io.cnt_out;
+                const long long os = io.os;
+                for (int u = t2; u < cnt; u += tpl) {
+                    cx<T> z = line[sp(u, pad)];
+                    if (cc) z.i = -z.i;
+                    S2 o;
+                    o.x = sc.apply(z.r, esc);
+                    o.y = sc.apply(z.i, esc);
+                    *reinterpret_cast<S2 *>(base + (long long)u * os) = o;
+                }
+                return;
+            }
+            if constexpr (LAY == LAY_R2HC) {
+                const int cnt = io.cnt_out;
+                const long long os = io.os, nreal = io.nreal;
+                for (int u = t2; u < cnt; u += tpl) {
+                    const cx<T> z = line[sp(u, pad)];
+                    if (u == 0) {
+                        *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
+                    } else {
+                        char *p = base + (2 * (long long)u - 1) * os;
+                        *reinterpret_cast<S *>(p) = sc.apply(z.r, esc);
+                        if (2 * (long long)u < nreal) *reinterpret_cast<S *>(p + os) = sc.apply(z.i, esc);
+                    }
+                }
+                return;
+            }
+            if constexpr (LAY == LAY_PR2HC) {
+                const int cnt = io.cnt_out;
+                const long long os = io.os, nreal = io.nreal, po = io.pair_out;
+                for (int u = t2; u < cnt; u += tpl) {
+                    const cx<T> za = u == 0 ? cx<T>{z0.r, zero} : line[sp(u, pad)];
+                    const cx<T> zb = u == 0 ? cx<T>{z0.i, zero} : line[sp(M - u, pad)];
+                    if (u == 0) {
+                        *reinterpret_cast<S *>(base) = sc.apply(za.r, esc);
+                        if (has_b) *reinterpret_cast<S *>(base + po) = sc.apply(zb.r, escb);
+                    } else {
+                        char *p = base + (2 * (long long)u - 1) * os;
+                        *reinterpret_cast<S *>(p) = sc.apply(za.r, esc);
+                        if (has_b) *reinterpret_cast<S *>(p + po) = sc.apply(zb.r, escb);
+                        if (2 * (long long)u < nreal) {
+                            *reinterpret_cast<S *>(p + os) = sc.apply(za.i, esc);
+                            if (has_b) *reinterpret_cast<S *>(p + os + po) = sc.apply(zb.i, escb);
+                        }
+                    }
+                }
+                return;
+            }
             for (int u = t2; u < io.cnt_out; u += tpl) {
                 if (paired) {
                     if (io.out_kind == OUT_R) {
@@ -540,10 +645,10 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     }
 }
 
-template <class T, int E, int RS>
+template <class T, int E, int RS, int LAY>
 __global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
 {
-    fft_block<T, E, RS>(P, io, blockIdx.x, io.in, io.out);
+    fft_block<T, E, RS, LAY>(P, io, blockIdx.x, io.in, io.out);
 }
 
 // Persistent kernel over a device work list: item w is block (w - prefix[g])
@@ -573,7 +678,7 @@ __global__ void __launch_bounds__(512, 1) k_fft_worklist(const WorkGroup *__rest
         const WorkGroup &G = groups[lo];
         const char *ib = G.in_base == 0 ? in : G.in_base == 1 ? (const char *)out : (const char *)scr;
         char *ob = G.out_base == 1 ? out : G.out_base == 2 ? scr : (char *)in;
-        fft_block<T, E, RS_ALL>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]), ib + (size_t)G.io.in,
+        fft_block<T, E, RS_ALL, LAY_GEN>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]), ib + (size_t)G.io.in,
                         ob + (size_t)G.io.out);
         __syncthreads();
     }
@@ -710,7 +815,7 @@ __global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_consta
     const long long cnt = io.cnt_out;
     const long long total = io.nlines * cnt;
     OutScale<T> sc;
-    sc.init(io.fct);
+    sc.init(io);
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
         long long l = idx / cnt, u = idx - l * cnt;
@@ -858,7 +963,7 @@ __global__ void k_scatter_pair(const __grid_constant__ IODesc io, const __grid_c
     const long long cnt = io.cnt_out;
     const long long total = io.nlines * cnt;
     OutScale<T> sc;
-    sc.init(io.fct);
+    sc.init(io);
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
         const long long l = idx / cnt;

@@ -19,6 +19,14 @@ struct StageDesc {
     FastDiv fns;    // division by ns
 };
 
+// layout classes of the kernel variants: the common layouts compile without
+// per-element runtime checks
+constexpr int LAY_GEN = 0;    // any layout (runtime kinds, pre / post steps, pairs, twiddles)
+constexpr int LAY_C2C = 1;    // complex in, complex out, nothing else
+constexpr int LAY_R2HC = 2;   // contiguous reals as complex pairs, real split, halfcomplex out
+constexpr int LAY_PR2HC = 3;  // two real lines per complex line, pair split, halfcomplex out
+constexpr int LAY_TW = 4;     // complex in / out with the four-step twiddle or a pointwise table
+
 // radix classes of the kernel variants
 constexpr int RS_P2 = 0;   // 2, 4, 8, 16
 constexpr int RS_P235 = 1; // 2, 4, 8, 16, 3, 5
@@ -68,6 +76,12 @@ struct IODesc {
     long long nreal;        // real length N for halfcomplex units
     int fwd;                // direction of the core transform
     double fct;             // output scale
+    // fct pre-split on the host (the device never compares or converts
+    // doubles: those instructions issue on GB300's narrow FP64 pipe):
+    // FP32 value, and mantissa (hi, lo) in [1, 2) with exponent for double-float
+    float fct_f, fct_h, fct_l;
+    int fct_e;
+    int lay;                // layout class of the kernel variant (set by the host)
     // four-step inter-pass twiddle on output unit u of line l:
     // t = ((l % bn0) * u) mod tw4N, value w_hi[t / tw4S] * w_lo[t % tw4S]
     int tw4;
