@@ -254,6 +254,17 @@ def run_ours(args, rank, world):
     def max_over_ranks(v):
         return aggregate(v, 0.0, world, dev)[0]
 
+    # per-length autotuning (outside every timed region): radix order, elements per
+    # thread, lines per CTA and the four-step split, kept for the plans made below
+    tune_s = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        for code in (L.IG_F64, L.IG_F32):
+            for n in lengths:
+                F.autotune(n, code, 1)
+        torch.cuda.synchronize()
+        tune_s = round(time.perf_counter() - t0, 2)
+
     result = {}
     items64 = make("f64")
     bytes64 = sum(2 * 8 * n * b for n, b, *_ in items64)
@@ -345,7 +356,8 @@ def run_ours(args, rank, world):
                                "~2^24 reals per length, out of place",
                    "lengths": lengths, "reals_per_step": int(bytes64 / 16),
                    "l2": "inputs larger than L2 (128 MiB per length, 35 lengths per step)",
-                   "arith": "double-float butterflies on FP64 data"},
+                   "arith": "double-float butterflies on FP64 data",
+                   "autotune_s": tune_s},
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clocks,
@@ -548,6 +560,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-autotune", action="store_true", help="use the default plan heuristics")
     ap.add_argument("--no-extra", action="store_true", help="skip the uneven-batch and convolution measurements")
     ap.add_argument("--case", default=None, choices=sorted(PROFILE_CASES), help="run one small case once and exit")
     args = ap.parse_args()

@@ -78,6 +78,9 @@ SIGNATURES = {
     "ig_multi_exec_device": (C.c_int, [_vp, _vp, _vp, _vp]),
     "ig_multi_exec_graph": (C.c_int, [_vp, _vp, _vp, _vp]),
     "ig_multi_exec_loop_device": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "ig_autotune": (C.c_int, [C.c_int, _sz, C.c_int, C.POINTER(C.c_double)]),
+    "ig_autotune_save": (C.c_int, [C.c_char_p]),
+    "ig_autotune_load": (C.c_int, [C.c_char_p]),
     "ig_set_f64_arith": (C.c_int, [C.c_int]),
     "ig_release_caches": (None, []),
     "ig_launch_count": (C.c_ulonglong, [C.c_int]),

@@ -100,14 +100,44 @@ static int max_smem()
 // --------------------------------------------------------------------------
 // cores: complex transforms of one length
 // --------------------------------------------------------------------------
-// Radices for a Stockham length L.  Cores of up to 4096 points run 8
-// elements per thread, where a radix-16 stage would leave half the threads
-// idle, so they use radix 8 at most.
-static bool gpu_factor(long long L, std::vector<int> &rad)
+// ---- autotuner configuration --------------------------------------------------
+// Per (arithmetic, Stockham or four-step length): radix order (0 large radices
+// first, 1 reversed), elements per thread (0 default, 8, 16), lines per CTA
+// (0 default) and the four-step split N1 (0 default).
+struct TuneCfg {
+    int order = 0, E = 0, lpc = 0;
+    long long N1 = 0;
+    double ms = 0.0;
+};
+static std::mutex g_tune_mu;
+static std::map<std::pair<int, long long>, TuneCfg> g_tune;
+static thread_local const TuneCfg *g_cfg_override = nullptr;
+static thread_local long long g_cfg_override_len = 0;
+static thread_local int g_cfg_override_arith = -1;
+
+static TuneCfg tune_lookup(int a, long long L)
+{
+    if (g_cfg_override && g_cfg_override_len == L && g_cfg_override_arith == a) return *g_cfg_override;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(std::make_pair(a, L));
+    return it == g_tune.end() ? TuneCfg() : it->second;
+}
+
+static int elems_per_thread(long long L, int cfgE = 0)
+{
+    if (cfgE == 8 && L <= 4096) return 8;
+    if (cfgE == 16) return 16;
+    return L <= 4096 ? 8 : 16;
+}
+
+// Radices for a Stockham length L.  Cores of 8 elements per thread (up to
+// 4096 points by default) use radix 8 at most, since a radix-16 stage would
+// leave half the threads idle.
+static bool gpu_factor(long long L, std::vector<int> &rad, int E = 0, int order = 0)
 {
     rad.clear();
     long long n = L;
-    const bool small = L <= 4096;
+    const bool small = elems_per_thread(L, E) == 8;
     while (!small && n % 16 == 0) { rad.push_back(16); n /= 16; }
     while (small && n % 8 == 0) { rad.push_back(8); n /= 8; }
     if (n % 8 == 0) { rad.push_back(8); n /= 8; }
@@ -115,6 +145,7 @@ static bool gpu_factor(long long L, std::vector<int> &rad)
     if (n % 2 == 0) { rad.push_back(2); n /= 2; }
     for (int p : {11, 7, 5, 3})
         while (n % p == 0) { rad.push_back(p); n /= p; }
+    if (order == 1) std::reverse(rad.begin(), rad.end());
     return n == 1;
 }
 
@@ -191,7 +222,6 @@ static constexpr int kMaxThreads = 512;
 // smem slots a core of Stockham length L needs per line
 static long long smem_slots(long long L, long long M) { return std::max(L, M + 1); }
 
-static int elems_per_thread(long long L) { return L <= 4096 ? 8 : 16; }
 
 static bool fits_smem(Arith a, long long L, long long M)
 {
@@ -322,9 +352,10 @@ static int choose_pad(const CoreDesc &d, int slot)
     return best_pad;
 }
 
-static void finish_layout(Core &c, long long L, long long M)
+static void finish_layout(Core &c, long long L, long long M, const TuneCfg &cfg = TuneCfg())
 {
-    c.d.E = elems_per_thread(L);
+    c.d.E = elems_per_thread(L, cfg.E);
+    c.d.lpc_pref = cfg.lpc;
     bool odd35 = false, odd711 = false;
     for (int s = 0; s < c.d.nst; ++s) {
         odd35 |= c.d.st[s].R == 3 || c.d.st[s].R == 5;
@@ -384,8 +415,9 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
     c->M = M;
     c->real_tw = real_tw;
     c->d.M = (int)std::min<long long>(M, 1 << 30);
+    const TuneCfg cfg = tune_lookup(a, M);
     std::vector<int> rad;
-    bool smooth = gpu_factor(M, rad);
+    bool smooth = gpu_factor(M, rad, cfg.E, cfg.order);
     if (real_tw) {
         void *rtw = c->alloc((M + 1) * slot_bytes(a));
         launch_roots_a(a, rtw, M + 1, 1, 2 * (unsigned long long)M);
@@ -396,16 +428,16 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
         c->kind = 0;
         build_stockham(*c, M, rad);
         c->d.blue = 0;
-        finish_layout(*c, M, M);
+        finish_layout(*c, M, M, cfg);
     } else if (!smooth) {
         long long L = good_size_gpu(2 * M - 1);
         std::vector<int> radL;
-        gpu_factor(L, radL);
+        gpu_factor(L, radL, cfg.E, cfg.order);
         if (fits_smem(a, L, M)) {
             c->kind = 0;
             c->d.blue = 1;
             build_stockham(*c, L, radL);
-            finish_layout(*c, L, M);
+            finish_layout(*c, L, M, cfg);
             void *ch, *chf;
             build_chirp(*c, M, L, ch, chf);
             c->d.chirp = ch;
@@ -431,6 +463,10 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
                 best = d;
         }
         if (!best) raise(IG_ETOOLARGE, "no four-step split of this length fits the GPU kernels");
+        if (cfg.N1 > 1 && M % cfg.N1 == 0 && fits_smem(a, cfg.N1, cfg.N1) && fits_smem(a, M / cfg.N1, M / cfg.N1)) {
+            std::vector<int> r1, r2;
+            if (gpu_factor(cfg.N1, r1) && gpu_factor(M / cfg.N1, r2)) best = cfg.N1;
+        }
         c->kind = 1;
         c->N1 = best;
         c->N2 = M / best;
@@ -474,6 +510,7 @@ static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
     const int smax = max_smem();
     long long lpc = std::max<long long>(1, 256 / tpl);
     if (io.cols_in || io.cols_out) lpc = std::max<long long>(lpc, 8);
+    if (d.lpc_pref > 0) lpc = d.lpc_pref;
     lpc = std::min<long long>(lpc, kMaxLinesPerCta);
     lpc = std::min<long long>(lpc, std::max<long long>(1, kMaxThreads / tpl));
     // keep two CTAs per SM when a line is small enough
@@ -906,7 +943,8 @@ static Arith arith_for(int dtype)
     return g_f64_arith == 1 ? A_F64 : A_DF;
 }
 
-static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, double fct, cudaStream_t st)
+static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, double fct, cudaStream_t st,
+                    std::shared_ptr<Core> forced = nullptr)
 {
     if (ln.nlines <= 0 || N <= 0) return;
     IODesc io = blank_io();
@@ -928,7 +966,7 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
     std::shared_ptr<Core> core;
     switch (op) {
     case OP_C2C:
-        core = get_core(a, N, false);
+        core = forced ? forced : get_core(a, N, false);
         io.in_kind = IN_C;
         io.out_kind = OUT_C;
         io.cnt_in = io.cnt_out = (int)N;
@@ -937,7 +975,7 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
     case OP_R2HC:
     case OP_R2C:
         M = even ? N / 2 : N;
-        core = get_core(a, M, even);
+        core = forced ? forced : get_core(a, M, even);
         if (even && ln.es_in == sr) {
             io.in_kind = IN_C;  // contiguous reals read as complex pairs
             io.is = 2 * sr;
@@ -964,7 +1002,7 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
     case OP_HC2R:
     case OP_C2R:
         M = even ? N / 2 : N;
-        core = get_core(a, M, even);
+        core = forced ? forced : get_core(a, M, even);
         io.in_kind = op == OP_HC2R ? IN_HC : IN_C;
         io.cnt_in = (int)(even ? N / 2 + 1 : (N + 1) / 2);
         if (op == OP_C2R) io.conj_in = forward ? 1 : 0;
@@ -2127,6 +2165,167 @@ int ig_multi_exec_loop_device(ig_multi_plan plan, const void *in, void *out, voi
                                         plan->len[i], plan->len[i], es, es);
             exec_op(plan->a, OP_C2C, plan->len[i], ln, plan->fwd, plan->fct, as_stream(stream));
         }
+    });
+}
+
+// ---- autotuner -------------------------------------------------------------------
+static std::string gpu_name()
+{
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, device_id()) != cudaSuccess) return "unknown";
+    return p.name;
+}
+
+static std::string tune_cache_path(const char *path)
+{
+    if (path && *path) return path;
+    const char *e = getenv("IG_AUTOTUNE_CACHE");
+    return e ? std::string(e) : std::string();
+}
+
+// one entry per line: gpu<TAB>arith<TAB>length<TAB>order<TAB>E<TAB>lpc<TAB>N1<TAB>ms
+int ig_autotune_save(const char *path)
+{
+    return guarded([&] {
+        std::string f = tune_cache_path(path);
+        if (f.empty()) raise(IG_EINVAL, "no autotune cache path (argument or IG_AUTOTUNE_CACHE)");
+        FILE *fp = fopen(f.c_str(), "w");
+        if (!fp) raise(IG_EINVAL, "cannot write " + f);
+        std::string g = gpu_name();
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        for (auto &kv : g_tune)
+            fprintf(fp, "%s\t%d\t%lld\t%d\t%d\t%d\t%lld\t%.6f\n", g.c_str(), kv.first.first, kv.first.second,
+                    kv.second.order, kv.second.E, kv.second.lpc, kv.second.N1, kv.second.ms);
+        fclose(fp);
+    });
+}
+
+int ig_autotune_load(const char *path)
+{
+    return guarded([&] {
+        std::string f = tune_cache_path(path);
+        if (f.empty()) raise(IG_EINVAL, "no autotune cache path (argument or IG_AUTOTUNE_CACHE)");
+        FILE *fp = fopen(f.c_str(), "r");
+        if (!fp) raise(IG_EINVAL, "cannot read " + f);
+        std::string g = gpu_name();
+        char name[256];
+        int a, order, E, lpc;
+        long long len, N1;
+        double ms;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        while (fscanf(fp, " %255[^\t]\t%d\t%lld\t%d\t%d\t%d\t%lld\t%lf", name, &a, &len, &order, &E, &lpc, &N1, &ms) ==
+               8) {
+            if (g != name) continue;
+            TuneCfg c;
+            c.order = order;
+            c.E = E;
+            c.lpc = lpc;
+            c.N1 = N1;
+            c.ms = ms;
+            g_tune[std::make_pair(a, len)] = c;
+        }
+        fclose(fp);
+        std::lock_guard<std::mutex> lk2(g_mu);
+        g_cores.clear();
+    });
+}
+
+// Tune the transform of `length` (kind 0: complex, 1: real halfcomplex
+// forward) for dtype: every candidate (radix order x elements per thread x
+// lines per CTA, or the four-step split) is built, timed with CUDA events on
+// a synthetic batch of ~64 MiB, and the fastest is kept for later plans.
+int ig_autotune(int dtype, size_t length, int kind, double *best_ms)
+{
+    return guarded([&] {
+        if (dtype != IG_F64 && dtype != IG_F32) raise(IG_EINVAL, "bad dtype");
+        if (!length) raise(IG_EZERO_LEN, "zero-length FFT requested");
+        const Arith a = arith_for(dtype);
+        const long long N = (long long)length;
+        const bool even = kind == 1 && N % 2 == 0 && N > 1;
+        const long long M = even ? N / 2 : N;
+        const Op op = kind == 1 ? OP_R2HC : OP_C2C;
+        const long long es = (kind == 1 ? 1 : 2) * (long long)store_real_bytes(a);
+        const long long batch = std::max<long long>(2, (64ll << 20) / (N * es));
+        DevBuf in((size_t)(batch * N * es)), out((size_t)(batch * N * es));
+        ck(cudaMemset(in.p, 0x3f, in.bytes), "tuning data");
+        Lines ln = contiguous_lines(in.p, out.p, batch, N, N, es, es);
+        // candidates
+        auto base = make_core(a, M, even);
+        std::vector<TuneCfg> cands;
+        if (base->kind == 2) {
+            // Bluestein over a four-step core: tune the core's complex length
+            double sub_ms = 0.0;
+            int rc = ig_autotune(dtype, (size_t)base->n2, 0, &sub_ms);
+            if (rc != IG_OK) raise(rc, ig_last_error_string());
+        } else if (base->kind == 1) {
+            for (long long d = 2; d * d <= M; ++d)
+                if (M % d == 0 && fits_smem(a, d, d) && fits_smem(a, M / d, M / d)) {
+                    std::vector<int> r1, r2;
+                    if (gpu_factor(d, r1) && gpu_factor(M / d, r2)) {
+                        for (long long n1 : {d, M / d}) {
+                            TuneCfg c;
+                            c.N1 = n1;
+                            cands.push_back(c);
+                            if (d * d == M) break;
+                        }
+                    }
+                }
+        } else {
+            const long long L = base->d.L;
+            for (int order : {0, 1})
+                for (int E : {8, 16}) {
+                    if (E == 8 && L > 4096) continue;
+                    for (int lpc : {0, 1, 2, 4, 8, 16, 32}) {
+                        long long tpl = (L + E - 1) / E;
+                        if (lpc * tpl > 512) continue;
+                        TuneCfg c;
+                        c.order = order;
+                        c.E = E;
+                        c.lpc = lpc;
+                        cands.push_back(c);
+                    }
+                }
+        }
+        if (cands.empty()) cands.push_back(TuneCfg());
+        cudaEvent_t e0, e1;
+        ck(cudaEventCreate(&e0), "event");
+        ck(cudaEventCreate(&e1), "event");
+        TuneCfg best;
+        best.ms = -1.0;
+        for (const TuneCfg &c : cands) {
+            g_cfg_override = &c;
+            g_cfg_override_len = M;
+            g_cfg_override_arith = a;
+            std::shared_ptr<Core> core;
+            try {
+                core = make_core(a, M, even);
+            } catch (...) {
+                g_cfg_override = nullptr;
+                continue;
+            }
+            g_cfg_override = nullptr;
+            exec_op(a, op, N, ln, 1, 1.0, 0, core);
+            ck(cudaEventRecord(e0, 0), "event");
+            for (int r = 0; r < 3; ++r) exec_op(a, op, N, ln, 1, 1.0, 0, core);
+            ck(cudaEventRecord(e1, 0), "event");
+            ck(cudaEventSynchronize(e1), "event");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            TuneCfg r = c;
+            r.ms = ms / 3.0;
+            if (best.ms < 0 || r.ms < best.ms) best = r;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tune[std::make_pair((int)a, M)] = best;
+        }
+        {
+            std::lock_guard<std::mutex> lk(g_mu);
+            g_cores.clear();  // cores that embed the tuned length are rebuilt on next use
+        }
+        if (best_ms) *best_ms = best.ms;
     });
 }
 

@@ -45,6 +45,7 @@ struct CoreDesc {
     int pad;  // shared-memory padding: slot i is stored at i + (i >> pad)
     int E;    // complex elements per thread (kernel variant 8 or 16): L / E threads per line
     int rs;   // radix class of the kernel variant (0: 2/4/8/16, 1: + 3/5, 2: all)
+    int lpc_pref;  // lines per CTA chosen by the autotuner (0: planner default)
     int nst;
     StageDesc st[kMaxStages];
     const void *tw;     // cx<T> stage twiddles, forward sign

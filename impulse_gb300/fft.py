@@ -357,3 +357,20 @@ def cfft_batch(x: np.ndarray, forward=True, fct=1.0):
     plan = FFTPlanComplex(n, _dtype_code(x))
     L.check(L.load().ig_cfft_exec_batch(plan.pocket, x.ctypes.data, x.size // n, n, int(forward), fct))
     return x
+
+
+def autotune(n, dtype=L.IG_F64, kind=1):
+    """Autotune the length-n transform (kind 0 complex, 1 real halfcomplex); returns ms per call."""
+    ms = C.c_double()
+    L.check(L.load().ig_autotune(dtype, n, kind, C.byref(ms)))
+    return ms.value
+
+
+def autotune_save(path=None):
+    """Write the tuned table (one line per length, keyed by GPU name); None uses IG_AUTOTUNE_CACHE."""
+    L.check(L.load().ig_autotune_save(path.encode() if path else None))
+
+
+def autotune_load(path=None):
+    """Read a table written by autotune_save; entries for other GPU models are skipped."""
+    L.check(L.load().ig_autotune_load(path.encode() if path else None))

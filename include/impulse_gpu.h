@@ -202,6 +202,19 @@ int ig_fftconv_forward(ig_fftconv conv, const void *x, const void *k, void *y, v
 int ig_fftconv_backward(ig_fftconv conv, const void *x, const void *k, const void *gy, void *gx, void *gk,
                         void *stream);
 
+/* ---- autotuner -----------------------------------------------------------------
+ * ig_autotune times every candidate configuration of one transform (kind 0:
+ * complex, 1: real halfcomplex forward) -- radix order, elements per thread
+ * and lines (transforms) per CTA for single-CTA lengths, the split N1 x N2
+ * for four-step lengths -- on a ~64 MiB synthetic batch with CUDA events,
+ * keeps the fastest for plans made afterwards and returns its time per call.
+ * ig_autotune_save / _load write / read the table (one line per entry, keyed
+ * by GPU name); path NULL means the IG_AUTOTUNE_CACHE environment variable.
+ * No counterpart in the reference (PocketFFT's planner is fixed). */
+int ig_autotune(int dtype, size_t length, int kind, double *best_ms);
+int ig_autotune_save(const char *path);
+int ig_autotune_load(const char *path);
+
 /* ---- engine control ------------------------------------------------------ */
 /* Select the arithmetic used for IG_F64 data: 0 = double-float (default;
  * FP32-pair butterflies, ~48-bit significand, for GB300's narrow FP64
