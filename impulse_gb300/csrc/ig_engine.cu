@@ -506,15 +506,16 @@ static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
 {
     if (io.nlines <= 0) return;
     const long long tpl = (d.L + d.E - 1) / d.E;
-    const long long line_bytes = (long long)d.LS * (long long)slot_bytes(a);
+    // 8-element kernels double-buffer their stages: two line buffers
+    const long long line_bytes = (long long)d.LS * (long long)slot_bytes(a) * (d.E == 8 ? 2 : 1);
     const int smax = max_smem();
     long long lpc = std::max<long long>(1, 256 / tpl);
     if (io.cols_in || io.cols_out) lpc = std::max<long long>(lpc, 8);
     if (d.lpc_pref > 0) lpc = d.lpc_pref;
     lpc = std::min<long long>(lpc, kMaxLinesPerCta);
     lpc = std::min<long long>(lpc, std::max<long long>(1, kMaxThreads / tpl));
-    // keep two CTAs per SM when a line is small enough
-    long long budget = line_bytes * 2 <= smax / 2 ? smax / 2 : smax;
+    // keep three (or two) CTAs per SM when a line is small enough
+    long long budget = line_bytes * 3 <= smax ? smax / 3 : line_bytes * 2 <= smax ? smax / 2 : smax;
     lpc = std::min<long long>(lpc, std::max<long long>(1, budget / line_bytes));
     lpc = std::min<long long>(lpc, std::max<long long>(1, io.nlines));
     io.lpc = (int)lpc;

@@ -22,6 +22,7 @@
 // of two (exact), so any finite input magnitude keeps ~48-bit accuracy.
 #pragma once
 #include <cuda_runtime.h>
+#include <type_traits>
 #include "ig_dft.cuh"
 #include "ig_types.h"
 
@@ -131,6 +132,43 @@ __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int 
     __syncthreads();
 }
 
+// The same stage between two buffers (double-buffered Stockham): each
+// butterfly reads src and writes dst, so no barrier separates its reads from
+// its writes and only one butterfly is live in registers at a time; one
+// barrier per stage.  Line g's buffers are src/dst + g * LS2.
+template <class T, int E, int R>
+__device__ __forceinline__ void stage_db(const cx<T> *src, cx<T> *dst, int LS2, const CoreDesc &P, int si, int nl,
+                                         int tpl, int g, int t)
+{
+    constexpr int NB = (E + R - 1) / R;
+    const int nr = P.L / R, ns = P.st[si].ns, pad = P.pad;
+    const FastDiv fns = P.st[si].fns;
+    const cx<T> *tw = reinterpret_cast<const cx<T> *>(P.tw) + P.st[si].tw;
+    if (g >= nl) return;
+    const cx<T> *in = src + (size_t)g * LS2;
+    cx<T> *out = dst + (size_t)g * LS2;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        const int j = t + i * tpl;
+        if (j < nr) {
+            cx<T> v[R];
+#pragma unroll
+            for (int m = 0; m < R; ++m) v[m] = in[sp(j + m * nr, pad)];
+            const int q = (int)fdiv((unsigned)j, fns), k = j - q * ns;
+            if (k) {
+                const cx<T> *twk = tw + k * (R - 1) - 1;
+#pragma unroll
+                for (int m = 1; m < R; ++m) v[m] = cmul(v[m], twk[m]);
+            }
+            dft<R, true>(v);
+            const int base = q * ns * R + k;
+#pragma unroll
+            for (int m = 0; m < R; ++m) out[sp(base + m * ns, pad)] = crenorm(v[m]);
+        }
+        asm volatile("" ::: "memory");
+    }
+}
+
 // Radix classes: a kernel instantiation compiles only the radix cases of its
 // class, which keeps the register allocation of the whole kernel small
 // (the union of all radix cases spills).
@@ -161,6 +199,32 @@ __device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl,
         default: break;
         }
     }
+}
+
+// double-buffered core: buffers A = sm, B = sm + LS (line stride LS2 = 2 LS);
+// returns the offset (0 or LS) of the buffer that holds the result
+template <class T, int E, int RS>
+__device__ __forceinline__ int run_stages_db(cx<T> *sm, int cur, const CoreDesc &P, int nl, int tpl, int g, int t)
+{
+    const int LS = P.LS, LS2 = 2 * P.LS;
+    for (int s = 0; s < P.nst; ++s) {
+        const cx<T> *src = sm + cur;
+        cx<T> *dst = sm + (LS - cur);
+        switch (P.st[s].R) {
+        case 2: stage_db<T, E, 2>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 4: stage_db<T, E, 4>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 8: stage_db<T, E, 8>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 16: if constexpr (rs_has<E, RS>(16)) stage_db<T, E, 16>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 3: if constexpr (rs_has<E, RS>(3)) stage_db<T, E, 3>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 5: if constexpr (rs_has<E, RS>(5)) stage_db<T, E, 5>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 7: if constexpr (rs_has<E, RS>(7)) stage_db<T, E, 7>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 11: if constexpr (rs_has<E, RS>(11)) stage_db<T, E, 11>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        default: break;
+        }
+        cur = LS - cur;
+        __syncthreads();
+    }
+    return cur;
 }
 
 // scale helper: multiply by fct and store with the per-line exponent
@@ -262,6 +326,9 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     __shared__ int s_emax[2 * kMaxLinesPerCta];
     __shared__ int s_rescale;
 
+    // 8 elements per thread: double-buffered stages (2 LS slots per line)
+    constexpr bool DB = E == 8;
+    const int LSt = DB ? 2 * P.LS : P.LS;
     const int lpc = io.lpc, tpl = io.tpl, pad = P.pad;
     const long long line0 = blk * lpc;
     const int nl = (int)min((long long)lpc, io.nlines - line0);
@@ -270,7 +337,9 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     const bool cc = !io.fwd && !P.blue;
     // core mapping: line g, lane t of the line
     const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
-    cx<T> *myline = sm + (size_t)(g < nl ? g : 0) * P.LS;
+    cx<T> *const line_a = sm + (size_t)(g < nl ? g : 0) * LSt;
+    int cur = 0;  // offset of the buffer holding the line (double-buffered stages)
+    cx<T> *myline = line_a;
 
     // range scaling: double-float lines always, FP32 lines when two real lines share one complex line
     const bool paired = LAY == LAY_PR2HC || (LAY == LAY_GEN && io.pair != 0);
@@ -294,7 +363,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         const char *base = act ? in_base + line_off(io, line0 + gi, false) : nullptr;
         const bool has_b = act && paired && (2LL * line_i0(io, line0 + gi) + 1 < io.pair_n0);
         const char *base_b = base + io.pair_in;
-        cx<T> *line = sm + (size_t)(act ? gi : 0) * P.LS;
+        cx<T> *line = sm + (size_t)(act ? gi : 0) * LSt;
         for (int attempt = 0; attempt < (scaled ? 2 : 1); ++attempt) {
             const int esc = (scaled && act) ? s_esc[2 * gi] : 0;
             const int escb = (scaled && act) ? s_esc[2 * gi + 1] : 0;
@@ -487,7 +556,12 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 }
             }
             if (P.blue) __syncthreads();
-            run_stages<T, E, RS>(sm, P, nl, tpl, g, t);
+            if constexpr (DB) {
+                cur = run_stages_db<T, E, RS>(sm, cur, P, nl, tpl, g, t);
+                myline = line_a + cur;
+            } else {
+                run_stages<T, E, RS>(sm, P, nl, tpl, g, t);
+            }
         }
         if (P.blue) {
             if (g < nl)
@@ -548,7 +622,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const int escb = scaled ? s_esc[2 * g2 + 1] : 0;
             const long long l = line0 + g2;
             char *base = out_base + line_off(io, l, true);
-            const cx<T> *line = sm + (size_t)g2 * P.LS;
+            const cx<T> *line = sm + (size_t)g2 * LSt + cur;
             const int i0l = (io.tw4 || io.mul || paired) ? line_i0(io, l) : 0;
             const bool has_b = paired && (2LL * i0l + 1 < io.pair_n0);
             const int n2 = io.tw4 ? i0l : 0;
@@ -645,8 +719,18 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     }
 }
 
+// register caps of the shared-memory kernel: the double-buffered 8-element
+// variants hold one butterfly at a time and fit without spills in fewer
+// registers, which lets three 256-thread CTAs share an SM
+template <class T, int E, int RS> constexpr int fft_smem_regs()
+{
+    if constexpr (E == 8 && std::is_same<T, df>::value) return RS == RS_ALL ? 96 : 72;
+    if constexpr (E == 8 && std::is_same<T, float>::value) return 80;
+    return 128;
+}
+
 template <class T, int E, int RS, int LAY>
-__global__ void __launch_bounds__(512, 1) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
+__global__ void __launch_bounds__(512) __maxnreg__((fft_smem_regs<T, E, RS>())) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
 {
     fft_block<T, E, RS, LAY>(P, io, blockIdx.x, io.in, io.out);
 }
