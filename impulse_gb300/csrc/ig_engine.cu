@@ -365,6 +365,9 @@ static void finish_layout(Core &c, long long L, long long M, const TuneCfg &cfg 
     c.d.pad = choose_pad(c.d, (int)slot_bytes(c.a));
     long long last = std::max(L, M + 1) - 1;
     c.d.LS = (int)(last + (last >> c.d.pad) + 1);
+    // double-buffered stages whenever two line buffers fit (always for E = 8)
+    // (margin: the kernels' static shared memory comes out of the same budget)
+    c.d.db = c.d.E == 8 || 2LL * c.d.LS * (long long)slot_bytes(c.a) <= (long long)max_smem() - 4096;
 }
 
 static void build_stockham(Core &c, long long L, const std::vector<int> &rad)
@@ -506,8 +509,8 @@ static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
 {
     if (io.nlines <= 0) return;
     const long long tpl = (d.L + d.E - 1) / d.E;
-    // 8-element kernels double-buffer their stages: two line buffers
-    const long long line_bytes = (long long)d.LS * (long long)slot_bytes(a) * (d.E == 8 ? 2 : 1);
+    // double-buffered stages: two line buffers
+    const long long line_bytes = (long long)d.LS * (long long)slot_bytes(a) * (d.db ? 2 : 1);
     const int smax = max_smem();
     long long lpc = std::max<long long>(1, 256 / tpl);
     if (io.cols_in || io.cols_out) lpc = std::max<long long>(lpc, 8);
@@ -1919,6 +1922,7 @@ static const int kWorklistThreads = 512;
 static void worklist_fit(Arith a, WorkGroup &g, size_t phase_smem)
 {
     g.P.E = 16;
+    g.P.db = 0;  // the work-list kernel runs in-place stages
     const long long tpl = (g.P.L + 15) / 16;
     const long long line_bytes = (long long)g.P.LS * (long long)slot_bytes(a);
     long long lpc = std::min<long long>(kMaxLinesPerCta, kWorklistThreads / tpl);

@@ -12,13 +12,17 @@ template <> struct TagType<TagF64> { using T = double; };
 
 // k_fft_smem variants of one (arithmetic, elements-per-thread) pair live in
 // their own translation unit (ig_inst_<arith>_e<E>.cu) to compile in parallel
-template <class T, int E> cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
-template <class T, int E> cudaError_t set_smem_E(int bytes);
+// (16 elements per thread: in-place and double-buffered variants)
+template <class T, int E, bool DB>
+cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
+template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes);
 
 template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
     using T = typename TagType<Tag>::T;
-    return d.E == 8 ? launch_fft_E<T, 8>(d, io, smem, st) : launch_fft_E<T, 16>(d, io, smem, st);
+    return d.E == 8 ? launch_fft_E<T, 8, true>(d, io, smem, st)
+         : d.db     ? launch_fft_E<T, 16, true>(d, io, smem, st)
+                    : launch_fft_E<T, 16, false>(d, io, smem, st);
 }
 template <class K> static cudaError_t set_smem_attr(K kernel, int bytes)
 {
@@ -32,8 +36,9 @@ template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
     using T = typename TagType<Tag>::T;
     // the dynamic limit excludes each kernel's static shared memory
     cudaError_t e;
-    if ((e = set_smem_E<T, 8>(bytes)) != cudaSuccess) return e;
-    if ((e = set_smem_E<T, 16>(bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_E<T, 8, true>(bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_E<T, 16, false>(bytes)) != cudaSuccess) return e;
+    if ((e = set_smem_E<T, 16, true>(bytes)) != cudaSuccess) return e;
     return set_smem_attr(k_fft_worklist<T, 16>, bytes);
 }
 template <class Tag>

@@ -11,8 +11,8 @@ template <class T, int E> struct Variants {
     static constexpr bool kSpecialised = !std::is_same<T, double>::value;
 };
 
-#define IG_K(RS_, LAY_) k_fft_smem<T, E, RS_, LAY_><<<grid, blk, smem, st>>>(d, io)
-template <class T, int E, int RS>
+#define IG_K(RS_, LAY_) k_fft_smem<T, E, RS_, LAY_, DB><<<grid, blk, smem, st>>>(d, io)
+template <class T, int E, bool DB, int RS>
 static void launch_rs(const CoreDesc &d, const IODesc &io, unsigned grid, unsigned blk, size_t smem, cudaStream_t st)
 {
     switch (io.lay) {
@@ -25,31 +25,32 @@ static void launch_rs(const CoreDesc &d, const IODesc &io, unsigned grid, unsign
 }
 #undef IG_K
 
-template <class T, int E> cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
+template <class T, int E, bool DB>
+cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
     const unsigned grid = (unsigned)((io.nlines + io.lpc - 1) / io.lpc), blk = (unsigned)(io.lpc * io.tpl);
     if constexpr (!Variants<T, E>::kSpecialised) {
-        k_fft_smem<T, E, RS_ALL, LAY_GEN><<<grid, blk, smem, st>>>(d, io);
+        k_fft_smem<T, E, RS_ALL, LAY_GEN, DB><<<grid, blk, smem, st>>>(d, io);
     } else {
-        if (io.lay == LAY_GEN) k_fft_smem<T, E, RS_ALL, LAY_GEN><<<grid, blk, smem, st>>>(d, io);
-        else if (d.rs == RS_P2) launch_rs<T, E, RS_P2>(d, io, grid, blk, smem, st);
-        else if (E == 8 && d.rs == RS_P235) launch_rs<T, E, (E == 8 ? RS_P235 : RS_ALL)>(d, io, grid, blk, smem, st);
-        else launch_rs<T, E, RS_ALL>(d, io, grid, blk, smem, st);
+        if (io.lay == LAY_GEN) k_fft_smem<T, E, RS_ALL, LAY_GEN, DB><<<grid, blk, smem, st>>>(d, io);
+        else if (d.rs == RS_P2) launch_rs<T, E, DB, RS_P2>(d, io, grid, blk, smem, st);
+        else if (E == 8 && d.rs == RS_P235) launch_rs<T, E, DB, (E == 8 ? RS_P235 : RS_ALL)>(d, io, grid, blk, smem, st);
+        else launch_rs<T, E, DB, RS_ALL>(d, io, grid, blk, smem, st);
     }
     return cudaGetLastError();
 }
 
-template <class T, int E> cudaError_t set_smem_E(int bytes)
+template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes)
 {
-    cudaError_t e = set_smem_attr(k_fft_smem<T, E, RS_ALL, LAY_GEN>, bytes);
+    cudaError_t e = set_smem_attr(k_fft_smem<T, E, RS_ALL, LAY_GEN, DB>, bytes);
     if constexpr (Variants<T, E>::kSpecialised) {
         const int lays[4] = {LAY_C2C, LAY_R2HC, LAY_PR2HC, LAY_TW};
         (void)lays;
 #define IG_S(RS_)                                                                                         \
-    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_C2C>, bytes);                     \
-    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_R2HC>, bytes);                    \
-    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_PR2HC>, bytes);                   \
-    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_TW>, bytes);
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_C2C, DB>, bytes);                     \
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_R2HC, DB>, bytes);                    \
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_PR2HC, DB>, bytes);                   \
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_TW, DB>, bytes);
         IG_S(RS_P2)
         IG_S(RS_ALL)
         if constexpr (E == 8) { IG_S(RS_P235) }

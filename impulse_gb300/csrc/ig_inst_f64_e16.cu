@@ -2,6 +2,6 @@
 #include "ig_inst_e.cuh"
 
 namespace ig {
-template cudaError_t launch_fft_E<double, 16>(const CoreDesc &, const IODesc &, size_t, cudaStream_t);
-template cudaError_t set_smem_E<double, 16>(int);
+template cudaError_t launch_fft_E<double, 16, false>(const CoreDesc &, const IODesc &, size_t, cudaStream_t);
+template cudaError_t set_smem_E<double, 16, false>(int);
 }  // namespace ig

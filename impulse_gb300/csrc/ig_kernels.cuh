@@ -313,7 +313,7 @@ __device__ __forceinline__ void store_unit(const IODesc &io, char *base, int u, 
 // input / output base pointers given explicitly (the persistent work-list
 // kernel keeps its groups' pointers relative to per-launch bases).  Threads
 // beyond lpc * tpl take part only in the barriers.
-template <class T, int E, int RS, int LAY>
+template <class T, int E, int RS, int LAY, bool DB = (E == 8)>
 __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, long long blk, const char *in_base,
                                           char *out_base)
 {
@@ -326,8 +326,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     __shared__ int s_emax[2 * kMaxLinesPerCta];
     __shared__ int s_rescale;
 
-    // 8 elements per thread: double-buffered stages (2 LS slots per line)
-    constexpr bool DB = E == 8;
+    // DB: double-buffered stages (2 LS slots per line)
     const int LSt = DB ? 2 * P.LS : P.LS;
     const int lpc = io.lpc, tpl = io.tpl, pad = P.pad;
     const long long line0 = blk * lpc;
@@ -722,17 +721,18 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
 // register caps of the shared-memory kernel: the double-buffered 8-element
 // variants hold one butterfly at a time and fit without spills in fewer
 // registers, which lets three 256-thread CTAs share an SM
-template <class T, int E, int RS> constexpr int fft_smem_regs()
+template <class T, int E, int RS, bool DB> constexpr int fft_smem_regs()
 {
-    if constexpr (E == 8 && std::is_same<T, df>::value) return RS == RS_ALL ? 96 : 72;
-    if constexpr (E == 8 && std::is_same<T, float>::value) return 80;
+    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS == RS_ALL ? 96 : 72;
+    if constexpr (DB && E == 8 && std::is_same<T, float>::value) return 80;
     return 128;
 }
 
-template <class T, int E, int RS, int LAY>
-__global__ void __launch_bounds__(512) __maxnreg__((fft_smem_regs<T, E, RS>())) k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
+template <class T, int E, int RS, int LAY, bool DB>
+__global__ void __launch_bounds__(512) __maxnreg__((fft_smem_regs<T, E, RS, DB>()))
+    k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
 {
-    fft_block<T, E, RS, LAY>(P, io, blockIdx.x, io.in, io.out);
+    fft_block<T, E, RS, LAY, DB>(P, io, blockIdx.x, io.in, io.out);
 }
 
 // Persistent kernel over a device work list: item w is block (w - prefix[g])
