@@ -145,48 +145,37 @@ IGD df df_scale2(df a, float p2) { return df{IG_FMUL(a.h, p2), IG_FMUL(a.l, p2)}
 
 // double -> double-float with integer and FP32 instructions only.  `escale`
 // multiplies by 2^escale exactly (per-line range scaling).  High part: the
-// sign, the exponent and the top 23 fraction bits rounded; low part: the remaining
-// 29 fraction bits as a signed residual, converted to float and scaled.
-// Relative error <= 2^-48.
+// sign, the rebiased exponent and the top 23 fraction bits (truncated); low
+// part: the remaining 29 fraction bits rounded to 23, placed under a power of
+// two with one exact FP32 subtraction.  Relative error <= 2^-47.  Zeros, double
+// subnormals and values below the float range of the scaled high part
+// flush to zero; infinities and NaNs map to float infinities and NaNs.
 IGD df df_from_double(double x, int escale = 0)
 {
-    uint64_t b = d2u(x);
-    uint32_t hw = (uint32_t)(b >> 32);
-    uint32_t sign = hw & 0x80000000u;
-    int e = (int)((hw >> 20) & 0x7ff);
+    const uint64_t b = d2u(x);
+    const uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
+    const uint32_t sign = hw & 0x80000000u;
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    const int ef = e + escale - 896;  // float biased exponent of the high part
+    if ((unsigned)(ef - 24) < 231u && e != 0x7ff) {
+        const uint32_t f23 = ((hw << 3) | (lw >> 29)) & 0x7fffffu;
+        const uint32_t eb = (uint32_t)ef << 23;
+        const float h = u2f(sign | eb | f23);
+        // (1 + m / 2^23) 2^(ef-23-127) - 2^(ef-23-127) = m 2^(ef-173), m = fraction bits
+        // 28..0 / 2^6 rounded (m = 2^23 carries into the exponent, which is exact too)
+        const uint32_t lb = eb - (23u << 23);
+        const float l = IG_FSUB(u2f(lb + (((lw & 0x1fffffffu) + 32u) >> 6)), u2f(lb));
+        return df{h, u2f(f2u(l) | sign)};
+    }
     if (e == 0x7ff) {  // inf / nan
-        uint32_t frac = (uint32_t)(b >> 29) & 0x7fffffu;
-        return df{u2f(sign | 0x7f800000u | (frac ? 0x400000u : 0u)), 0.0f};
+        const uint32_t frac = ((hw & 0xfffffu) | lw) ? 0x400000u : 0u;
+        return df{u2f(sign | 0x7f800000u | frac), 0.0f};
     }
-    if (e == 0) return df{u2f(sign), 0.0f};  // zero or double subnormal: flushed
-    e += escale;
-    int ef = e - 1023 + 127;  // float biased exponent of the high part
     if (ef >= 255) return df{u2f(sign | 0x7f800000u), 0.0f};
-    if (ef <= 0) return df{u2f(sign), 0.0f};
-    // high part rounded to nearest: incrementing the float's bit pattern
-    // carries into its exponent when the fraction overflows
-    uint32_t top = (uint32_t)(b >> 29) & 0x7fffffu;
-    uint32_t rbit = (uint32_t)(b >> 28) & 1u;
-    uint32_t hb = (((uint32_t)ef << 23) | top) + rbit;
-    if (hb >= 0x7f800000u) return df{u2f(sign | 0x7f800000u), 0.0f};
-    float h = u2f(sign | hb);
-    // low part = (low29 - rbit*2^29) * 2^(e - 1023 - 52), |.| <= 2^28 units
-    int32_t r = (int32_t)((uint32_t)b & 0x1fffffffu) - (int32_t)(rbit << 29);
-    int el = e - 1023 - 52 + 127;  // biased exponent of the scale factor
-    float l = 0.0f;
-    if (el >= 1 && r) {
-        // int -> float without a conversion instruction (those issue on
-        // GB300's narrow FP64 pipe): two exact magic-number conversions of
-        // 15-bit pieces, joined by one correctly rounded FMA
-        int32_t rh = r >> 15;                 // |rh| <= 2^13
-        int32_t rl = r & 0x7fff;              // 0 .. 32767
-        float fh = IG_FSUB(u2f(0x4B400000u + (uint32_t)rh), 12582912.0f);
-        float fl = IG_FSUB(u2f(0x4B000000u + (uint32_t)rl), 8388608.0f);
-        float lf = IG_FMA(fh, 32768.0f, fl);
-        l = IG_FMUL(lf, u2f((uint32_t)el << 23));
-        if (sign) l = -l;
-    }
-    return df{h, l};
+    if (ef <= 0 || e == 0) return df{u2f(sign), 0.0f};
+    // 0 < ef < 24: high part only (the low part would be a float subnormal)
+    const uint32_t f23 = ((hw << 3) | (lw >> 29)) & 0x7fffffu;
+    return df{u2f(sign | ((uint32_t)ef << 23) | f23), 0.0f};
 }
 
 // float -> exact double via bit manipulation (normal floats; others special-cased)
@@ -201,10 +190,10 @@ IGD double f2d_bits(float f)
     return u2d(sign | ((uint64_t)(ef - 127 + 1023) << 52) | ((uint64_t)fr << 29));
 }
 
-// double-float -> double with integer instructions only: the two
-// significands are aligned into one 64-bit integer, normalised and rounded
-// (round-half-up on the discarded bits), and the double is assembled.
-IGD double df_to_double(df v, int escale = 0)
+// double-float -> double, general case: the two significands are aligned
+// into one 64-bit integer, normalised and rounded (round-half-up on the
+// discarded bits), and the double is assembled with integer instructions.
+IGD double df_to_double_slow(df v, int escale)
 {
     uint32_t uh = f2u(v.h), ul = f2u(v.l);
     int eh = (int)((uh >> 23) & 0xff);
@@ -247,6 +236,29 @@ IGD double df_to_double(df v, int escale = 0)
     if (ed >= 0x7ff) return u2d(sgn | 0x7ff0000000000000ull);
     if (ed <= 0) return u2d(sgn);
     return u2d(sgn | ((uint64_t)ed << 52) | (M & 0xfffffffffffffull));
+}
+
+// double-float -> double: both parts are rebuilt exactly as doubles from
+// their bit fields (scaled by 2^-escale through the exponent) and added
+// with one correctly rounded FP64 addition.  Zero, special and
+// out-of-range parts take the general path.
+IGD double df_to_double(df v, int escale = 0)
+{
+    const uint32_t uh = f2u(v.h), ul = f2u(v.l);
+    const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
+    const int ed = eh + 896 - escale;  // double biased exponent of the high part
+    const int edl = el + 896 - escale;
+    if ((unsigned)(eh - 1) < 254u && (unsigned)(ed - 1) < 2046u &&
+        (el == 0 || ((unsigned)(el - 1) < 254u && (unsigned)(edl - 1) < 2046u))) {
+        const uint32_t rebias = (uint32_t)(896 - escale) << 20;
+        const double dh = u2d(((uint64_t)((uh & 0x80000000u) | (((uh & 0x7fffffffu) >> 3) + rebias)) << 32) |
+                              (uint64_t)(uh << 29));
+        // a zero (or float subnormal) low part adds nothing
+        const uint32_t lhi = el ? (ul & 0x80000000u) | (((ul & 0x7fffffffu) >> 3) + rebias) : 0u;
+        const double dl = u2d(((uint64_t)lhi << 32) | (uint64_t)(el ? ul << 29 : 0u));
+        return dh + dl;
+    }
+    return df_to_double_slow(v, escale);
 }
 
 // sign flip of a double through its bit pattern (no FP64 instruction)
