@@ -384,10 +384,12 @@ static void build_stockham(Core &c, long long L, const std::vector<int> &rad)
         off += ns * (rad[s] - 1);
         ns *= rad[s];
     }
-    void *tw = c.alloc(std::max<long long>(off, 1) * slot_bytes(c.a));
+    // double-float stage twiddles are stored packed (48 bytes an entry)
+    const size_t twb = c.a == A_DF ? 48 : slot_bytes(c.a);
+    void *tw = c.alloc(std::max<long long>(off, 1) * twb);
     c.d.tw = tw;
     for (size_t s = 0; s < rad.size(); ++s) {
-        void *p = (char *)tw + (size_t)c.d.st[s].tw * slot_bytes(c.a);
+        void *p = (char *)tw + (size_t)c.d.st[s].tw * twb;
         launch_stage_tw(c.a, p, rad[s], c.d.st[s].ns);
     }
 }

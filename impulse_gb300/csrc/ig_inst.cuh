@@ -56,7 +56,7 @@ template <class Tag> cudaError_t Launch<Tag>::stage_tw(void *tw, int R, int ns)
     using T = typename TagType<Tag>::T;
     int n = ns * (R - 1);
     if (!n) return cudaSuccess;
-    k_gen_stage_tw<T><<<(n + 255) / 256, 256>>>((cx<T> *)tw, R, ns);
+    k_gen_stage_tw<T><<<(n + 255) / 256, 256>>>((typename Bfly<T>::W *)tw, R, ns);
     return cudaGetLastError();
 }
 template <class Tag>

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 #include <type_traits>
 #include "ig_dft.cuh"
+#include "ig_pdf.cuh"
 #include "ig_types.h"
 
 namespace ig {
@@ -82,8 +83,35 @@ template <class T, bool RAW> __device__ __forceinline__ cx<T> sload(const cx<T> 
     }
 }
 
+// shared-memory slot access: double-float complexes are stored as
+// (re.h, im.h, re.l, im.l) for the packed butterflies
+template <class T> __device__ __forceinline__ cx<T> sget(const cx<T> *p) { return *p; }
+template <class T> __device__ __forceinline__ void sput(cx<T> *p, cx<T> v) { *p = v; }
+template <> __device__ __forceinline__ cx<df> sget<df>(const cx<df> *p) { return from_p(pld(p)); }
+template <> __device__ __forceinline__ void sput<df>(cx<df> *p, cx<df> v) { pst(p, to_p(v)); }
+
 // padded shared-memory slot of element i
 __device__ __forceinline__ int sp(int i, int pad) { return i + (i >> pad); }
+
+// Butterfly arithmetic of the stages: plain complexes for float / double,
+// packed pairs (ig_pdf.cuh) for double-float, whose stage twiddle table
+// holds the packed form (48 bytes an entry).
+template <class T> struct Bfly {
+    using V = cx<T>;
+    using W = cx<T>;
+    static __device__ __forceinline__ V ld(const cx<T> *p) { return *p; }
+    static __device__ __forceinline__ void st(cx<T> *p, V v) { *p = crenorm(v); }
+    static __device__ __forceinline__ V tw(V a, const W *w) { return cmul(a, *w); }
+    template <int R> static __device__ __forceinline__ void dft(V *v) { ig::dft<R, true>(v); }
+};
+template <> struct Bfly<df> {
+    using V = pcx;
+    using W = ptw;
+    static __device__ __forceinline__ V ld(const cx<df> *p) { return pld(p); }
+    static __device__ __forceinline__ void st(cx<df> *p, V v) { pst(p, prenorm(v)); }
+    static __device__ __forceinline__ V tw(V a, const W *w) { return pmulw(a, w); }
+    template <int R> static __device__ __forceinline__ void dft(V *v) { pdft<R>(v); }
+};
 
 // One Stockham stage of radix R in shared memory, in place through
 // registers.  Butterfly j (j < L/R) of a line reads x[j + m L/R], twiddles
@@ -93,12 +121,14 @@ __device__ __forceinline__ int sp(int i, int pad) { return i + (i >> pad); }
 template <class T, int E, int R>
 __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int nl, int tpl, int g, int t)
 {
+    using B = Bfly<T>;
+    using V = typename B::V;
     constexpr int NB = (E + R - 1) / R;
     const int nr = P.L / R, ns = P.st[si].ns, pad = P.pad;
     const FastDiv fns = P.st[si].fns;
-    const cx<T> *tw = reinterpret_cast<const cx<T> *>(P.tw) + P.st[si].tw;
+    const typename B::W *tw = reinterpret_cast<const typename B::W *>(P.tw) + P.st[si].tw;
     cx<T> *line = sm + (size_t)g * P.LS;
-    cx<T> v[NB][R];
+    V v[NB][R];
     int jj[NB];
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
@@ -106,7 +136,7 @@ __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int 
         jj[i] = (g < nl && j < nr) ? j : -1;
         if (jj[i] >= 0) {
 #pragma unroll
-            for (int m = 0; m < R; ++m) v[i][m] = line[sp(j + m * nr, pad)];
+            for (int m = 0; m < R; ++m) v[i][m] = B::ld(line + sp(j + m * nr, pad));
         }
     }
     __syncthreads();
@@ -116,14 +146,14 @@ __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int 
             const int j = jj[i];
             const int q = (int)fdiv((unsigned)j, fns), k = j - q * ns;
             if (k) {
-                const cx<T> *twk = tw + k * (R - 1) - 1;
+                const typename B::W *twk = tw + k * (R - 1) - 1;
 #pragma unroll
-                for (int m = 1; m < R; ++m) v[i][m] = cmul(v[i][m], twk[m]);
+                for (int m = 1; m < R; ++m) v[i][m] = B::tw(v[i][m], twk + m);
             }
-            dft<R, true>(v[i]);
+            B::template dft<R>(v[i]);
             const int base = q * ns * R + k;
 #pragma unroll
-            for (int m = 0; m < R; ++m) line[sp(base + m * ns, pad)] = crenorm(v[i][m]);
+            for (int m = 0; m < R; ++m) B::st(line + sp(base + m * ns, pad), v[i][m]);
         }
         // keep the next butterfly's twiddle loads below this one's stores, so
         // that only one butterfly's twiddles are live at a time
@@ -140,10 +170,12 @@ template <class T, int E, int R>
 __device__ __forceinline__ void stage_db(const cx<T> *src, cx<T> *dst, int LS2, const CoreDesc &P, int si, int nl,
                                          int tpl, int g, int t)
 {
+    using B = Bfly<T>;
+    using V = typename B::V;
     constexpr int NB = (E + R - 1) / R;
     const int nr = P.L / R, ns = P.st[si].ns, pad = P.pad;
     const FastDiv fns = P.st[si].fns;
-    const cx<T> *tw = reinterpret_cast<const cx<T> *>(P.tw) + P.st[si].tw;
+    const typename B::W *tw = reinterpret_cast<const typename B::W *>(P.tw) + P.st[si].tw;
     if (g >= nl) return;
     const cx<T> *in = src + (size_t)g * LS2;
     cx<T> *out = dst + (size_t)g * LS2;
@@ -151,19 +183,19 @@ __device__ __forceinline__ void stage_db(const cx<T> *src, cx<T> *dst, int LS2, 
     for (int i = 0; i < NB; ++i) {
         const int j = t + i * tpl;
         if (j < nr) {
-            cx<T> v[R];
+            V v[R];
 #pragma unroll
-            for (int m = 0; m < R; ++m) v[m] = in[sp(j + m * nr, pad)];
+            for (int m = 0; m < R; ++m) v[m] = B::ld(in + sp(j + m * nr, pad));
             const int q = (int)fdiv((unsigned)j, fns), k = j - q * ns;
             if (k) {
-                const cx<T> *twk = tw + k * (R - 1) - 1;
+                const typename B::W *twk = tw + k * (R - 1) - 1;
 #pragma unroll
-                for (int m = 1; m < R; ++m) v[m] = cmul(v[m], twk[m]);
+                for (int m = 1; m < R; ++m) v[m] = B::tw(v[m], twk + m);
             }
-            dft<R, true>(v);
+            B::template dft<R>(v);
             const int base = q * ns * R + k;
 #pragma unroll
-            for (int m = 0; m < R; ++m) out[sp(base + m * ns, pad)] = crenorm(v[m]);
+            for (int m = 0; m < R; ++m) B::st(out + sp(base + m * ns, pad), v[m]);
         }
         asm volatile("" ::: "memory");
     }
@@ -390,7 +422,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                             emax = max(emax, max(e1 == 0x7ff ? 0 : e1, e2 == 0x7ff ? 0 : e2));
                         }
                         cx<T> z{Store<T>::in(v[c].x, esc), Store<T>::in(v[c].y, esc)};
-                        line[sp(u, pad)] = cc ? conjx(z) : z;
+                        sput(line + sp(u, pad), cc ? conjx(z) : z);
                     }
                 }
             } else if (act && LAY == LAY_PR2HC) {
@@ -422,7 +454,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                             emax = max(emax, e1 == 0xff ? 0 : e1);
                             emaxb = max(emaxb, e2 == 0xff ? 0 : e2);
                         }
-                        line[sp(u, pad)] = cx<T>{Store<T>::in(va[c], esc), Store<T>::in(vb[c], escb)};
+                        sput(line + sp(u, pad), cx<T>{Store<T>::in(va[c], esc), Store<T>::in(vb[c], escb)});
                     }
                 }
             } else if (act) {
@@ -461,18 +493,18 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     if (!paired) {
                         cx<T> z{Store<T>::in(re, esc), Store<T>::in(im, esc)};
                         const bool cz = cc && io.pre != PRE_HERM_EVEN;
-                        line[sp(u, pad)] = cz ? conjx(z) : z;
-                        if (io.pre == PRE_HERM_ODD && u > 0) line[sp(M - u, pad)] = cz ? z : conjx(z);
+                        sput(line + sp(u, pad), cz ? conjx(z) : z);
+                        if (io.pre == PRE_HERM_ODD && u > 0) sput(line + sp(M - u, pad), cz ? z : conjx(z));
                     } else {
                         // Z = A + i B: real lines -> (a, b); half spectra -> Z[u] = A + iB,
                         // Z[M-u] = conj(A) + i conj(B)
                         cx<T> A{Store<T>::in(re, esc), Store<T>::in(im, esc)};
                         cx<T> B{Store<T>::in(rb, escb), Store<T>::in(ib, escb)};
                         cx<T> z = cx<T>{A.r - B.i, A.i + B.r};
-                        line[sp(u, pad)] = cc ? conjx(z) : z;
+                        sput(line + sp(u, pad), cc ? conjx(z) : z);
                         if (io.in_kind != IN_R && u > 0) {
                             cx<T> zm = cx<T>{A.r + B.i, B.r - A.i};
-                            line[sp(M - u, pad)] = cc ? conjx(zm) : zm;
+                            sput(line + sp(M - u, pad), cc ? conjx(zm) : zm);
                         }
                     }
                 }
@@ -512,20 +544,20 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
         for (int k = t; k <= M / 2; k += tpl) {
             const int k2 = M - k;
-            cx<T> a = myline[sp(k, pad)], b = myline[sp(k2, pad)];
+            cx<T> a = sget(myline + sp(k, pad)), b = sget(myline + sp(k2, pad));
             {
                 cx<T> xb = conjx(b);
                 cx<T> A = a + xb, Bv = a - xb;
                 cx<T> tB = cmulc(Bv, rtw[k]);
                 cx<T> z{A.r - tB.i, A.i + tB.r};
-                myline[sp(k, pad)] = cc ? conjx(z) : z;  // conjugated for a backward Stockham core
+                sput(myline + sp(k, pad), cc ? conjx(z) : z);  // conjugated for a backward Stockham core
             }
             if (k > 0 && k2 != k) {
                 cx<T> xb = conjx(a);
                 cx<T> A = b + xb, Bv = b - xb;
                 cx<T> tB = cmulc(Bv, rtw[k2]);
                 cx<T> z{A.r - tB.i, A.i + tB.r};
-                myline[sp(k2, pad)] = cc ? conjx(z) : z;
+                sput(myline + sp(k2, pad), cc ? conjx(z) : z);
             }
         }
     }
@@ -545,14 +577,14 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 if (pass == 0) {
                     for (int u = t; u < L; u += tpl) {
                         cx<T> z = cx<T>{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
-                        if (u < M) z = io.fwd ? cmulc(myline[sp(u, pad)], ch[u]) : cmul(myline[sp(u, pad)], ch[u]);
-                        myline[sp(u, pad)] = z;
+                        if (u < M) z = io.fwd ? cmulc(sget(myline + sp(u, pad)), ch[u]) : cmul(sget(myline + sp(u, pad)), ch[u]);
+                        sput(myline + sp(u, pad), z);
                     }
                 } else {
                     // backward FFT_L as conj(FFT_L(conj(.)))
                     for (int u = t; u < L; u += tpl) {
-                        cx<T> z = io.fwd ? cmul(myline[sp(u, pad)], chf[u]) : cmulc(myline[sp(u, pad)], chf[u]);
-                        myline[sp(u, pad)] = conjx(z);
+                        cx<T> z = io.fwd ? cmul(sget(myline + sp(u, pad)), chf[u]) : cmulc(sget(myline + sp(u, pad)), chf[u]);
+                        sput(myline + sp(u, pad), conjx(z));
                     }
                 }
             }
@@ -567,8 +599,8 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         if (P.blue) {
             if (g < nl)
                 for (int u = t; u < M; u += tpl) {
-                    cx<T> z = conjx(myline[sp(u, pad)]);
-                    myline[sp(u, pad)] = io.fwd ? cmulc(z, ch[u]) : cmul(z, ch[u]);
+                    cx<T> z = conjx(sget(myline + sp(u, pad)));
+                    sput(myline + sp(u, pad), io.fwd ? cmulc(z, ch[u]) : cmul(z, ch[u]));
                 }
             __syncthreads();
         }
@@ -584,16 +616,16 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
         for (int k = t; k <= M / 2; k += tpl) {
             const int k2 = M - k;
-            cx<T> a = myline[sp(k, pad)], b = myline[sp(k == 0 ? 0 : k2, pad)];
+            cx<T> a = sget(myline + sp(k, pad)), b = sget(myline + sp(k == 0 ? 0 : k2, pad));
             {
                 cx<T> zb = conjx(b);
                 cx<T> E = chalf(a + zb), D = chalf(a - zb);
-                myline[sp(k, pad)] = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k]));
+                sput(myline + sp(k, pad), crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k])));
             }
             if (k2 != k) {
                 cx<T> zb = conjx(a);
                 cx<T> E = chalf(b + zb), D = chalf(b - zb);
-                myline[sp(k2, pad)] = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k2]));
+                sput(myline + sp(k2, pad), crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k2])));
             }
         }
     }
@@ -603,10 +635,10 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         // B[k] = -i (Z[k] - conj(Z[M-k]))/2 at slot M-k; slot 0 keeps (A[0], B[0])
         for (int k = 1 + t; 2 * k < M + 1; k += tpl) {
             const int k2 = M - k;
-            cx<T> a = myline[sp(k, pad)], b = conjx(myline[sp(k2, pad)]);
+            cx<T> a = sget(myline + sp(k, pad)), b = conjx(sget(myline + sp(k2, pad)));
             cx<T> A = chalf(a + b), D = chalf(a - b);
-            myline[sp(k, pad)] = crenorm(A);
-            myline[sp(k2, pad)] = crenorm(cx<T>{D.i, -D.r});
+            sput(myline + sp(k, pad), crenorm(A));
+            sput(myline + sp(k2, pad), crenorm(cx<T>{D.i, -D.r}));
         }
     }
     if (post_pair) __syncthreads();
@@ -631,13 +663,13 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const cx<T> *whi = reinterpret_cast<const cx<T> *>(io.tw4hi);
             const cx<T> *wlo = reinterpret_cast<const cx<T> *>(io.tw4lo);
             const cx<T> *mt = reinterpret_cast<const cx<T> *>(io.mul);
-            const cx<T> z0 = paired ? line[0] : cx<T>{};
+            const cx<T> z0 = paired ? sget(line + 0) : cx<T>{};
             constexpr T zero = RealOps<T>::k(0.0);
             if constexpr (LAY == LAY_C2C) {
                 const int cnt = io.cnt_out;
                 const long long os = io.os;
                 for (int u = t2; u < cnt; u += tpl) {
-                    cx<T> z = line[sp(u, pad)];
+                    cx<T> z = sget(line + sp(u, pad));
                     if (cc) z.i = -z.i;
                     S2 o;
                     o.x = sc.apply(z.r, esc);
@@ -650,7 +682,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 const int cnt = io.cnt_out;
                 const long long os = io.os, nreal = io.nreal;
                 for (int u = t2; u < cnt; u += tpl) {
-                    const cx<T> z = line[sp(u, pad)];
+                    const cx<T> z = sget(line + sp(u, pad));
                     if (u == 0) {
                         *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
                     } else {
@@ -665,8 +697,8 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 const int cnt = io.cnt_out;
                 const long long os = io.os, nreal = io.nreal, po = io.pair_out;
                 for (int u = t2; u < cnt; u += tpl) {
-                    const cx<T> za = u == 0 ? cx<T>{z0.r, zero} : line[sp(u, pad)];
-                    const cx<T> zb = u == 0 ? cx<T>{z0.i, zero} : line[sp(M - u, pad)];
+                    const cx<T> za = u == 0 ? cx<T>{z0.r, zero} : sget(line + sp(u, pad));
+                    const cx<T> zb = u == 0 ? cx<T>{z0.i, zero} : sget(line + sp(M - u, pad));
                     if (u == 0) {
                         *reinterpret_cast<S *>(base) = sc.apply(za.r, esc);
                         if (has_b) *reinterpret_cast<S *>(base + po) = sc.apply(zb.r, escb);
@@ -685,20 +717,20 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             for (int u = t2; u < io.cnt_out; u += tpl) {
                 if (paired) {
                     if (io.out_kind == OUT_R) {
-                        cx<T> z = line[sp(u, pad)];
+                        cx<T> z = sget(line + sp(u, pad));
                         if (cc) z.i = -z.i;
                         *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, esc);
                         if (has_b) *reinterpret_cast<S *>(base + io.pair_out + (long long)u * io.os) = sc.apply(z.i, escb);
                     } else {
-                        cx<T> za = u == 0 ? cx<T>{z0.r, zero} : line[sp(u, pad)];
-                        cx<T> zb = u == 0 ? cx<T>{z0.i, zero} : line[sp(M - u, pad)];
+                        cx<T> za = u == 0 ? cx<T>{z0.r, zero} : sget(line + sp(u, pad));
+                        cx<T> zb = u == 0 ? cx<T>{z0.i, zero} : sget(line + sp(M - u, pad));
                         if (io.conj_out) { za.i = -za.i; zb.i = -zb.i; }
                         store_unit<T, S, S2>(io, base, u, za, sc, esc);
                         if (has_b) store_unit<T, S, S2>(io, base + io.pair_out, u, zb, sc, escb);
                     }
                     continue;
                 }
-                cx<T> z = line[sp(u, pad)];
+                cx<T> z = sget(line + sp(u, pad));
                 if (cc) z.i = -z.i;
                 if (io.tw4) {
                     // t = n2 u < M: w^t = w_hi[t / S] * w_lo[t mod S]
@@ -725,7 +757,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
 // registers, which lets three 256-thread CTAs share an SM
 template <class T, int E, int RS, bool DB> constexpr int fft_smem_regs()
 {
-    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS == RS_ALL ? 96 : 72;
+    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS == RS_ALL ? 96 : 80;
     if constexpr (DB && E == 8 && std::is_same<T, float>::value) return 80;
     return 128;
 }
@@ -1226,14 +1258,21 @@ template <> __device__ inline cx<double> to_arith<double>(double2 v) { return cx
 template <> __device__ inline cx<df> to_arith<df>(double2 v) { return cx<df>{df_from_double(v.x), df_from_double(v.y)}; }
 
 // stage twiddles: entry k*(R-1) + m-1 = exp(-2 pi i m k / (ns R)), k < ns, 1 <= m < R
-template <class T> __global__ void k_gen_stage_tw(cx<T> *tw, int R, int ns)
+template <class T> __global__ void k_gen_stage_tw(typename Bfly<T>::W *tw, int R, int ns)
 {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ns * (R - 1)) return;
     int k = e / (R - 1), m = e % (R - 1) + 1;
     double2 v = exp2pi_frac((unsigned long long)m * k, (unsigned long long)ns * R);
     v.y = -v.y;
-    tw[e] = to_arith<T>(v);
+    if constexpr (std::is_same<T, df>::value) {
+        // packed: (wr, wr), (-wi, wi) for the high and the low parts, negated high pairs
+        const cx<df> w = to_arith<df>(v);
+        tw[e] = ptw{pk(w.r.h, w.r.h), pk(-w.i.h, w.i.h), pk(w.r.l, w.r.l), pk(-w.i.l, w.i.l), pk(-w.r.h, -w.r.h),
+                    pk(w.i.h, -w.i.h)};
+    } else {
+        tw[e] = to_arith<T>(v);
+    }
 }
 
 // roots: out[j] = exp(-2 pi i (j * mult) / D), j < count
