@@ -362,6 +362,9 @@ static void finish_layout(Core &c, long long L, long long M, const TuneCfg &cfg 
         odd711 |= c.d.st[s].R == 7 || c.d.st[s].R == 11;
     }
     c.d.rs = odd711 ? RS_ALL : odd35 ? (c.d.E == 8 ? RS_P235 : RS_ALL) : RS_P2;
+    // double-float 8-element kernels: the 2/3/5 variant fits the register cap
+    // without spills where the power-of-two one does not
+    if (c.a == A_DF && c.d.E == 8 && c.d.rs == RS_P2) c.d.rs = RS_P235;
     c.d.pad = choose_pad(c.d, (int)slot_bytes(c.a));
     long long last = std::max(L, M + 1) - 1;
     c.d.LS = (int)(last + (last >> c.d.pad) + 1);
@@ -384,8 +387,9 @@ static void build_stockham(Core &c, long long L, const std::vector<int> &rad)
         off += ns * (rad[s] - 1);
         ns *= rad[s];
     }
-    // double-float stage twiddles are stored packed (48 bytes an entry)
-    const size_t twb = c.a == A_DF ? 48 : slot_bytes(c.a);
+    // double-float stage twiddles are stored packed (32 bytes an entry)
+    const size_t twb = c.a == A_DF ? 32 : slot_bytes(c.a);
+    c.d.neg1 = -1.0f;
     void *tw = c.alloc(std::max<long long>(off, 1) * twb);
     c.d.tw = tw;
     for (size_t s = 0; s < rad.size(); ++s) {

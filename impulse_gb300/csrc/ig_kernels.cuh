@@ -95,13 +95,13 @@ __device__ __forceinline__ int sp(int i, int pad) { return i + (i >> pad); }
 
 // Butterfly arithmetic of the stages: plain complexes for float / double,
 // packed pairs (ig_pdf.cuh) for double-float, whose stage twiddle table
-// holds the packed form (48 bytes an entry).
+// holds the packed form (32 bytes an entry).
 template <class T> struct Bfly {
     using V = cx<T>;
     using W = cx<T>;
     static __device__ __forceinline__ V ld(const cx<T> *p) { return *p; }
     static __device__ __forceinline__ void st(cx<T> *p, V v) { *p = crenorm(v); }
-    static __device__ __forceinline__ V tw(V a, const W *w) { return cmul(a, *w); }
+    static __device__ __forceinline__ V tw(V a, const W *w, const CoreDesc &) { return cmul(a, *w); }
     template <int R> static __device__ __forceinline__ void dft(V *v) { ig::dft<R, true>(v); }
 };
 template <> struct Bfly<df> {
@@ -109,7 +109,7 @@ template <> struct Bfly<df> {
     using W = ptw;
     static __device__ __forceinline__ V ld(const cx<df> *p) { return pld(p); }
     static __device__ __forceinline__ void st(cx<df> *p, V v) { pst(p, prenorm(v)); }
-    static __device__ __forceinline__ V tw(V a, const W *w) { return pmulw(a, w); }
+    static __device__ __forceinline__ V tw(V a, const W *w, const CoreDesc &P) { return pmulw(a, w, bcast(P.neg1)); }
     template <int R> static __device__ __forceinline__ void dft(V *v) { pdft<R>(v); }
 };
 
@@ -148,7 +148,7 @@ __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int 
             if (k) {
                 const typename B::W *twk = tw + k * (R - 1) - 1;
 #pragma unroll
-                for (int m = 1; m < R; ++m) v[i][m] = B::tw(v[i][m], twk + m);
+                for (int m = 1; m < R; ++m) v[i][m] = B::tw(v[i][m], twk + m, P);
             }
             B::template dft<R>(v[i]);
             const int base = q * ns * R + k;
@@ -190,7 +190,7 @@ __device__ __forceinline__ void stage_db(const cx<T> *src, cx<T> *dst, int LS2, 
             if (k) {
                 const typename B::W *twk = tw + k * (R - 1) - 1;
 #pragma unroll
-                for (int m = 1; m < R; ++m) v[m] = B::tw(v[m], twk + m);
+                for (int m = 1; m < R; ++m) v[m] = B::tw(v[m], twk + m, P);
             }
             B::template dft<R>(v);
             const int base = q * ns * R + k;
@@ -1266,10 +1266,9 @@ template <class T> __global__ void k_gen_stage_tw(typename Bfly<T>::W *tw, int R
     double2 v = exp2pi_frac((unsigned long long)m * k, (unsigned long long)ns * R);
     v.y = -v.y;
     if constexpr (std::is_same<T, df>::value) {
-        // packed: (wr, wr), (-wi, wi) for the high and the low parts, negated high pairs
+        // packed: (wr, wr), (-wi, wi) for the high and the low parts
         const cx<df> w = to_arith<df>(v);
-        tw[e] = ptw{pk(w.r.h, w.r.h), pk(-w.i.h, w.i.h), pk(w.r.l, w.r.l), pk(-w.i.l, w.i.l), pk(-w.r.h, -w.r.h),
-                    pk(w.i.h, -w.i.h)};
+        tw[e] = ptw{pk(w.r.h, w.r.h), pk(-w.i.h, w.i.h), pk(w.r.l, w.r.l), pk(-w.i.l, w.i.l)};
     } else {
         tw[e] = to_arith<T>(v);
     }

@@ -174,16 +174,21 @@ IGP pcx pcmul(pcx a, cx<df> w)
     return pmulw(a, bcast(w.r.h), pk(-w.i.h, w.i.h), bcast(w.r.l), pk(-w.i.l, w.i.l), bcast(-w.r.h),
                  pk(w.i.h, -w.i.h));
 }
-// stage twiddle in packed form: (W1h, W2h, W1l, W2l, nW1h, nW2h), 48 bytes
+// stage twiddle in packed form: (W1h, W2h, W1l, W2l), 32 bytes.  The
+// negated high pairs are formed with a product by `neg` = (-1, -1), a value
+// the kernels read from their parameters: a negation the compiler can see
+// would let it cancel the FMA error term against the product it was taken
+// from.
 struct ptw {
-    f2p W1h, W2h, W1l, W2l, nW1h, nW2h;
+    f2p W1h, W2h, W1l, W2l;
 };
 #if defined(__CUDACC__)
-IGP pcx pmulw(pcx a, const ptw *w)
+IGP pcx pmulw(pcx a, const ptw *w, f2p neg)
 {
     const ulonglong2 *q = reinterpret_cast<const ulonglong2 *>(w);
-    const ulonglong2 q0 = q[0], q1 = q[1], q2 = q[2];
-    return pmulw(a, f2p{q0.x}, f2p{q0.y}, f2p{q1.x}, f2p{q1.y}, f2p{q2.x}, f2p{q2.y});
+    const ulonglong2 q0 = q[0], q1 = q[1];
+    const f2p W1h{q0.x}, W2h{q0.y};
+    return pmulw(a, W1h, W2h, f2p{q1.x}, f2p{q1.y}, W1h * neg, W2h * neg);
 }
 #endif
 

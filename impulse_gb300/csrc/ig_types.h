@@ -47,6 +47,7 @@ struct CoreDesc {
     int rs;   // radix class of the kernel variant (0: 2/4/8/16, 1: + 3/5, 2: all)
     int lpc_pref;  // lines per CTA chosen by the autotuner (0: planner default)
     int db;   // 1: double-buffered stages (two line buffers; always with E = 8)
+    float neg1;  // -1 (a runtime value for the packed double-float twiddle products)
     int nst;
     StageDesc st[kMaxStages];
     const void *tw;     // cx<T> stage twiddles, forward sign
