@@ -1,10 +1,10 @@
-// ig_dft.cuh -- register-resident small DFTs (radix 2, 3, 4, 5, 7, 8, 11, 16).
+// ig_dft.cuh -- register-resident small DFTs (radix 2, 3, 4, 5, 7, 8, 11, 13, 16).
 //
 // dft<R, FWD>(v) replaces v[0..R) by V[q] = sum_m v[m] exp(-+2 pi i m q / R)
 // (minus sign for the forward transform), the codelet set that PocketFFT's
 // passes cover (impulse/fft/c_pocketfft/pocketfft.c:300-865 for radix
 // 2/3/4/5/7/11; impulse/fft/cpp_pocketfft/pocketfft_hdronly.h:727-1305 adds
-// radix 8).  Radix 16 is new here.  The odd prime radices use the symmetric
+// radix 8).  Radices 13 and 16 are new here.  The odd prime radices use the symmetric
 // pair form: with a_k = v_k + v_{R-k} and b_k = v_k - v_{R-k},
 //   V_q = v_0 + sum_k a_k cos(2 pi k q/R) -+ i sum_k b_k sin(2 pi k q/R),
 // and V_{R-q} the same with the sign of the second sum flipped.
@@ -20,9 +20,12 @@ IGD constexpr double odd_cos(int P, int k)
          : P == 5 ? (k == 1 ? 0.3090169943749474241022934 : -0.8090169943749474241022934)
          : P == 7 ? (k == 1 ? 0.6234898018587335305250049 : k == 2 ? -0.2225209339563144042889026
                                                                      : -0.9009688679024191262361023)
-         : (k == 1 ? 0.8412535328311811688618117 : k == 2 ? 0.4154150130018864255292741
+         : P == 11 ? (k == 1 ? 0.8412535328311811688618117 : k == 2 ? 0.4154150130018864255292741
             : k == 3 ? -0.1423148382732851404437927 : k == 4 ? -0.6548607339452850640569251
-                                                              : -0.9594929736144973898903681);
+                                                              : -0.9594929736144973898903681)
+         : (k == 1 ? 0.8854560256532098959003755 : k == 2 ? 0.5680647467311558025118076
+            : k == 3 ? 0.1205366802553230533490677 : k == 4 ? -0.3546048870425356259696379
+            : k == 5 ? -0.7485107481711010986346306 : -0.9709418174260520271569823);
 }
 IGD constexpr double odd_sin(int P, int k)
 {
@@ -30,9 +33,12 @@ IGD constexpr double odd_sin(int P, int k)
          : P == 5 ? (k == 1 ? 0.9510565162951535721164393 : 0.5877852522924731291687060)
          : P == 7 ? (k == 1 ? 0.7818314824680298087084445 : k == 2 ? 0.9749279121818236070181317
                                                                      : 0.4338837391175581204757683)
-         : (k == 1 ? 0.5406408174555975821076360 : k == 2 ? 0.9096319953545183714117154
+         : P == 11 ? (k == 1 ? 0.5406408174555975821076360 : k == 2 ? 0.9096319953545183714117154
             : k == 3 ? 0.9898214418809327323760920 : k == 4 ? 0.7557495743542582837740358
-                                                             : 0.2817325568414296977114179);
+                                                             : 0.2817325568414296977114179)
+         : (k == 1 ? 0.4647231720437685456560153 : k == 2 ? 0.8229838658936563945796174
+            : k == 3 ? 0.9927088740980539928007516 : k == 4 ? 0.9350162426854148234397846
+            : k == 5 ? 0.6631226582407952023767855 : 0.2393156642875577671487537);
 }
 
 constexpr double kSqrtHalf = 0.7071067811865475244008444;

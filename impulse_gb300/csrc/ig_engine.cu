@@ -143,7 +143,7 @@ static bool gpu_factor(long long L, std::vector<int> &rad, int E = 0, int order 
     if (n % 8 == 0) { rad.push_back(8); n /= 8; }
     if (n % 4 == 0) { rad.push_back(4); n /= 4; }
     if (n % 2 == 0) { rad.push_back(2); n /= 2; }
-    for (int p : {11, 7, 5, 3})
+    for (int p : {13, 11, 7, 5, 3})
         while (n % p == 0) { rad.push_back(p); n /= p; }
     if (order == 1) std::reverse(rad.begin(), rad.end());
     return n == 1;
@@ -356,12 +356,13 @@ static void finish_layout(Core &c, long long L, long long M, const TuneCfg &cfg 
 {
     c.d.E = elems_per_thread(L, cfg.E);
     c.d.lpc_pref = cfg.lpc;
-    bool odd35 = false, odd711 = false;
+    bool odd35 = false, odd711 = false, full = c.d.blue == 2;
     for (int s = 0; s < c.d.nst; ++s) {
         odd35 |= c.d.st[s].R == 3 || c.d.st[s].R == 5;
         odd711 |= c.d.st[s].R == 7 || c.d.st[s].R == 11;
+        full |= c.d.st[s].R == 13;
     }
-    c.d.rs = odd711 ? RS_ALL : odd35 ? (c.d.E == 8 ? RS_P235 : RS_ALL) : RS_P2;
+    c.d.rs = full ? RS_FULL : odd711 ? RS_ALL : odd35 ? (c.d.E == 8 ? RS_P235 : RS_ALL) : RS_P2;
     // double-float 8-element kernels: the 2/3/5 variant fits the register cap
     // without spills where the power-of-two one does not
     if (c.a == A_DF && c.d.E == 8 && c.d.rs == RS_P2) c.d.rs = RS_P235;
@@ -417,6 +418,77 @@ static void build_chirp(Core &c, long long M, long long L, void *&chirp, void *&
     ck(cudaDeviceSynchronize(), "chirp tables");
 }
 
+// Rader tables for a prime M over the Stockham length L = M - 1: the index
+// maps of the generator g and B = FFT_L(exp(-2 pi i g^m / M)) / L, computed
+// from long-double roots with the double-float engine, then rounded to the
+// core type.
+static bool is_prime(long long n)
+{
+    if (n < 2) return false;
+    for (long long d = 2; d * d <= n; ++d)
+        if (n % d == 0) return false;
+    return true;
+}
+static long long powmod(long long b, long long e, long long m)
+{
+    long long r = 1;
+    b %= m;
+    while (e) {
+        if (e & 1) r = r * b % m;
+        b = b * b % m;
+        e >>= 1;
+    }
+    return r;
+}
+static long long primitive_root(long long p)
+{
+    std::vector<long long> fac;
+    long long n = p - 1;
+    for (long long d = 2; d * d <= n; ++d)
+        if (n % d == 0) {
+            fac.push_back(d);
+            while (n % d == 0) n /= d;
+        }
+    if (n > 1) fac.push_back(n);
+    for (long long g = 2; g < p; ++g) {
+        bool ok = true;
+        for (long long f : fac)
+            if (powmod(g, (p - 1) / f, p) == 1) { ok = false; break; }
+        if (ok) return g;
+    }
+    return 1;
+}
+static void build_rader(Core &c, long long M)
+{
+    const long long L = M - 1;
+    const long long g = primitive_root(M), gi = powmod(g, M - 2, M);
+    std::vector<int> rin(L), rout(M, 0);
+    std::vector<double> b(2 * L);
+    long long x = 1, y = 1;
+    for (long long q = 0; q < L; ++q) {
+        rin[q] = (int)x;        // g^-q
+        rout[y] = (int)q;       // g^q = y
+        const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)y / (long double)M;
+        b[2 * q] = (double)cosl(ang);
+        b[2 * q + 1] = (double)sinl(ang);
+        x = x * gi % M;
+        y = y * g % M;
+    }
+    int *din = (int *)c.alloc(L * sizeof(int)), *dout = (int *)c.alloc(M * sizeof(int));
+    ck(cudaMemcpy(din, rin.data(), L * sizeof(int), cudaMemcpyHostToDevice), "rader tables");
+    ck(cudaMemcpy(dout, rout.data(), M * sizeof(int), cudaMemcpyHostToDevice), "rader tables");
+    DevBuf b64(L * 16);
+    ck(cudaMemcpy(b64.p, b.data(), L * 16, cudaMemcpyHostToDevice), "rader tables");
+    auto dfcore = get_core(A_DF, L, false);
+    run_core_on_device(*dfcore, b64.p, b64.p, 1, 1, 1.0 / (double)L, 0);
+    void *bf = c.alloc(L * slot_bytes(c.a));
+    launch_convert_a(c.a, b64.p, bf, L);
+    ck(cudaDeviceSynchronize(), "rader tables");
+    c.d.rin = din;
+    c.d.rout = dout;
+    c.d.chirpf = bf;
+}
+
 static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
 {
     auto c = std::make_shared<Core>();
@@ -438,6 +510,15 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
         build_stockham(*c, M, rad);
         c->d.blue = 0;
         finish_layout(*c, M, M, cfg);
+    } else if (!smooth && M > 2 && is_prime(M) &&
+               gpu_factor(M - 1, rad, cfg.E, cfg.order) && fits_smem(a, M - 1, M)) {
+        // prime length: Rader over the Stockham length M - 1
+        c->kind = 0;
+        c->d.blue = 2;
+        build_stockham(*c, M - 1, rad);
+        finish_layout(*c, M - 1, M, cfg);
+        build_rader(*c, M);
+        c->n2 = M - 1;
     } else if (!smooth) {
         long long L = good_size_gpu(2 * M - 1);
         std::vector<int> radL;
@@ -1317,14 +1398,14 @@ size_t ig_rfft_length(ig_rfft_plan plan) { return plan ? plan->n : 0; }
 int ig_cfft_uses_bluestein(ig_cfft_plan plan, size_t *n2)
 {
     if (!plan) return IG_EINVAL;
-    bool b = plan->core->d.blue || plan->core->kind == 2;
+    bool b = plan->core->d.blue == 1 || plan->core->kind == 2;
     if (n2) *n2 = b ? (size_t)plan->core->n2 : 0;
     return b ? 1 : 0;
 }
 int ig_rfft_uses_bluestein(ig_rfft_plan plan, size_t *n2)
 {
     if (!plan) return IG_EINVAL;
-    bool b = plan->core->d.blue || plan->core->kind == 2;
+    bool b = plan->core->d.blue == 1 || plan->core->kind == 2;
     if (n2) *n2 = b ? (size_t)plan->core->n2 : 0;
     return b ? 1 : 0;
 }

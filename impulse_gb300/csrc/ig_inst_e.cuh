@@ -20,7 +20,7 @@ static void launch_rs(const CoreDesc &d, const IODesc &io, unsigned grid, unsign
     case LAY_R2HC: IG_K(RS, LAY_R2HC); break;
     case LAY_PR2HC: IG_K(RS, LAY_PR2HC); break;
     case LAY_TW: IG_K(RS, LAY_TW); break;
-    default: IG_K(RS_ALL, LAY_GEN); break;
+    default: IG_K(RS_FULL, LAY_GEN); break;
     }
 }
 #undef IG_K
@@ -30,19 +30,20 @@ cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaS
 {
     const unsigned grid = (unsigned)((io.nlines + io.lpc - 1) / io.lpc), blk = (unsigned)(io.lpc * io.tpl);
     if constexpr (!Variants<T, E>::kSpecialised) {
-        k_fft_smem<T, E, RS_ALL, LAY_GEN, DB><<<grid, blk, smem, st>>>(d, io);
+        k_fft_smem<T, E, RS_FULL, LAY_GEN, DB><<<grid, blk, smem, st>>>(d, io);
     } else {
-        if (io.lay == LAY_GEN) k_fft_smem<T, E, RS_ALL, LAY_GEN, DB><<<grid, blk, smem, st>>>(d, io);
+        if (io.lay == LAY_GEN) k_fft_smem<T, E, RS_FULL, LAY_GEN, DB><<<grid, blk, smem, st>>>(d, io);
         else if (d.rs == RS_P2) launch_rs<T, E, DB, RS_P2>(d, io, grid, blk, smem, st);
         else if (E == 8 && d.rs == RS_P235) launch_rs<T, E, DB, (E == 8 ? RS_P235 : RS_ALL)>(d, io, grid, blk, smem, st);
-        else launch_rs<T, E, DB, RS_ALL>(d, io, grid, blk, smem, st);
+        else if (d.rs == RS_ALL) launch_rs<T, E, DB, RS_ALL>(d, io, grid, blk, smem, st);
+        else launch_rs<T, E, DB, RS_FULL>(d, io, grid, blk, smem, st);
     }
     return cudaGetLastError();
 }
 
 template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes)
 {
-    cudaError_t e = set_smem_attr(k_fft_smem<T, E, RS_ALL, LAY_GEN, DB>, bytes);
+    cudaError_t e = set_smem_attr(k_fft_smem<T, E, RS_FULL, LAY_GEN, DB>, bytes);
     if constexpr (Variants<T, E>::kSpecialised) {
         const int lays[4] = {LAY_C2C, LAY_R2HC, LAY_PR2HC, LAY_TW};
         (void)lays;
@@ -53,6 +54,7 @@ template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes)
     if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_TW, DB>, bytes);
         IG_S(RS_P2)
         IG_S(RS_ALL)
+        IG_S(RS_FULL)
         if constexpr (E == 8) { IG_S(RS_P235) }
 #undef IG_S
     }

@@ -209,7 +209,7 @@ __device__ __forceinline__ void stage_db(const cx<T> *src, cx<T> *dst, int LS2, 
 template <int E, int RS> __host__ __device__ constexpr bool rs_has(int R)
 {
     return (R == 2 || R == 4 || R == 8) || (R == 16 && E == 16) || (RS >= RS_P235 && (R == 3 || R == 5)) ||
-           (RS == RS_ALL && (R == 7 || R == 11));
+           (RS >= RS_ALL && (R == 7 || R == 11)) || (RS == RS_FULL && R == 13);
 }
 
 // Forward stages only: a backward transform runs them on conjugated data
@@ -228,6 +228,7 @@ __device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl,
         case 5: if constexpr (rs_has<E, RS>(5)) stage<T, E, 5>(sm, P, s, nl, tpl, g, t); break;
         case 7: if constexpr (rs_has<E, RS>(7)) stage<T, E, 7>(sm, P, s, nl, tpl, g, t); break;
         case 11: if constexpr (rs_has<E, RS>(11)) stage<T, E, 11>(sm, P, s, nl, tpl, g, t); break;
+        case 13: if constexpr (rs_has<E, RS>(13)) stage<T, E, 13>(sm, P, s, nl, tpl, g, t); break;
         default: break;
         }
     }
@@ -251,6 +252,7 @@ __device__ __forceinline__ int run_stages_db(cx<T> *sm, int cur, const CoreDesc 
         case 5: if constexpr (rs_has<E, RS>(5)) stage_db<T, E, 5>(src, dst, LS2, P, s, nl, tpl, g, t); break;
         case 7: if constexpr (rs_has<E, RS>(7)) stage_db<T, E, 7>(src, dst, LS2, P, s, nl, tpl, g, t); break;
         case 11: if constexpr (rs_has<E, RS>(11)) stage_db<T, E, 11>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 13: if constexpr (rs_has<E, RS>(13)) stage_db<T, E, 13>(src, dst, LS2, P, s, nl, tpl, g, t); break;
         default: break;
         }
         cur = LS - cur;
@@ -347,6 +349,44 @@ __device__ __forceinline__ void store_unit(const IODesc &io, char *base, int u, 
 // input / output base pointers given explicitly (the persistent work-list
 // kernel keeps its groups' pointers relative to per-launch bases).  Threads
 // beyond lpc * tpl take part only in the barriers.
+// Rader permutations of one line through registers (reads, barrier, writes,
+// barrier).  A thread covers u = t + k tpl, k <= E, which reaches M because
+// E tpl >= L = M - 1.
+//  gather (out = false): line[q] = line[idx[q]] for q < L, x[0] saved at *x0s;
+//  scatter (out = true): line[0] = x0 + A0 (A0 saved at *a0s), and
+//  line[u] = x0 + conj(line[idx[u]]) for 0 < u < M.
+template <class T, int E>
+__device__ __forceinline__ void rader_permute(cx<T> *line, const int *__restrict__ idx, int L, int tpl, int t,
+                                              int pad, bool act, cx<T> *x0s, cx<T> *a0s, bool out)
+{
+    constexpr int K = E + 1;
+    const int n = out ? L + 1 : L;
+    cx<T> v[K];
+    cx<T> x0{};
+    if (act) {
+        x0 = out ? sget(x0s) : sget(line);
+        const cx<T> a0 = out ? sget(a0s) : cx<T>{};
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int u = t + k * tpl;
+            if (u < n) {
+                if (!out) v[k] = sget(line + sp(idx[u], pad));
+                else v[k] = u == 0 ? a0 : conjx(sget(line + sp(idx[u], pad)));
+            }
+        }
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int u = t + k * tpl;
+            if (u < n) sput(line + sp(u, pad), out ? crenorm(x0 + v[k]) : v[k]);
+        }
+        if (!out && t == 0) sput(x0s, x0);
+    }
+    __syncthreads();
+}
+
 template <class T, int E, int RS, int LAY, bool DB = (E == 8)>
 __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, long long blk, const char *in_base,
                                           char *out_base)
@@ -367,7 +407,8 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     const int nl = (int)min((long long)lpc, io.nlines - line0);
     const int M = P.M;
     // backward Stockham cores run the forward stages on conjugated data
-    const bool cc = !io.fwd && !P.blue;
+    // (Rader cores compute the forward DFT like Stockham ones)
+    const bool cc = !io.fwd && P.blue != 1;
     // core mapping: line g, lane t of the line
     const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
     cx<T> *const line_a = sm + (size_t)(g < nl ? g : 0) * LSt;
@@ -567,13 +608,18 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     // Stockham: one pass in the transform's direction.  Bluestein (fftblue_fft,
     // pocketfft.c:1945): a = x * chirp(-+), zero pad to L, FFT_L, multiply by
     // chirpf (conjugated for the backward transform), IFFT_L, multiply by chirp(-+).
+    // Rader (prime M, L = M - 1; forward): a[q] = x[g^-q], A = FFT_L(a),
+    // C = A * B with B = FFT_L(w^(g^m)) / L, c = IFFT_L(C) as conj(FFT_L(conj C)),
+    // X[0] = x[0] + A[0], X[g^p] = x[0] + c[p].
     {
         const cx<T> *ch = reinterpret_cast<const cx<T> *>(P.chirp);
         const cx<T> *chf = reinterpret_cast<const cx<T> *>(P.chirpf);
         const int L = P.L;
+        constexpr bool kRader = RS == RS_FULL;  // Rader steps compiled in the full class only
+        const bool blue = P.blue == 1, rader = kRader && P.blue == 2;
         const int npass = P.blue ? 2 : 1;
         for (int pass = 0; pass < npass; ++pass) {
-            if (P.blue && g < nl) {
+            if (blue && g < nl) {
                 if (pass == 0) {
                     for (int u = t; u < L; u += tpl) {
                         cx<T> z = cx<T>{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
@@ -588,6 +634,21 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     }
                 }
             }
+            if constexpr (kRader) if (rader) {
+                if (pass == 0) {
+                    // gather a[q] = x[rin[q]] through registers; x[0] kept at slot L + 1
+                    rader_permute<T, E>(myline, P.rin, L, tpl, t, pad, g < nl, line_a + sp(L + 1, pad), nullptr, false);
+                } else {
+                    // A[0] to slot L; C = A B, stored conjugated
+                    cx<T> a0{};
+                    if (g < nl) a0 = sget(myline);
+                    __syncthreads();
+                    if (g < nl) {
+                        if (t == 0) sput(line_a + sp(L, pad), a0);
+                        for (int u = t; u < L; u += tpl) sput(myline + sp(u, pad), conjx(cmul(sget(myline + sp(u, pad)), chf[u])));
+                    }
+                }
+            }
             if (P.blue) __syncthreads();
             if constexpr (DB) {
                 cur = run_stages_db<T, E, RS>(sm, cur, P, nl, tpl, g, t);
@@ -596,7 +657,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 run_stages<T, E, RS>(sm, P, nl, tpl, g, t);
             }
         }
-        if (P.blue) {
+        if (blue) {
             if (g < nl)
                 for (int u = t; u < M; u += tpl) {
                     cx<T> z = conjx(sget(myline + sp(u, pad)));
@@ -604,6 +665,10 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 }
             __syncthreads();
         }
+        if constexpr (kRader)
+            if (rader)
+                rader_permute<T, E>(myline, P.rout, L, tpl, t, pad, g < nl, line_a + sp(L + 1, pad),
+                                    line_a + sp(L, pad), true);
     }
 
     // ---- post-processing: real split ------------------------------------------
@@ -757,7 +822,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
 // registers, which lets three 256-thread CTAs share an SM
 template <class T, int E, int RS, bool DB> constexpr int fft_smem_regs()
 {
-    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS == RS_ALL ? 96 : 80;
+    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS >= RS_ALL ? 96 : 80;
     if constexpr (DB && E == 8 && std::is_same<T, float>::value) return 80;
     return 128;
 }
@@ -796,7 +861,7 @@ __global__ void __launch_bounds__(512, 1) k_fft_worklist(const WorkGroup *__rest
         const WorkGroup &G = groups[lo];
         const char *ib = G.in_base == 0 ? in : G.in_base == 1 ? (const char *)out : (const char *)scr;
         char *ob = G.out_base == 1 ? out : G.out_base == 2 ? scr : (char *)in;
-        fft_block<T, E, RS_ALL, LAY_GEN>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]), ib + (size_t)G.io.in,
+        fft_block<T, E, RS_FULL, LAY_GEN>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]), ib + (size_t)G.io.in,
                         ob + (size_t)G.io.out);
         __syncthreads();
     }

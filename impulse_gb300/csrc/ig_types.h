@@ -31,6 +31,7 @@ constexpr int LAY_TW = 4;     // complex in / out with the four-step twiddle or 
 constexpr int RS_P2 = 0;   // 2, 4, 8, 16
 constexpr int RS_P235 = 1; // 2, 4, 8, 16, 3, 5
 constexpr int RS_ALL = 2;  // 2, 3, 4, 5, 7, 8, 11, 16
+constexpr int RS_FULL = 3; // all of RS_ALL, 13, and the Rader steps (also the generic-layout kernels)
 
 enum InKind { IN_C = 0, IN_R = 1, IN_P = 2, IN_HC = 3 };
 enum OutKind { OUT_C = 0, OUT_R = 1, OUT_P = 2, OUT_HC = 3 };
@@ -41,7 +42,7 @@ struct CoreDesc {
     int M;    // logical complex length of the core transform
     int L;    // Stockham length run in shared memory (M, or n2 for Bluestein)
     int LS;   // shared-memory complex slots per line (>= max(L, M + 1))
-    int blue; // 1: Bluestein core
+    int blue; // 1: Bluestein core, 2: Rader core (prime M, Stockham length M - 1)
     int pad;  // shared-memory padding: slot i is stored at i + (i >> pad)
     int E;    // complex elements per thread (kernel variant 8 or 16): L / E threads per line
     int rs;   // radix class of the kernel variant (0: 2/4/8/16, 1: + 3/5, 2: all)
@@ -54,6 +55,8 @@ struct CoreDesc {
     const void *chirp;  // cx<T> exp(+i pi m^2 / M), m < M  (Bluestein)
     const void *chirpf; // cx<T> FFT_L of the padded chirp / L  (Bluestein)
     const void *rtw;    // cx<T> exp(-2 pi i k / (2M)), k <= M  (real split)
+    const int *rin;     // Rader (blue = 2): g^-q mod M, q < M - 1
+    const int *rout;    // Rader: p with g^p = u, 0 < u < M
 };
 
 struct IODesc {
