@@ -167,7 +167,7 @@ struct Core {
     Arith a;
     long long M = 0;
     bool real_tw = false;  // rtw built (core of an even real transform of length 2M)
-    int kind = 0;          // 0 smem, 1 four-step, 2 Bluestein over a four-step core
+    int kind = 0;          // 0 smem, 1 four-step, 2 Bluestein / 3 Rader over a multi-pass core
     CoreDesc d{};
     std::vector<std::unique_ptr<DevBuf>> mem;
     // four-step
@@ -270,7 +270,7 @@ static void set_fct_parts(IODesc &io)
 // variants compile the common layouts without per-element runtime checks)
 static int choose_layout(Arith a, const IODesc &io)
 {
-    if (a == A_F64) return LAY_GEN;
+    if (a == A_F64 || io.keep0) return LAY_GEN;
     const bool plain = !io.conj_in && !io.conj_out && !io.real_out && io.pre == PRE_NONE;
     if (io.tw4 || io.mul)
         return (plain && !io.pair && io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C) ? LAY_TW
@@ -458,6 +458,29 @@ static long long primitive_root(long long p)
     }
     return 1;
 }
+// Rader in one CTA when M - 1 factors into the kernel radices and its core
+// runs double-buffered (a single-buffered 16-element core spills registers);
+// over a multi-pass core when M - 1 splits into two such factors.
+static bool rader_single(Arith a, long long M, const TuneCfg &cfg)
+{
+    std::vector<int> rad;
+    if (!gpu_factor(M - 1, rad, cfg.E, cfg.order) || !fits_smem(a, M - 1, M)) return false;
+    if (elems_per_thread(M - 1, cfg.E) == 8) return true;
+    const long long slots = (M + 1) + ((M + 1) >> 3);
+    return 2 * slots * (long long)slot_bytes(a) <= (long long)max_smem() - 4096;
+}
+static bool rader_multi(Arith a, long long M)
+{
+    const long long L = M - 1;
+    for (long long d = 2; d * d <= L; ++d) {
+        if (L % d) continue;
+        std::vector<int> r1, r2;
+        if (gpu_factor(d, r1) && gpu_factor(L / d, r2) && fits_smem(a, d, d) && fits_smem(a, L / d, L / d))
+            return true;
+    }
+    return false;
+}
+
 static void build_rader(Core &c, long long M)
 {
     const long long L = M - 1;
@@ -510,15 +533,21 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
         build_stockham(*c, M, rad);
         c->d.blue = 0;
         finish_layout(*c, M, M, cfg);
-    } else if (!smooth && M > 2 && is_prime(M) &&
-               gpu_factor(M - 1, rad, cfg.E, cfg.order) && fits_smem(a, M - 1, M)) {
-        // prime length: Rader over the Stockham length M - 1
+    } else if (!smooth && M > 2 && is_prime(M) && rader_single(a, M, cfg)) {
+        // prime length: Rader over the Stockham length M - 1 in one CTA
         c->kind = 0;
         c->d.blue = 2;
+        gpu_factor(M - 1, rad, cfg.E, cfg.order);
         build_stockham(*c, M - 1, rad);
         finish_layout(*c, M - 1, M, cfg);
         build_rader(*c, M);
         c->n2 = M - 1;
+    } else if (!smooth && M > 2 && is_prime(M) && rader_multi(a, M)) {
+        // prime length: Rader over a multi-pass core of length M - 1
+        c->kind = 3;
+        c->n2 = M - 1;
+        c->sub = get_core(a, M - 1, false);
+        build_rader(*c, M);
     } else if (!smooth) {
         long long L = good_size_gpu(2 * M - 1);
         std::vector<int> radL;
@@ -643,7 +672,7 @@ static IODesc blank_io()
 // scratch for the multi-pass paths: per (device, stream), grow-only
 // --------------------------------------------------------------------------
 struct Scratch {
-    std::unique_ptr<DevBuf> buf[4];
+    std::unique_ptr<DevBuf> buf[6];
     void *get(int i, size_t bytes)
     {
         if (!buf[i] || buf[i]->bytes < bytes) {
@@ -762,6 +791,7 @@ static void fourstep_passes(const Core &c, const IODesc &io, char *B, IODesc &p1
     p1.conj_out = 0;
     p1.real_out = 0;
     p1.mul = nullptr;
+    p1.keep0 = nullptr;
     p1.fct = 1.0;
     p1.tw4 = 1;
     p1.tw4N = M;
@@ -799,6 +829,40 @@ static void fourstep_passes(const Core &c, const IODesc &io, char *B, IODesc &p1
         p2.mul_a = 1;
         p2.mul_b = N1;
     }
+    p2.keep0_rows = (int)N1;
+}
+
+// The convolution of Bluestein (kind 2) and Rader (kind 3) on nl contiguous
+// scratch lines of length L, in place: forward FFT_L with the product by the
+// transformed kernel (chirpf / B) fused into its last pass, then the
+// backward FFT_L.  Bluestein conjugates the kernel for the backward
+// direction; Rader always runs forward (its maps conjugate) and keeps each
+// line's A[0] from before the product in a0buf.
+static void convolve_passes(const Core &c, char *A, long long L, long long nl, int fwd, void *a0buf,
+                            cudaStream_t st)
+{
+    const long long ES = 2 * (long long)store_real_bytes(c.a);
+    const bool rader = c.kind == 3;
+    for (int pass = 0; pass < 2; ++pass) {
+        IODesc q = blank_io();
+        contig_side(q, false, A, ES, L, nl);
+        contig_side(q, true, A, ES, L, nl);
+        q.nlines = nl;
+        q.in_kind = IN_C;
+        q.out_kind = OUT_C;
+        q.cnt_in = q.cnt_out = (int)L;
+        q.nreal = L;
+        q.fwd = pass == 0 ? 1 : 0;
+        if (pass == 0) {
+            q.mul = rader ? c.d.chirpf : c.chirpf;
+            q.mul_a = 0;
+            q.mul_b = 1;
+            q.mul_conj = (!rader && !fwd) ? 1 : 0;
+            q.keep0 = a0buf;
+            q.keep0_rows = 1;  // four-step cores set N1 for their second pass
+        }
+        run_complex(*c.sub, q, st);
+    }
 }
 
 // Run a complex core of any kind.  io: user-facing sides, kinds, pre/post,
@@ -824,18 +888,25 @@ static void run_complex(const Core &c, const IODesc &io_all, cudaStream_t st)
         if (io.pair) {
             // two real lines per complex line: per-line scales, paired gather,
             // complex core on contiguous scratch, paired scatter
-            const long long L = c.kind == 2 ? c.n2 : c.M;
+            const bool rader = c.kind == 3;
+            const long long L = (c.kind == 2 || rader) ? c.n2 : c.M;
             int *esc = (int *)scr.get(3, (size_t)(2 * nl * sizeof(int)));
             char *A = (char *)scr.get(0, (size_t)(nl * L * ES));
             MapDesc mp{};
-            mp.kind = c.kind == 2 ? MAP_BLUE : MAP_PLAIN;
+            mp.kind = c.kind == 2 ? MAP_BLUE : rader ? MAP_RADER : MAP_PLAIN;
             mp.M = c.M;
             mp.scr_len = L;
             mp.scr = A;
             mp.chirp = c.chirp;
             mp.fwd = io.fwd;
+            if (rader) {
+                mp.ridx = c.d.rin;
+                mp.x0buf = scr.get(4, (size_t)(nl * ES));
+                mp.a0buf = scr.get(5, (size_t)(nl * ES));
+            }
             launch_pair_map(c.a, 0, io, mp, esc, st);
             launch_pair_map(c.a, 1, io, mp, esc, st);
+            if (rader) mp.ridx = c.d.rout;
             if (c.kind == 1) {
                 char *B = (char *)scr.get(1, (size_t)(nl * L * ES));
                 IODesc q = blank_io();
@@ -849,24 +920,7 @@ static void run_complex(const Core &c, const IODesc &io_all, cudaStream_t st)
                 q.fwd = io.fwd;
                 run_fourstep(c, q, B, st);
             } else {
-                for (int pass = 0; pass < 2; ++pass) {
-                    IODesc q = blank_io();
-                    contig_side(q, false, A, ES, L, nl);
-                    contig_side(q, true, A, ES, L, nl);
-                    q.nlines = nl;
-                    q.in_kind = IN_C;
-                    q.out_kind = OUT_C;
-                    q.cnt_in = q.cnt_out = (int)L;
-                    q.nreal = L;
-                    q.fwd = pass == 0 ? 1 : 0;
-                    if (pass == 0) {
-                        q.mul = c.chirpf;
-                        q.mul_a = 0;
-                        q.mul_b = 1;
-                        q.mul_conj = io.fwd ? 0 : 1;
-                    }
-                    run_complex(*c.sub, q, st);
-                }
+                convolve_passes(c, A, L, nl, io.fwd, rader ? mp.a0buf : nullptr, st);
             }
             launch_pair_map(c.a, 2, io, mp, esc, st);
             continue;
@@ -922,7 +976,8 @@ static void run_complex(const Core &c, const IODesc &io_all, cudaStream_t st)
                 run_fourstep(c, f, B, st);
             }
         } else {
-            // Bluestein over a (four-step) core of length n2
+            // Bluestein (kind 2) or Rader (kind 3) over a multi-pass core of length n2
+            const bool rader = c.kind == 3;
             const long long M = c.M, L = c.n2;
             char *A = (char *)scr.get(0, (size_t)(nl * L * ES));
             IODesc src = io;
@@ -942,31 +997,20 @@ static void run_complex(const Core &c, const IODesc &io_all, cudaStream_t st)
                 src.cnt_in = (int)M;
             }
             MapDesc mp{};
-            mp.kind = MAP_BLUE;
+            mp.kind = rader ? MAP_RADER : MAP_BLUE;
             mp.M = M;
             mp.scr_len = L;
             mp.scr = A;
             mp.chirp = c.chirp;
             mp.fwd = io.fwd;
-            launch_map(c.a, true, src, mp, st);
-            // forward FFT_L with the chirp-spectrum product, backward FFT_L, in place in A
-            for (int pass = 0; pass < 2; ++pass) {
-                IODesc q = blank_io();
-                contig_side(q, false, A, ES, L, nl);
-                contig_side(q, true, A, ES, L, nl);
-                q.nlines = nl;
-                q.in_kind = IN_C;
-                q.out_kind = OUT_C;
-                q.cnt_in = q.cnt_out = (int)L;
-                q.fwd = pass == 0 ? 1 : 0;
-                if (pass == 0) {
-                    q.mul = c.chirpf;
-                    q.mul_a = 0;
-                    q.mul_b = 1;
-                    q.mul_conj = io.fwd ? 0 : 1;
-                }
-                run_complex(*c.sub, q, st);
+            if (rader) {
+                mp.ridx = c.d.rin;
+                mp.x0buf = scr.get(4, (size_t)(nl * ES));
+                mp.a0buf = scr.get(5, (size_t)(nl * ES));
             }
+            launch_map(c.a, true, src, mp, st);
+            if (rader) mp.ridx = c.d.rout;
+            convolve_passes(c, A, L, nl, io.fwd, rader ? mp.a0buf : nullptr, st);
             IODesc h = io;
             h.pre = PRE_NONE;
             if (io.post == POST_SPLIT) {
@@ -1472,7 +1516,7 @@ static void *noalloc_scratch()
 // Same transform as ig_cfft_exec_device, with no device-memory allocation:
 // single-CTA plans need no scratch, four-step plans use the static array
 // (at most IG_NOALLOC_SCRATCH_BYTES = batch * length * complex size).  Plans
-// that run Bluestein over a four-step core are rejected.  The first call on
+// that run Bluestein or Rader over a multi-pass core are rejected.  The first call on
 // a device looks up the array's address there; make that first call before
 // any stream capture.  All calls share the array and it keeps the previous
 // call's contents (this path writes every scratch element before reading
@@ -1484,8 +1528,8 @@ int ig_cfft_exec_device_noalloc(ig_cfft_plan plan, const void *in, void *out, si
         if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
         const Core &c = *plan->core;
         const long long es = 2 * (long long)store_real_bytes(plan->a);
-        if (c.kind == 2)
-            raise(IG_EINVAL, "no-allocation execution does not cover Bluestein over a multi-pass core");
+        if (c.kind == 2 || c.kind == 3)
+            raise(IG_EINVAL, "no-allocation execution does not cover Bluestein or Rader over a multi-pass core");
         if (batch == 0) return;
         char *scr = nullptr;
         if (c.kind == 1) {
@@ -2344,8 +2388,8 @@ int ig_autotune(int dtype, size_t length, int kind, double *best_ms)
         // candidates
         auto base = make_core(a, M, even);
         std::vector<TuneCfg> cands;
-        if (base->kind == 2) {
-            // Bluestein over a four-step core: tune the core's complex length
+        if (base->kind == 2 || base->kind == 3) {
+            // Bluestein or Rader over a multi-pass core: tune the core's complex length
             double sub_ms = 0.0;
             int rc = ig_autotune(dtype, (size_t)base->n2, 0, &sub_ms);
             if (rc != IG_OK) raise(rc, ig_last_error_string());

@@ -721,7 +721,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const long long l = line0 + g2;
             char *base = out_base + line_off(io, l, true);
             const cx<T> *line = sm + (size_t)g2 * LSt + cur;
-            const int i0l = (io.tw4 || io.mul || paired) ? line_i0(io, l) : 0;
+            const int i0l = (io.tw4 || io.mul || io.keep0 || paired) ? line_i0(io, l) : 0;
             const bool has_b = paired && (2LL * i0l + 1 < io.pair_n0);
             const int n2 = io.tw4 ? i0l : 0;
             const int ml = io.mul ? (int)(i0l * io.mul_a) : 0;
@@ -803,6 +803,13 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     const unsigned hi = fdiv(tt, io.fdS), lo = tt - hi * (unsigned)io.tw4S;
                     cx<T> w = cmul(whi[hi], wlo[lo]);
                     z = io.fwd ? cmul(z, w) : cmulc(z, w);
+                }
+                if (io.keep0 && u == 0 && (io.keep0_rows == 1 || i0l == 0)) {
+                    // the transform's unit 0 before the product (Rader's A[0])
+                    S2 o;
+                    o.x = sc.apply(z.r, esc);
+                    o.y = sc.apply(z.i, esc);
+                    reinterpret_cast<S2 *>(io.keep0)[io.keep0_rows == 1 ? l : (long long)fdiv((unsigned)l, io.fb0)] = o;
                 }
                 if (io.mul) {
                     cx<T> w = mt[ml + (long long)u * io.mul_b];
@@ -959,15 +966,31 @@ __global__ void k_gather(const __grid_constant__ IODesc io, const __grid_constan
             continue;
         }
         long long cnt = io.cnt_in;
-        if (u < mp.M) {
-            long long uu = u;
+        auto read_z = [&](long long v, double &zr, double &zi) {
+            long long uu = v;
             bool cj = false;
-            if (io.pre == PRE_HERM_ODD && u >= cnt) { uu = mp.M - u; cj = true; }
+            zr = zi = 0;
+            if (io.pre == PRE_HERM_ODD && v >= cnt) { uu = mp.M - v; cj = true; }
             if (uu < cnt) {
-                read_unit<S, S2>(io, base, uu, re, im);
-                if (io.pre != PRE_NONE && uu == 0) im = 0;
-                if (cj) im = -im;
+                read_unit<S, S2>(io, base, uu, zr, zi);
+                if (io.pre != PRE_NONE && uu == 0) zi = 0;
+                if (cj) zi = -zi;
             }
+        };
+        if (mp.kind == MAP_RADER) {
+            // a[q] = x[g^-q]; x[0] kept per line (conjugated for the backward direction)
+            read_z(mp.ridx[u], re, im);
+            if (!mp.fwd) im = -im;
+            if (u == 0) {
+                double r0, i0;
+                read_z(0, r0, i0);
+                S2 o0;
+                o0.x = (S)r0;
+                o0.y = (S)(mp.fwd ? i0 : -i0);
+                reinterpret_cast<S2 *>(mp.x0buf)[l] = o0;
+            }
+        } else if (u < mp.M) {
+            read_z(u, re, im);
         }
         if (mp.kind == MAP_BLUE) {
             if (u < mp.M) {
@@ -1016,6 +1039,13 @@ __global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_consta
             cx<T> D = chalf(za - zb);
             cx<T> O = cx<T>{D.i, -D.r};
             z = E + cmul(O, reinterpret_cast<const cx<T> *>(mp.rtw)[u]);
+        } else if (mp.kind == MAP_RADER) {
+            // X[0] = x0 + A0, X[u] = x0 + c[log_g u]
+            const S2 x0 = reinterpret_cast<const S2 *>(mp.x0buf)[l];
+            const S2 a = u == 0 ? reinterpret_cast<const S2 *>(mp.a0buf)[l] : src[mp.ridx[u]];
+            lc.fit(a.x, a.y, x0.x, x0.y);
+            z = crenorm(lc.in(a.x, a.y) + lc.in(x0.x, x0.y));
+            if (!mp.fwd) z = conjx(z);
         } else {
             S2 a = src[u];
             lc.fit(a.x, a.y);
@@ -1106,12 +1136,13 @@ __global__ void k_gather_pair(const __grid_constant__ IODesc io, const __grid_co
         const long long l = idx / mp.scr_len, u = idx - l * mp.scr_len;
         S2 *dst = reinterpret_cast<S2 *>(mp.scr) + idx;
         cx<T> z{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
-        if (u < mp.M) {
-            const char *base = io.in + line_off(io, l, false);
-            const bool has_b = 2LL * line_i0(io, l) + 1 < io.pair_n0;
-            const int ea = esc[2 * l], eb = esc[2 * l + 1];
-            const bool mirror = io.in_kind != IN_R && u >= io.cnt_in;
-            const int uu = (int)(mirror ? mp.M - u : u);
+        const char *base = io.in + line_off(io, l, false);
+        const bool has_b = 2LL * line_i0(io, l) + 1 < io.pair_n0;
+        const int ea = esc[2 * l], eb = esc[2 * l + 1];
+        // Z at logical index v of the complex line
+        auto zat = [&](long long v) {
+            const bool mirror = io.in_kind != IN_R && v >= io.cnt_in;
+            const int uu = (int)(mirror ? mp.M - v : v);
             S ar, ai, br = S(0), bi = S(0);
             load_unit<S, S2>(io, base, uu, ar, ai);
             if (has_b) load_unit<S, S2>(io, base + io.pair_in, uu, br, bi);
@@ -1119,9 +1150,23 @@ __global__ void k_gather_pair(const __grid_constant__ IODesc io, const __grid_co
             if (io.in_kind != IN_R && uu == 0) { ai = S(0); bi = S(0); }
             cx<T> A{Store<T>::in(ar, ea), Store<T>::in(ai, ea)};
             cx<T> B{Store<T>::in(br, eb), Store<T>::in(bi, eb)};
-            if (io.in_kind == IN_R) z = cx<T>{A.r, B.r};
-            else if (!mirror) z = cx<T>{A.r - B.i, A.i + B.r};
-            else z = cx<T>{A.r + B.i, B.r - A.i};
+            if (io.in_kind == IN_R) return cx<T>{A.r, B.r};
+            if (!mirror) return cx<T>{A.r - B.i, A.i + B.r};
+            return cx<T>{A.r + B.i, B.r - A.i};
+        };
+        if (mp.kind == MAP_RADER) {
+            z = zat(mp.ridx[u]);
+            if (!mp.fwd) z = conjx(z);
+            if (u == 0) {
+                cx<T> z0 = zat(0);
+                if (!mp.fwd) z0 = conjx(z0);
+                S2 o0;
+                o0.x = (S)Loc2<T>::out(crenorm(z0).r, 0);
+                o0.y = (S)Loc2<T>::out(crenorm(z0).i, 0);
+                reinterpret_cast<S2 *>(mp.x0buf)[l] = o0;
+            }
+        } else if (u < mp.M) {
+            z = zat(u);
             if (mp.kind == MAP_BLUE) {
                 cx<T> c = reinterpret_cast<const cx<T> *>(mp.chirp)[u];
                 z = mp.fwd ? cmulc(z, c) : cmul(z, c);
@@ -1157,6 +1202,13 @@ __global__ void k_scatter_pair(const __grid_constant__ IODesc io, const __grid_c
         const S2 *src = reinterpret_cast<const S2 *>(mp.scr) + l * mp.scr_len;
         const cx<T> *ch = reinterpret_cast<const cx<T> *>(mp.chirp);
         auto fetch = [&](long long k) {
+            if (mp.kind == MAP_RADER) {
+                // X[0] = x0 + A0, X[k] = x0 + c[log_g k]
+                const S2 x0 = reinterpret_cast<const S2 *>(mp.x0buf)[l];
+                const S2 a = k == 0 ? reinterpret_cast<const S2 *>(mp.a0buf)[l] : src[mp.ridx[k]];
+                cx<T> z = crenorm(cx<T>{Loc2<T>::in(a.x), Loc2<T>::in(a.y)} + cx<T>{Loc2<T>::in(x0.x), Loc2<T>::in(x0.y)});
+                return mp.fwd ? z : conjx(z);
+            }
             S2 a = src[k];
             cx<T> z{Loc2<T>::in(a.x), Loc2<T>::in(a.y)};
             if (mp.kind == MAP_BLUE) z = mp.fwd ? cmulc(z, ch[k]) : cmul(z, ch[k]);

@@ -99,6 +99,10 @@ struct IODesc {
     const void *mul;
     long long mul_a, mul_b;
     int mul_conj;
+    // storage complex of output unit 0 of each transform's first line (before
+    // the product), one per transform: Rader's A[0] on a multi-pass core
+    void *keep0;
+    int keep0_rows;  // lines per transform: 1 (one-pass core) or N1 (four-step second pass)
     // per-line byte offsets (device arrays) replacing the batch dims when set
     const long long *loff_in, *loff_out;
 };
@@ -120,6 +124,8 @@ enum MapKind {
     MAP_BLUE = 1,       // times chirp (Bluestein pre / post); gather zero-pads to scr_len
     MAP_HERM_EVEN = 2,  // gather: halfcomplex X[0..M] -> Z[0..M) (inverse of the real split)
     MAP_SPLIT_EVEN = 3, // scatter: Z[0..M) -> X[0..M] (real split), written as halfcomplex or half spectrum
+    MAP_RADER = 4,      // gather: scratch[q] = x[ridx[q]], x[0] to x0buf; scatter: X[0] = x0 + A0,
+                        // X[u] = x0 + scratch[ridx[u]]; conjugated on both sides for the backward direction
 };
 struct MapDesc {
     int kind;
@@ -128,7 +134,10 @@ struct MapDesc {
     char *scr;          // scratch base (storage complex)
     const void *chirp;  // cx<T>, MAP_BLUE
     const void *rtw;    // cx<T> exp(-2 pi i k/2M), k <= M, real split
-    int fwd;            // Bluestein direction
+    int fwd;            // Bluestein / Rader direction
+    const int *ridx;    // MAP_RADER: g^-q (gather) or the discrete log (scatter)
+    void *x0buf;        // MAP_RADER: storage complex x[0] of each scratch line
+    void *a0buf;        // MAP_RADER: storage complex A[0] of each scratch line
 };
 
 
