@@ -528,7 +528,13 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
         c->rtw = rtw;
         c->d.rtw = rtw;
     }
-    if (smooth && fits_smem(a, M, M)) {
+    // a tuned four-step split may replace a single-CTA core
+    bool force4 = false;
+    if (smooth && cfg.N1 > 1 && M % cfg.N1 == 0 && fits_smem(a, cfg.N1, cfg.N1) && fits_smem(a, M / cfg.N1, M / cfg.N1)) {
+        std::vector<int> r1, r2;
+        force4 = gpu_factor(cfg.N1, r1) && gpu_factor(M / cfg.N1, r2);
+    }
+    if (smooth && fits_smem(a, M, M) && !force4) {
         c->kind = 0;
         build_stockham(*c, M, rad);
         c->d.blue = 0;
@@ -2408,6 +2414,20 @@ int ig_autotune(int dtype, size_t length, int kind, double *best_ms)
                 }
         } else {
             const long long L = base->d.L;
+            // long single-CTA cores without double buffering also try four-step splits
+            if (!base->d.blue && base->d.E == 16 && !base->d.db) {
+                for (long long d = 2; d * d <= M; ++d)
+                    if (M % d == 0 && fits_smem(a, d, d) && fits_smem(a, M / d, M / d)) {
+                        std::vector<int> r1, r2;
+                        if (gpu_factor(d, r1) && gpu_factor(M / d, r2))
+                            for (long long n1 : {d, M / d}) {
+                                TuneCfg c;
+                                c.N1 = n1;
+                                cands.push_back(c);
+                                if (d * d == M) break;
+                            }
+                    }
+            }
             for (int order : {0, 1})
                 for (int E : {8, 16}) {
                     if (E == 8 && L > 4096) continue;
@@ -2440,11 +2460,20 @@ int ig_autotune(int dtype, size_t length, int kind, double *best_ms)
                 continue;
             }
             g_cfg_override = nullptr;
-            exec_op(a, op, N, ln, 1, 1.0, 0, core);
-            ck(cudaEventRecord(e0, 0), "event");
-            for (int r = 0; r < 3; ++r) exec_op(a, op, N, ln, 1, 1.0, 0, core);
-            ck(cudaEventRecord(e1, 0), "event");
-            ck(cudaEventSynchronize(e1), "event");
+            try {
+                exec_op(a, op, N, ln, 1, 1.0, 0, core);
+                ck(cudaEventRecord(e0, 0), "event");
+                for (int r = 0; r < 3; ++r) exec_op(a, op, N, ln, 1, 1.0, 0, core);
+                ck(cudaEventRecord(e1, 0), "event");
+                ck(cudaEventSynchronize(e1), "event");
+            } catch (const Error &err) {
+                // a configuration the kernels cannot launch is skipped
+                if (getenv("IG_TUNE_VERBOSE"))
+                    fprintf(stderr, "ig_autotune: N=%lld order=%d E=%d lpc=%d N1=%lld skipped: %s\n", N, c.order, c.E,
+                            c.lpc, c.N1, err.msg.c_str());
+                cudaGetLastError();
+                continue;
+            }
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
             TuneCfg r = c;
