@@ -329,14 +329,25 @@ def run_ours(args, rank, world):
     peak_kind = "measured"
     if not peak:
         peak, peak_kind = 6800.0, "fallback"
-    # roofline over the FFT launches: algorithmic bytes / event-timed duration per length
-    achieved = bytes64 / (sum(per_ms) / 1e3) / 1e9
+    # roofline of the dominant kernel: the lengths whose call is one k_fft_smem
+    # launch (counted live); algorithmic bytes / event-timed launch durations
+    single = []
+    for i, it in enumerate(items64):
+        lib.ig_launch_count(1)
+        step([it])
+        torch.cuda.synchronize()
+        if lib.ig_launch_count(0) == 1:
+            single.append(i)
+    sb = sum(2 * 8 * items64[i][0] * items64[i][1] for i in single)
+    st = sum(per_ms[i] for i in single)
+    achieved = sb / (st / 1e3) / 1e9 if single else 0.0
+    workload_achieved = bytes64 / (sum(per_ms) / 1e3) / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "traffic_ratio.txt")
-    if os.path.exists(prof):
+    if os.path.exists(prof) and single:
         for ln in open(prof):
             if ln.startswith("dram_bytes_per_algorithmic_byte:"):
-                traffic = round(float(ln.split(":")[1]) * bytes64 / len(items64), 1)
+                traffic = round(float(ln.split(":")[1]) * sb / len(single))
     slow = [(n, round(2 * 8 * n * b / (t / 1e3) / 1e9, 1)) for (n, b, *_), t in zip(items64, per_ms)]
     result = {
         "metric": "FFT GB/s (halfcomplex real FFT, algorithmic bytes) vs HBM peak",
@@ -355,7 +366,7 @@ def run_ours(args, rank, world):
                                f"{len(lengths)} lengths 2^a3^b5^c7^d11^e in [64,65536] + primes 1009/8191/65521, "
                                "~2^24 reals per length, out of place",
                    "lengths": lengths, "reals_per_step": int(bytes64 / 16),
-                   "l2": "inputs larger than L2 (128 MiB per length, 35 lengths per step)",
+                   "l2": f"inputs larger than L2 (128 MiB per length, {len(lengths)} lengths per step)",
                    "arith": "double-float butterflies on FP64 data",
                    "autotune_s": tune_s},
         "e2e": e2e,
@@ -363,9 +374,13 @@ def run_ours(args, rank, world):
         "clocks": clocks,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "kernel": f"k_fft_smem, one launch per length ({len(single)} of {len(items64)} lengths)",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s",
-                     "note": "achieved = algorithmic bytes of all lengths / sum of their event-timed call durations"},
+                     "workload_achieved": round(workload_achieved, 1),
+                     "note": "achieved = algorithmic bytes of the single-launch lengths / their event-timed "
+                             "launch durations; traffic = ncu DRAM bytes per algorithmic byte x bytes per launch; "
+                             "workload_achieved covers every length, multi-pass ones included"},
         "fp32": {"value": round(world * bytes32 / (ms32 / args.steps / 1e3) / 1e9, 2), "unit": "GB/s",
                  "ms_per_step": round(ms32 / args.steps, 4),
                  "speedup_vs_f64": round(ms64 / ms32, 3),
