@@ -1084,10 +1084,33 @@ static Arith arith_for(int dtype)
     return g_f64_arith == 1 ? A_F64 : A_DF;
 }
 
+// every line start and element of one side at a multiple of `align` bytes
+static bool side_aligned(const void *p, long long es, const long long *bn, const long long *bs, long long align)
+{
+    if ((uintptr_t)p % (uintptr_t)align || std::llabs(es) % align) return false;
+    for (int i = 0; i < 3; ++i)
+        if (bn[i] > 1 && std::llabs(bs[i]) % align) return false;
+    return true;
+}
+
+static void require_aligned(const void *p, size_t align, const char *what)
+{
+    if ((uintptr_t)p % align) raise(IG_EINVAL, std::string(what) + " not aligned to its element size");
+}
+
 static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, double fct, cudaStream_t st,
                     std::shared_ptr<Core> forced = nullptr)
 {
     if (ln.nlines <= 0 || N <= 0) return;
+    // scalar accesses need natural alignment; complex (pair) accesses need
+    // twice that, else the kernels read and write the two halves separately
+    {
+        const long long sr0 = (long long)store_real_bytes(a);
+        if (!side_aligned(ln.in, ln.es_in, ln.bn, ln.bsi, sr0) || !side_aligned(ln.out, ln.es_out, ln.bn, ln.bso, sr0))
+            raise(IG_EINVAL, "data pointer or stride not aligned to the element size");
+    }
+    const bool pair_in = side_aligned(ln.in, ln.es_in, ln.bn, ln.bsi, 2 * (long long)store_real_bytes(a));
+    const bool pair_out = side_aligned(ln.out, ln.es_out, ln.bn, ln.bso, 2 * (long long)store_real_bytes(a));
     IODesc io = blank_io();
     io.in = ln.in;
     io.out = ln.out;
@@ -1110,6 +1133,14 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
         core = forced ? forced : get_core(a, N, false);
         io.in_kind = IN_C;
         io.out_kind = OUT_C;
+        if (!pair_in) {
+            io.in_kind = IN_P;
+            io.ps_in = sr;
+        }
+        if (!pair_out) {
+            io.out_kind = OUT_P;
+            io.ps_out = sr;
+        }
         io.cnt_in = io.cnt_out = (int)N;
         io.fwd = forward;
         break;
@@ -1117,7 +1148,8 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
     case OP_R2C:
         M = even ? N / 2 : N;
         core = forced ? forced : get_core(a, M, even);
-        if (even && ln.es_in == sr) {
+        if (even && ln.es_in == sr &&
+            side_aligned(ln.in, 2 * sr, ln.bn, ln.bsi, 2 * sr)) {
             io.in_kind = IN_C;  // contiguous reals read as complex pairs
             io.is = 2 * sr;
         } else if (even) {
@@ -1134,7 +1166,8 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
             io.out_kind = OUT_HC;
             io.cnt_out = (int)(even ? N / 2 + 1 : (N + 1) / 2);
         } else {
-            io.out_kind = OUT_C;
+            io.out_kind = pair_out ? OUT_C : OUT_P;
+            if (!pair_out) io.ps_out = sr;
             io.cnt_out = (int)(N / 2 + 1);
             io.conj_out = forward ? 0 : 1;
             io.real_out = 1;
@@ -1144,13 +1177,14 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
     case OP_C2R:
         M = even ? N / 2 : N;
         core = forced ? forced : get_core(a, M, even);
-        io.in_kind = op == OP_HC2R ? IN_HC : IN_C;
+        io.in_kind = op == OP_HC2R ? IN_HC : (pair_in ? IN_C : IN_P);
+        if (io.in_kind == IN_P) io.ps_in = sr;
         io.cnt_in = (int)(even ? N / 2 + 1 : (N + 1) / 2);
         if (op == OP_C2R) io.conj_in = forward ? 1 : 0;
         io.pre = even ? PRE_HERM_EVEN : PRE_HERM_ODD;
         io.fwd = 0;
         if (even) {
-            if (ln.es_out == sr) {
+            if (ln.es_out == sr && side_aligned(ln.out, 2 * sr, ln.bn, ln.bso, 2 * sr)) {
                 io.out_kind = OUT_C;
                 io.os = 2 * sr;
             } else {
@@ -1319,6 +1353,36 @@ struct Workspace {
 static std::mutex g_ws_mu;
 static Workspace g_ws;
 
+// streams and chunk buffers of the pipelined host-memory batches
+static const int kPipe = 3;
+// chunk size of the pipeline: IG_PIPE_CHUNK_MB (default 16 MiB)
+static size_t pipe_chunk_bytes()
+{
+    static size_t v = [] {
+        const char *e = getenv("IG_PIPE_CHUNK_MB");
+        long mb = e ? atol(e) : 16;
+        return (size_t)std::max<long>(1, mb) << 20;
+    }();
+    return v;
+}
+struct Pipe {
+    cudaStream_t st[kPipe] = {};
+    Workspace ws[kPipe];
+};
+static std::map<int, std::unique_ptr<Pipe>> g_pipes;
+
+static Pipe &pipe_for_device()
+{
+    auto &p = g_pipes[device_id()];
+    if (!p) {
+        p.reset(new Pipe);
+        for (int i = 0; i < kPipe; ++i)
+            ck(cudaStreamCreateWithFlags(&p->st[i], cudaStreamNonBlocking), "pipeline stream");
+    }
+    return *p;
+}
+
+
 // byte span [lo, hi) covered by a strided array
 static void span_of(size_t ndim, const size_t *shape, const ptrdiff_t *st, size_t elem, long long &lo, long long &hi)
 {
@@ -1399,6 +1463,8 @@ void ig_release_caches(void)
     g_cores.clear();
     std::lock_guard<std::mutex> lk2(g_ws_mu);
     g_ws.release();
+    for (auto &kv : g_pipes)
+        for (int i = 0; i < kPipe; ++i) kv.second->ws[i].release();
 }
 
 unsigned long long ig_launch_count(int reset)
@@ -1544,6 +1610,8 @@ int ig_cfft_exec_device_noalloc(ig_cfft_plan plan, const void *in, void *out, si
                 raise(IG_ETOOLARGE, "batch * length * element size exceeds the 64 MiB no-allocation scratch");
             scr = (char *)noalloc_scratch();
         }
+        require_aligned(in, (size_t)es, "input");
+        require_aligned(out, (size_t)es, "output");
         IODesc io = blank_io();
         io.in = (const char *)in;
         io.out = (char *)out;
@@ -1575,6 +1643,11 @@ int ig_rfft_exec_device(ig_rfft_plan plan, const void *in, void *out, size_t bat
     });
 }
 
+// Host-memory batches.  Batches longer than one chunk run as a pipeline of
+// line chunks over three streams, so that the host-to-device copy of one
+// chunk, the transform of the next and the device-to-host copy of a third
+// overlap (fully so for page-locked memory; copies from pageable memory may
+// serialise with the host); shorter batches take one copy each way.
 static int host_batch(bool real, size_t n, Arith a, void *c, size_t batch, size_t dist, int forward, double fct)
 {
     return guarded([&] {
@@ -1583,12 +1656,40 @@ static int host_batch(bool real, size_t n, Arith a, void *c, size_t batch, size_
         long long es = (real ? 1 : 2) * (long long)store_real_bytes(a);
         if (dist < n) raise(IG_EINVAL, "line distance smaller than the length");
         size_t bytes = ((batch - 1) * dist + n) * (size_t)es;
+        const Op op = real ? (forward ? OP_R2HC : OP_HC2R) : OP_C2C;
         std::lock_guard<std::mutex> lk(g_ws_mu);
-        void *d = g_ws.get(bytes);
-        ck(cudaMemcpy(d, c, bytes, cudaMemcpyHostToDevice), "H2D copy");
-        Lines ln = contiguous_lines(d, d, (long long)batch, (long long)dist, (long long)dist, es, es);
-        exec_op(a, real ? (forward ? OP_R2HC : OP_HC2R) : OP_C2C, (long long)n, ln, forward, fct, 0);
-        ck(cudaMemcpy(c, d, bytes, cudaMemcpyDeviceToHost), "D2H copy");
+        const size_t line_bytes = dist * (size_t)es;
+        const size_t chunk_lines = std::max<size_t>(1, pipe_chunk_bytes() / line_bytes);
+        if (batch <= chunk_lines) {
+            void *d = g_ws.get(bytes);
+            ck(cudaMemcpy(d, c, bytes, cudaMemcpyHostToDevice), "H2D copy");
+            Lines ln = contiguous_lines(d, d, (long long)batch, (long long)dist, (long long)dist, es, es);
+            exec_op(a, op, (long long)n, ln, forward, fct, 0);
+            ck(cudaMemcpy(c, d, bytes, cudaMemcpyDeviceToHost), "D2H copy");
+            return;
+        }
+        Pipe &pp = pipe_for_device();
+        const size_t cbytes = ((chunk_lines - 1) * dist + n) * (size_t)es;
+        void *dbuf[kPipe];
+        for (int i = 0; i < kPipe; ++i) dbuf[i] = pp.ws[i].get(cbytes);
+        try {
+            size_t i = 0;
+            for (size_t l0 = 0; l0 < batch; l0 += chunk_lines, ++i) {
+                const size_t nl = std::min(chunk_lines, batch - l0);
+                const size_t nb = ((nl - 1) * dist + n) * (size_t)es;
+                char *h = (char *)c + l0 * line_bytes;
+                cudaStream_t st = pp.st[i % kPipe];
+                void *d = dbuf[i % kPipe];
+                ck(cudaMemcpyAsync(d, h, nb, cudaMemcpyHostToDevice, st), "H2D copy");
+                Lines ln = contiguous_lines(d, d, (long long)nl, (long long)dist, (long long)dist, es, es);
+                exec_op(a, op, (long long)n, ln, forward, fct, st);
+                ck(cudaMemcpyAsync(h, d, nb, cudaMemcpyDeviceToHost, st), "D2H copy");
+            }
+            for (int k = 0; k < kPipe; ++k) ck(cudaStreamSynchronize(pp.st[k]), "pipeline");
+        } catch (...) {
+            for (int k = 0; k < kPipe; ++k) cudaStreamSynchronize(pp.st[k]);
+            throw;
+        }
     });
 }
 
@@ -1777,6 +1878,8 @@ int ig_r2c_adjoint_device(int dtype, size_t ndim, const size_t *shape_in, const 
     return guarded([&] {
         if (ndim >= 1 && shape_in && prod(ndim, shape_in) == 0) return;
         nd_checks(dtype, ndim, shape_in, stride_g, stride_x, naxes, axes, g, x, false);
+        require_aligned(g, 2 * store_real_bytes(arith_for(dtype)), "gradient");
+        require_aligned(x, store_real_bytes(arith_for(dtype)), "output");
         if (naxes == 0) return;
         Arith a = arith_for(dtype);
         cudaStream_t st = as_stream(stream);
@@ -1798,7 +1901,9 @@ int ig_r2c_adjoint_device(int dtype, size_t ndim, const size_t *shape_in, const 
             io.os = ln.es_out;
             io.nlines = ln.nlines;
             for (int i = 0; i < 3; ++i) { io.bn[i] = ln.bn[i]; io.bsi[i] = ln.bsi[i]; io.bso[i] = ln.bso[i]; }
-            io.in_kind = IN_C;
+            const long long sr = (long long)store_real_bytes(a);
+            io.in_kind = side_aligned(ln.in, ln.es_in, ln.bn, ln.bsi, 2 * sr) ? IN_C : IN_P;
+            io.ps_in = sr;
             io.out_kind = OUT_C;
             io.cnt_in = io.cnt_out = (int)sh[last];
             io.nreal = (long long)shape_in[last];
@@ -1831,6 +1936,8 @@ int ig_c2r_adjoint_device(int dtype, size_t ndim, const size_t *shape_out, const
     return guarded([&] {
         if (ndim >= 1 && shape_out && prod(ndim, shape_out) == 0) return;
         nd_checks(dtype, ndim, shape_out, stride_y, stride_g, naxes, axes, y, g, false);
+        require_aligned(y, store_real_bytes(arith_for(dtype)), "gradient");
+        require_aligned(g, 2 * store_real_bytes(arith_for(dtype)), "output");
         if (naxes == 0) return;
         Arith a = arith_for(dtype);
         cudaStream_t st = as_stream(stream);
@@ -1973,6 +2080,7 @@ int ig_fftconv_forward(ig_fftconv c, const void *x, const void *k, void *y, void
 {
     return guarded([&] {
         if (!c || !x || !k || !y) raise(IG_EINVAL, "null argument");
+        for (const void *p : {x, k, (const void *)y}) require_aligned(p, store_real_bytes(c->a), "array");
         cudaStream_t st = as_stream(stream);
         conv_spectra(*c, x, k, st);
         const long long n = c->P0 * (c->P1 / 2 + 1);
@@ -1991,6 +2099,7 @@ int ig_fftconv_backward(ig_fftconv c, const void *x, const void *k, const void *
 {
     return guarded([&] {
         if (!c || !x || !k || !gy) raise(IG_EINVAL, "null argument");
+        for (const void *p : {x, k, gy, (const void *)gx, (const void *)gk}) require_aligned(p, store_real_bytes(c->a), "array");
         cudaStream_t st = as_stream(stream);
         if (!c->have_spectra) conv_spectra(*c, x, k, st);
         const long long off = (c->K - 1) / 2;
@@ -2254,6 +2363,8 @@ int ig_multi_exec_device(ig_multi_plan plan, const void *in, void *out, void *st
 {
     return guarded([&] {
         if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        require_aligned(in, 2 * store_real_bytes(plan->a), "input");
+        require_aligned(out, 2 * store_real_bytes(plan->a), "output");
         multi_launch(*plan, in, out, as_stream(stream));
     });
 }
@@ -2265,6 +2376,8 @@ int ig_multi_exec_graph(ig_multi_plan plan, const void *in, void *out, void *str
 {
     return guarded([&] {
         if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        require_aligned(in, 2 * store_real_bytes(plan->a), "input");
+        require_aligned(out, 2 * store_real_bytes(plan->a), "output");
         cudaStream_t st = as_stream(stream);
         if (!st) raise(IG_EINVAL, "graph capture needs a created stream, not the default stream");
         if (!plan->gexec || plan->g_in != in || plan->g_out != out || plan->g_st != st) {
@@ -2301,6 +2414,8 @@ int ig_multi_exec_loop_device(ig_multi_plan plan, const void *in, void *out, voi
 {
     return guarded([&] {
         if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        require_aligned(in, 2 * store_real_bytes(plan->a), "input");
+        require_aligned(out, 2 * store_real_bytes(plan->a), "output");
         const long long es = 2 * (long long)store_real_bytes(plan->a);
         for (size_t i = 0; i < plan->len.size(); ++i) {
             Lines ln = contiguous_lines((const char *)in + plan->off[i] * es, (char *)out + plan->off[i] * es, 1,
