@@ -109,13 +109,16 @@ int ig_rfft_exec_device(ig_rfft_plan plan, const void *in, void *out, size_t bat
  * a static device array of 64 MiB (held by every GPU that loads the library)
  * instead of the engine's cached workspace.  Limit: batch * length * complex
  * element size <= 64 MiB for plans longer than one CTA; plans running
- * Bluestein over a multi-pass core are rejected (IG_EINVAL).  The first call
+ * Bluestein or Rader over a multi-pass core are rejected (IG_EINVAL), and so
+ * are pointers not aligned to the complex element size.  The first call
  * on each device looks the array up there and should precede any stream
  * capture.  Calls share the array; calls that overlap on the GPU race. */
 int ig_cfft_exec_device_noalloc(ig_cfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in,
                                 size_t dist_out, int forward, double fct, void *stream);
 
-/* Plan introspection: 1 when the plan runs Bluestein; the padded length. */
+/* Plan introspection: 1 when the plan runs Bluestein; the padded length.
+ * (Prime lengths whose predecessor is 13-smooth run Rader's algorithm and
+ * report 0.) */
 int ig_cfft_uses_bluestein(ig_cfft_plan plan, size_t *n2);
 int ig_rfft_uses_bluestein(ig_rfft_plan plan, size_t *n2);
 
@@ -153,8 +156,8 @@ int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff
  * `out` (device pointers; may be equal).  The plan groups equal lengths that
  * fit one CTA and runs them, with the column passes of longer four-step
  * lengths, through one persistent work-list launch; a second launch runs the
- * row passes; lengths needing Bluestein over a multi-pass core use the
- * general path.  ig_multi_exec_graph captures that sequence into a CUDA graph
+ * row passes; lengths needing Bluestein or Rader over a multi-pass core use
+ * the general path.  ig_multi_exec_graph captures that sequence into a CUDA graph
  * on its first call for given pointers and replays it afterwards;
  * ig_multi_exec_loop_device is the one-call-per-transform pattern, for
  * comparison.  The reference transforms one line per call
