@@ -598,7 +598,53 @@ typedef struct {
     const void *plan;
     size_t t, nt;
     int rc;
+    int type, cosine, ortho, r2c; /* kinds 3-5 */
 } io_nd_job;
+
+/* ------------------------------------------------------------------ */
+/* DCT / DST I-IV by their defining sums (long double), with the       */
+/* scaling steps of pocketfft_hdronly.h:2424-2650: fct on every output; */
+/* ortho: DCT-I scales x[0], x[n-1] by sqrt2 and y[0], y[n-1] by       */
+/* 1/sqrt2; types II (DCT and DST) scale y[0] by 1/sqrt2; types III    */
+/* scale x[0] by sqrt2; DST-I and types IV ignore ortho.                */
+/* ------------------------------------------------------------------ */
+static void io_dcst_line(int type, int cosine, int ortho, size_t n, const double *x, double *y, double fct)
+{
+    const long double PI = 3.14159265358979323846264338327950288L, R2 = 1.41421356237309504880168872420969808L;
+    for (size_t k = 0; k < n; ++k) {
+        long double acc = 0.0L;
+        for (size_t j = 0; j < n; ++j) {
+            long double xj = x[j];
+            long double t;
+            if (type == 1 && cosine) {
+                if (ortho && (j == 0 || j == n - 1)) xj *= R2;
+                long double w = (j == 0 || j == n - 1) ? 1.0L : 2.0L;
+                t = w * xj * cosl(PI * (long double)k * (long double)j / (long double)(n - 1));
+            } else if (type == 1) {
+                t = 2.0L * xj * sinl(PI * (long double)(k + 1) * (long double)(j + 1) / (long double)(n + 1));
+            } else if (type == 2) {
+                long double a = PI * (long double)(cosine ? k : k + 1) * (long double)(2 * j + 1) / (long double)(2 * n);
+                t = 2.0L * xj * (cosine ? cosl(a) : sinl(a));
+            } else if (type == 3 && cosine) {
+                if (ortho && j == 0) xj *= R2;
+                long double w = j == 0 ? 1.0L : 2.0L;
+                t = w * xj * cosl(PI * (long double)j * (long double)(2 * k + 1) / (long double)(2 * n));
+            } else if (type == 3) {
+                if (ortho && j == 0) xj *= R2;
+                long double w = j == n - 1 ? 1.0L : 2.0L;
+                t = w * xj * sinl(PI * (long double)(j + 1) * (long double)(2 * k + 1) / (long double)(2 * n));
+            } else {
+                long double a = PI * (long double)(2 * j + 1) * (long double)(2 * k + 1) / (long double)(4 * n);
+                t = 2.0L * xj * (cosine ? cosl(a) : sinl(a));
+            }
+            acc += t;
+        }
+        acc *= fct;
+        if (ortho && type == 1 && cosine && (k == 0 || k == n - 1)) acc /= R2;
+        if (ortho && type == 2 && k == 0) acc /= R2;
+        y[k] = (double)acc;
+    }
+}
 
 static void *io_nd_worker(void *arg)
 {
@@ -636,6 +682,34 @@ static void *io_nd_worker(void *arg)
                 d[0] = buf[i]; d[1] = sg * buf[i + 1];
             }
             if (i < len) { d = (double *)(po + (ptrdiff_t)ii * so); d[0] = buf[i]; d[1] = 0.0; }
+        } else if (j->kind == 3 || j->kind == 4) {
+            /* r2r_fftpack (ExecR2R, pocketfft_hdronly.h:3252-3270): the halfcomplex transform in
+               the direction `forward`; real2hermitian=false negates the odd imaginary slots
+               before a forward pass, real2hermitian=true after a backward pass.
+               separable Hartley (ExecHartley, copy_hartley, pocketfft_hdronly.h:3066-3106):
+               forward halfcomplex, then h[0]; h[i] +- h[i+1] into i1 / n - i1; h[n-1] for even n */
+            for (size_t m = 0; m < len; ++m) buf[m] = *(const double *)(pi + (ptrdiff_t)m * si);
+            int fwd = j->kind == 4 ? 1 : j->forward;
+            if (j->kind == 3 && !j->r2c && fwd) for (size_t i = 2; i < len; i += 2) buf[i] = -buf[i];
+            if (io_rplan_exec((const io_rplan *)j->plan, buf, fwd, j->fct)) j->rc = -1;
+            if (j->kind == 3) {
+                if (j->r2c && !fwd) for (size_t i = 2; i < len; i += 2) buf[i] = -buf[i];
+                for (size_t m = 0; m < len; ++m) *(double *)(po + (ptrdiff_t)m * so) = buf[m];
+            } else {
+                double *o = buf + len;  /* second half of the 2(len+1) buffer */
+                o[0] = buf[0];
+                size_t i = 1, i1 = 1, i2 = len - 1;
+                for (; i + 1 < len; i += 2, ++i1, --i2) {
+                    o[i1] = buf[i] + buf[i + 1];
+                    o[i2] = buf[i] - buf[i + 1];
+                }
+                if (i < len) o[i1] = buf[i];
+                for (size_t m = 0; m < len; ++m) *(double *)(po + (ptrdiff_t)m * so) = o[m];
+            }
+        } else if (j->kind == 5) {
+            for (size_t m = 0; m < len; ++m) buf[m] = *(const double *)(pi + (ptrdiff_t)m * si);
+            io_dcst_line(j->type, j->cosine, j->ortho, len, buf, buf + len, j->fct);
+            for (size_t m = 0; m < len; ++m) *(double *)(po + (ptrdiff_t)m * so) = buf[len + m];
         } else {
             /* general_c2r: halfcomplex from the input (conjugated when forward), then hc2r */
             double sg = j->forward ? -1.0 : 1.0;
@@ -654,12 +728,22 @@ static void *io_nd_worker(void *arg)
     return NULL;
 }
 
+static int io_run_axis_x(int kind, size_t ndim, const size_t *shape_lines, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                         size_t axis, size_t len, const void *in, void *out, int forward, double fct, int nthreads,
+                         int type, int cosine, int ortho, int r2c);
 static int io_run_axis(int kind, size_t ndim, const size_t *shape_lines, const ptrdiff_t *sin, const ptrdiff_t *sout,
                        size_t axis, size_t len, const void *in, void *out, int forward, double fct, int nthreads)
 {
+    return io_run_axis_x(kind, ndim, shape_lines, sin, sout, axis, len, in, out, forward, fct, nthreads, 0, 0, 0, 0);
+}
+static int io_run_axis_x(int kind, size_t ndim, const size_t *shape_lines, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                         size_t axis, size_t len, const void *in, void *out, int forward, double fct, int nthreads,
+                         int type, int cosine, int ortho, int r2c)
+{
     size_t nlines = 1;
     for (size_t d = 0; d < ndim; ++d) if (d != axis) nlines *= shape_lines[d];
-    const void *plan = (kind == 0) ? (const void *)io_make_cplan(len) : (const void *)io_make_rplan(len);
+    const void *plan = (kind == 0) ? (const void *)io_make_cplan(len)
+                     : (kind == 5) ? (const void *)"direct" : (const void *)io_make_rplan(len);
     if (!plan) return -1;
     if (nthreads < 1) nthreads = 1;
     if ((size_t)nthreads > nlines) nthreads = (int)(nlines ? nlines : 1);
@@ -674,6 +758,7 @@ static int io_run_axis(int kind, size_t ndim, const size_t *shape_lines, const p
             v.L.ndim = ndim; v.L.shape = shape_lines; v.L.sin = sin; v.L.sout = sout; v.L.axis = axis; v.L.nlines = nlines;
             v.kind = kind; v.len = len; v.in = (const char *)in; v.out = (char *)out;
             v.forward = forward; v.fct = fct; v.plan = plan; v.t = (size_t)t; v.nt = (size_t)nthreads;
+            v.type = type; v.cosine = cosine; v.ortho = ortho; v.r2c = r2c;
             jobs[t] = v;
         }
         for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, io_nd_worker, &jobs[t]);
@@ -683,7 +768,8 @@ static int io_run_axis(int kind, size_t ndim, const size_t *shape_lines, const p
     }
     free(jobs);
     free(th);
-    if (kind == 0) io_destroy_cplan((io_cplan *)plan); else io_destroy_rplan((io_rplan *)plan);
+    if (kind == 0) io_destroy_cplan((io_cplan *)plan);
+    else if (kind != 5) io_destroy_rplan((io_rplan *)plan);
     return rc;
 }
 
@@ -770,6 +856,89 @@ int io_c2r(size_t ndim, const size_t *shape_out, const ptrdiff_t *sin, const ptr
     rc = io_c2c(ndim, shape_in, sin, sinter, naxes - 1, axes, forward, in, tmp, 1.0, nthreads);
     if (!rc) rc = io_run_axis(2, ndim, shape_out, sinter, sout, last, shape_out[last], tmp, out, forward, fct, nthreads);
     free(tmp);
+    return rc;
+}
+
+/* real-to-real transforms over axes (pocketfft_hdronly.h:3284-3318, 3392-3445): every axis
+   in order, the first reads `in`, later ones read and write `out`, fct on the first axis */
+static int io_r2r_axes(int kind, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                       size_t naxes, const size_t *axes, const double *in, double *out, double fct, int nthreads,
+                       int forward, int type, int cosine, int ortho, int r2c)
+{
+    size_t tot = 1;
+    for (size_t d = 0; d < ndim; ++d) tot *= shape[d];
+    if (ndim >= 1 && tot == 0) return 0;
+    int rc = io_check_axes(ndim, naxes, axes);
+    if (rc) return rc;
+    if (in == out) for (size_t d = 0; d < ndim; ++d) if (sin[d] != sout[d]) return IO_ESTRIDE;
+    for (size_t a = 0; a < naxes; ++a) {
+        const void *src = a == 0 ? (const void *)in : (const void *)out;
+        const ptrdiff_t *ss = a == 0 ? sin : sout;
+        rc = io_run_axis_x(kind, ndim, shape, ss, sout, axes[a], shape[axes[a]], src, out, forward, a == 0 ? fct : 1.0,
+                           nthreads, type, cosine, ortho, r2c);
+        if (rc) return rc;
+    }
+    return 0;
+}
+/* DCT / DST types 1-4 (pocketfft::dct / dst); DCT-I needs length >= 2 */
+int io_dct(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
+           const size_t *axes, int type, const double *in, double *out, double fct, int ortho, int nthreads)
+{
+    if (type < 1 || type > 4) return -1;
+    for (size_t a = 0; a < naxes; ++a) if (axes[a] < ndim && type == 1 && shape[axes[a]] < 2) return -10;
+    return io_r2r_axes(5, ndim, shape, sin, sout, naxes, axes, in, out, fct, nthreads, 1, type, 1, ortho, 0);
+}
+int io_dst(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
+           const size_t *axes, int type, const double *in, double *out, double fct, int ortho, int nthreads)
+{
+    if (type < 1 || type > 4) return -1;
+    return io_r2r_axes(5, ndim, shape, sin, sout, naxes, axes, in, out, fct, nthreads, 1, type, 0, ortho, 0);
+}
+int io_r2r_fftpack(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
+                   const size_t *axes, int real2hermitian, int forward, const double *in, double *out, double fct,
+                   int nthreads)
+{
+    return io_r2r_axes(3, ndim, shape, sin, sout, naxes, axes, in, out, fct, nthreads, forward, 0, 0, 0,
+                       real2hermitian);
+}
+int io_r2r_separable_hartley(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                             size_t naxes, const size_t *axes, const double *in, double *out, double fct, int nthreads)
+{
+    return io_r2r_axes(4, ndim, shape, sin, sout, naxes, axes, in, out, fct, nthreads, 1, 0, 0, 0, 0);
+}
+/* genuine Hartley over axes (pocketfft_hdronly.h:3420-3445): Re + Im of the forward DFT over the
+   axes, taken here from the full complex transform of the real input */
+int io_r2r_genuine_hartley(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                           size_t naxes, const size_t *axes, const double *in, double *out, double fct, int nthreads)
+{
+    size_t tot = 1;
+    for (size_t d = 0; d < ndim; ++d) tot *= shape[d];
+    if (ndim >= 1 && tot == 0) return 0;
+    int rc = io_check_axes(ndim, naxes, axes);
+    if (rc) return rc;
+    if (naxes == 1) return io_r2r_separable_hartley(ndim, shape, sin, sout, naxes, axes, in, out, fct, nthreads);
+    double *c = (double *)malloc(sizeof(double) * 2 * tot);
+    if (!c) return -1;
+    ptrdiff_t cs[64];
+    cs[ndim - 1] = 16;
+    for (size_t d = ndim - 1; d-- > 0;) cs[d] = cs[d + 1] * (ptrdiff_t)shape[d + 1];
+    size_t idx[64] = { 0 };
+    for (size_t e = 0; e < tot; ++e) {
+        ptrdiff_t o = 0;
+        size_t r = e;
+        for (size_t d = ndim; d-- > 0;) { idx[d] = r % shape[d]; r /= shape[d]; o += (ptrdiff_t)idx[d] * sin[d]; }
+        c[2 * e] = *(const double *)((const char *)in + o);
+        c[2 * e + 1] = 0.0;
+    }
+    rc = io_c2c(ndim, shape, cs, cs, naxes, axes, 1, c, c, fct, nthreads);
+    if (!rc)
+        for (size_t e = 0; e < tot; ++e) {
+            ptrdiff_t o = 0;
+            size_t r = e;
+            for (size_t d = ndim; d-- > 0;) { idx[d] = r % shape[d]; r /= shape[d]; o += (ptrdiff_t)idx[d] * sout[d]; }
+            *(double *)((char *)out + o) = c[2 * e] + c[2 * e + 1];
+        }
+    free(c);
     return rc;
 }
 

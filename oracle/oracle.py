@@ -56,6 +56,12 @@ def lib():
         for nm in ("io_c2c", "io_r2c", "io_c2r"):
             getattr(L, nm).argtypes = [_sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,
                                        C.POINTER(_sz), C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int]
+        nd_head = [_sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz, C.POINTER(_sz)]
+        for nm in ("io_dct", "io_dst"):
+            getattr(L, nm).argtypes = nd_head + [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int]
+        L.io_r2r_fftpack.argtypes = nd_head + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int]
+        for nm in ("io_r2r_separable_hartley", "io_r2r_genuine_hartley"):
+            getattr(L, nm).argtypes = nd_head + [C.c_void_p, C.c_void_p, C.c_double, C.c_int]
         L.io_largest_prime_factor.argtypes = [_sz]
         L.io_largest_prime_factor.restype = _sz
         L.io_good_size.argtypes = [_sz]
@@ -99,6 +105,11 @@ def ref():
             getattr(L, f"ref_r2r_fftpack_{sfx}").argtypes = [_sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd),
                                                            _sz, C.POINTER(_sz), C.c_int, C.c_int, C.c_void_p,
                                                            C.c_void_p, C.c_double, _sz]
+            nd_head = [_sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz, C.POINTER(_sz)]
+            for nm in ("ref_dct", "ref_dst"):
+                getattr(L, f"{nm}_{sfx}").argtypes = nd_head + [C.c_int, C.c_void_p, C.c_void_p, C.c_double,
+                                                                C.c_int, _sz]
+            getattr(L, f"ref_hartley_{sfx}").argtypes = nd_head + [C.c_int, C.c_void_p, C.c_void_p, C.c_double, _sz]
         L.ref_last_error.restype = C.c_char_p
         _ref = L
     return _ref
@@ -171,6 +182,47 @@ def c2r(x, shape_out, axes, forward=False, fct=1.0, nthreads=None):
     rc = _nd(lib().io_c2r, tuple(shape_out), x, out, axes, forward, fct, nthreads or os.cpu_count() or 1)
     if rc:
         raise ValueError(f"oracle c2r status {rc}")
+    return out
+
+
+def _nd_head(shape, xin, xout, axes):
+    return [len(shape), _arr(_sz, shape), _arr(_pd, list(xin.strides)), _arr(_pd, list(xout.strides)), len(axes),
+            _arr(_sz, list(axes))]
+
+
+def dct(x, axes, type=2, fct=1.0, ortho=False, nthreads=None, sine=False):
+    """pocketfft::dct / dst (pocketfft_hdronly.h:3284-3318) by the defining sums."""
+    x = np.asarray(x, dtype=np.float64)
+    out = np.empty(x.shape, np.float64)
+    fn = lib().io_dst if sine else lib().io_dct
+    rc = fn(*_nd_head(x.shape, x, out, axes), int(type), x.ctypes.data, out.ctypes.data, float(fct), int(ortho),
+            nthreads or os.cpu_count() or 1)
+    if rc:
+        raise ValueError(f"oracle dct/dst status {rc}")
+    return out
+
+
+def dst(x, axes, type=2, fct=1.0, ortho=False, nthreads=None):
+    return dct(x, axes, type, fct, ortho, nthreads, sine=True)
+
+
+def r2r_fftpack(x, axes, real2hermitian=True, forward=True, fct=1.0, nthreads=None):
+    x = np.asarray(x, dtype=np.float64)
+    out = np.empty(x.shape, np.float64)
+    rc = lib().io_r2r_fftpack(*_nd_head(x.shape, x, out, axes), int(real2hermitian), int(forward), x.ctypes.data,
+                              out.ctypes.data, float(fct), nthreads or os.cpu_count() or 1)
+    if rc:
+        raise ValueError(f"oracle r2r_fftpack status {rc}")
+    return out
+
+
+def hartley(x, axes, fct=1.0, genuine=False, nthreads=None):
+    x = np.asarray(x, dtype=np.float64)
+    out = np.empty(x.shape, np.float64)
+    fn = lib().io_r2r_genuine_hartley if genuine else lib().io_r2r_separable_hartley
+    rc = fn(*_nd_head(x.shape, x, out, axes), x.ctypes.data, out.ctypes.data, float(fct), nthreads or os.cpu_count() or 1)
+    if rc:
+        raise ValueError(f"oracle hartley status {rc}")
     return out
 
 
@@ -276,6 +328,28 @@ def ref_r2r_fftpack(x, axes, real2hermitian=True, forward=True, fct=1.0, nthread
     out = np.empty(x.shape, x.dtype)
     return _ref_nd("ref_r2r_fftpack", x.dtype, x.shape, x, out, axes, forward, fct, nthreads,
                    extra=int(real2hermitian))
+
+
+def ref_dct(x, axes, type=2, fct=1.0, ortho=False, nthreads=1, sine=False):
+    out = np.empty(x.shape, x.dtype)
+    L = ref()
+    sfx = "f64" if x.dtype == np.float64 else "f32"
+    fn = getattr(L, f"ref_{'dst' if sine else 'dct'}_{sfx}")
+    rc = fn(*_nd_head(x.shape, x, out, axes), int(type), x.ctypes.data, out.ctypes.data, float(fct), int(ortho),
+            nthreads)
+    if rc:
+        raise ValueError(L.ref_last_error().decode())
+    return out
+
+
+def ref_hartley(x, axes, fct=1.0, genuine=False, nthreads=1):
+    out = np.empty(x.shape, x.dtype)
+    L = ref()
+    fn = getattr(L, f"ref_hartley_{'f64' if x.dtype == np.float64 else 'f32'}")
+    rc = fn(*_nd_head(x.shape, x, out, axes), int(genuine), x.ctypes.data, out.ctypes.data, float(fct), nthreads)
+    if rc:
+        raise ValueError(L.ref_last_error().decode())
+    return out
 
 
 def rel_l2(a, b):

@@ -80,7 +80,46 @@ const char *ref_last_error(void) { return g_err.c_str(); }
     });                                                                                            \
   }
 
+#define REF_WRAP2(T, SFX)                                                                         \
+  int ref_dct_##SFX(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,   \
+                    size_t naxes, const size_t *axes, int type, const void *in, void *out, double fct, \
+                    int ortho, size_t nthreads)                                                    \
+  {                                                                                                \
+    return guard([&] {                                                                             \
+      pocketfft::dct<T>(mk_shape(ndim, shape), mk_stride(ndim, sin), mk_stride(ndim, sout),        \
+                        mk_shape(naxes, axes), type, (const T *)in, (T *)out, (T)fct, ortho != 0,  \
+                        nthreads);                                                                 \
+    });                                                                                            \
+  }                                                                                                \
+  int ref_dst_##SFX(size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,   \
+                    size_t naxes, const size_t *axes, int type, const void *in, void *out, double fct, \
+                    int ortho, size_t nthreads)                                                    \
+  {                                                                                                \
+    return guard([&] {                                                                             \
+      pocketfft::dst<T>(mk_shape(ndim, shape), mk_stride(ndim, sin), mk_stride(ndim, sout),        \
+                        mk_shape(naxes, axes), type, (const T *)in, (T *)out, (T)fct, ortho != 0,  \
+                        nthreads);                                                                 \
+    });                                                                                            \
+  }                                                                                                \
+  int ref_hartley_##SFX(size_t ndim, const size_t *shape, const ptrdiff_t *sin,                    \
+                        const ptrdiff_t *sout, size_t naxes, const size_t *axes, int genuine,      \
+                        const void *in, void *out, double fct, size_t nthreads)                    \
+  {                                                                                                \
+    return guard([&] {                                                                             \
+      if (genuine)                                                                                 \
+        pocketfft::r2r_genuine_hartley<T>(mk_shape(ndim, shape), mk_stride(ndim, sin),             \
+                                          mk_stride(ndim, sout), mk_shape(naxes, axes),            \
+                                          (const T *)in, (T *)out, (T)fct, nthreads);              \
+      else                                                                                         \
+        pocketfft::r2r_separable_hartley<T>(mk_shape(ndim, shape), mk_stride(ndim, sin),           \
+                                            mk_stride(ndim, sout), mk_shape(naxes, axes),          \
+                                            (const T *)in, (T *)out, (T)fct, nthreads);            \
+    });                                                                                            \
+  }
+
 REF_WRAP(double, f64)
 REF_WRAP(float, f32)
+REF_WRAP2(double, f64)
+REF_WRAP2(float, f32)
 
 }  // extern "C"

@@ -56,6 +56,24 @@ def main():
     rr = rng.standard_normal((4, 30))
     d["r2r_in"] = rr
     d["r2r_fftpack"] = O.ref_r2r_fftpack(rr, [1], True, True, 1.0)
+    # real-to-real transforms of the C++ backend (DCTDesc.apply -> pocketfft::dct, and the
+    # bound dst / r2r_fftpack / Hartley templates)
+    for sine in (False, True):
+        nm = "dst" if sine else "dct"
+        for t in (1, 2, 3, 4):
+            for n in (2, 3, 8, 9, 16, 31):
+                x = rng.standard_normal((2, n))
+                d[f"{nm}{t}_in_{n}"] = x
+                d[f"{nm}{t}_{n}"] = O.ref_dct(x, [1], t, 0.5, False, sine=sine)
+                d[f"{nm}{t}_ortho_{n}"] = O.ref_dct(x, [1], t, 1.0, True, sine=sine)
+    xr = rng.standard_normal((4, 6, 5))
+    d["r2r3_in"] = xr
+    for h in (0, 1):
+        for f in (0, 1):
+            d[f"r2r_fftpack_{h}{f}"] = O.ref_r2r_fftpack(xr, [1, 2], bool(h), bool(f), 0.5)
+    d["dct2_axes02"] = O.ref_dct(xr, [0, 2], 2, 1.0, True)
+    d["hartley_sep_axes12"] = O.ref_hartley(xr, [1, 2], 0.5, genuine=False)
+    d["hartley_gen_axes012"] = O.ref_hartley(xr, [0, 1, 2], 0.5, genuine=True)
     np.savez_compressed(OUT, **d)
     print(OUT, os.path.getsize(OUT), "bytes")
 

@@ -55,6 +55,32 @@ def test_halfcomplex_equals_r2r_fftpack(oracle_lib, gold):
     assert oracle_lib.rel_l2(oracle_lib.rfft_hc(gold["r2r_in"]), gold["r2r_fftpack"]) < TOL
 
 
+def test_dct_dst_vs_reference(oracle_lib, gold):
+    for k in gold.files:
+        if "_in_" not in k or not (k.startswith("dct") or k.startswith("dst")):
+            continue
+        nm, n = k.split("_in_")
+        n = int(n)
+        t, sine = int(nm[3]), nm.startswith("dst")
+        x = gold[k]
+        got = oracle_lib.dct(x, [1], t, 0.5, False, sine=sine)
+        assert oracle_lib.rel_l2(got, gold[f"{nm}_{n}"]) < TOL, (nm, n)
+        got = oracle_lib.dct(x, [1], t, 1.0, True, sine=sine)
+        assert oracle_lib.rel_l2(got, gold[f"{nm}_ortho_{n}"]) < TOL, (nm, n, "ortho")
+    xr = gold["r2r3_in"]
+    assert oracle_lib.rel_l2(oracle_lib.dct(xr, [0, 2], 2, 1.0, True), gold["dct2_axes02"]) < TOL
+
+
+def test_r2r_and_hartley_vs_reference(oracle_lib, gold):
+    xr = gold["r2r3_in"]
+    for h in (0, 1):
+        for f in (0, 1):
+            got = oracle_lib.r2r_fftpack(xr, [1, 2], bool(h), bool(f), 0.5)
+            assert oracle_lib.rel_l2(got, gold[f"r2r_fftpack_{h}{f}"]) < TOL, (h, f)
+    assert oracle_lib.rel_l2(oracle_lib.hartley(xr, [1, 2], 0.5), gold["hartley_sep_axes12"]) < TOL
+    assert oracle_lib.rel_l2(oracle_lib.hartley(xr, [0, 1, 2], 0.5, genuine=True), gold["hartley_gen_axes012"]) < TOL
+
+
 def test_known_answers(oracle_lib):
     """tests/test_fft2.nim:7-15 and README.md:41,68,98."""
     x = np.arange(4.0)
