@@ -29,6 +29,8 @@ IG_F32 = 1
 _sz = C.c_size_t
 _pd = C.c_ssize_t
 _vp = C.c_void_p
+# dtype, ndim, shape, stride_in, stride_out, naxes, axes
+_ND_HEAD = [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz, C.POINTER(_sz)]
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -78,6 +80,15 @@ SIGNATURES = {
     "ig_multi_exec_device": (C.c_int, [_vp, _vp, _vp, _vp]),
     "ig_multi_exec_graph": (C.c_int, [_vp, _vp, _vp, _vp]),
     "ig_multi_exec_loop_device": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "ig_dct": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, C.c_int, _sz]),
+    "ig_dst": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, C.c_int, _sz]),
+    "ig_r2r_fftpack": (C.c_int, _ND_HEAD + [C.c_int, C.c_int, _vp, _vp, C.c_double, _sz]),
+    "ig_r2r_separable_hartley": (C.c_int, _ND_HEAD + [_vp, _vp, C.c_double, _sz]),
+    "ig_r2r_genuine_hartley": (C.c_int, _ND_HEAD + [_vp, _vp, C.c_double, _sz]),
+    "ig_dct_device": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, C.c_int, _vp]),
+    "ig_dst_device": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, C.c_int, _vp]),
+    "ig_r2r_fftpack_device": (C.c_int, _ND_HEAD + [C.c_int, C.c_int, _vp, _vp, C.c_double, _vp]),
+    "ig_r2r_hartley_device": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, _vp]),
     "ig_autotune": (C.c_int, [C.c_int, _sz, C.c_int, C.POINTER(C.c_double)]),
     "ig_autotune_save": (C.c_int, [C.c_char_p]),
     "ig_autotune_load": (C.c_int, [C.c_char_p]),

@@ -678,7 +678,7 @@ static IODesc blank_io()
 // scratch for the multi-pass paths: per (device, stream), grow-only
 // --------------------------------------------------------------------------
 struct Scratch {
-    std::unique_ptr<DevBuf> buf[6];
+    std::unique_ptr<DevBuf> buf[8];
     void *get(int i, size_t bytes)
     {
         if (!buf[i] || buf[i]->bytes < bytes) {
@@ -1823,6 +1823,29 @@ int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff
 }
 
 // host-memory N-d: copy the byte spans to the GPU, run, copy back
+// host arrays: copy the spans the strides cover to the device, run `fn` on
+// device pointers with the same strides, copy the output span back
+static void host_nd_run(size_t ndim, const std::vector<size_t> &shp_in, const std::vector<size_t> &shp_out,
+                        const ptrdiff_t *sin, const ptrdiff_t *sout, size_t e_in, size_t e_out, const void *in,
+                        void *out, const std::function<void(const void *, void *)> &fn)
+{
+    long long ilo, ihi, olo, ohi;
+    span_of(ndim, shp_in.data(), sin, e_in, ilo, ihi);
+    span_of(ndim, shp_out.data(), sout, e_out, olo, ohi);
+    bool inplace = in == out;
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    size_t ibytes = (size_t)(ihi - ilo), obytes = (size_t)(ohi - olo);
+    size_t oalign = inplace ? 0 : ((ibytes + 255) / 256) * 256;
+    char *d = (char *)g_ws.get(oalign + (inplace ? std::max(ibytes, obytes) : obytes));
+    char *din = d - ilo;
+    char *dout = inplace ? din : d + oalign - olo;
+    ck(cudaMemcpy(d, (const char *)in + ilo, ibytes, cudaMemcpyHostToDevice), "H2D copy");
+    if (!inplace && !dense(ndim, shp_out.data(), sout, e_out))
+        ck(cudaMemcpy(dout + olo, (char *)out + olo, obytes, cudaMemcpyHostToDevice), "H2D copy (output gaps)");
+    fn(din, dout);
+    ck(cudaMemcpy((char *)out + olo, dout + olo, obytes, cudaMemcpyDeviceToHost), "D2H copy");
+}
+
 static void host_nd(int kind, int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
                     size_t naxes, const size_t *axes, int forward, const void *in, void *out, double fct)
 {
@@ -1837,26 +1860,207 @@ static void host_nd(int kind, int dtype, size_t ndim, const size_t *shape, const
         e_out = sr;
         if (naxes) shp_in[axes[naxes - 1]] = shape[axes[naxes - 1]] / 2 + 1;
     }
-    long long ilo, ihi, olo, ohi;
-    span_of(ndim, shp_in.data(), sin, e_in, ilo, ihi);
-    span_of(ndim, shp_out.data(), sout, e_out, olo, ohi);
-    bool inplace = in == out;
-    std::lock_guard<std::mutex> lk(g_ws_mu);
-    size_t ibytes = (size_t)(ihi - ilo), obytes = (size_t)(ohi - olo);
-    size_t oalign = inplace ? 0 : ((ibytes + 255) / 256) * 256;
-    char *d = (char *)g_ws.get(oalign + (inplace ? std::max(ibytes, obytes) : obytes));
-    char *din = d - ilo;
-    char *dout = inplace ? din : d + oalign - olo;
-    ck(cudaMemcpy(d, (const char *)in + ilo, ibytes, cudaMemcpyHostToDevice), "H2D copy");
-    if (!inplace && !dense(ndim, shp_out.data(), sout, e_out))
-        ck(cudaMemcpy(dout + olo, (char *)out + olo, obytes, cudaMemcpyHostToDevice), "H2D copy (output gaps)");
-    if (kind == 0) nd_c2c_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
-    else if (kind == 1) nd_r2c_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
-    else nd_c2r_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
-    ck(cudaMemcpy((char *)out + olo, dout + olo, obytes, cudaMemcpyDeviceToHost), "D2H copy");
+    host_nd_run(ndim, shp_in, shp_out, sin, sout, e_in, e_out, in, out, [&](const void *din, void *dout) {
+        if (kind == 0) nd_c2c_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
+        else if (kind == 1) nd_r2c_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
+        else nd_c2r_device(a, ndim, shape, sin, sout, naxes, axes, forward, din, dout, fct, 0);
+    });
 }
 
-// ---- adjoints of the real transforms ------------------------------------------
+
+// ---- real-to-real transforms (pocketfft::dct / dst / r2r_fftpack / Hartley) ------
+// One axis at a time, like the reference's general_nd (pocketfft_hdronly.h:3012-3050):
+// the first axis reads the input, later axes read and write the output, fct on
+// the first axis only.  Per axis: pre-map into contiguous scratch lines, one
+// FFT of the scratch lines, post-map into the output lines (kernels k_r2r_pre /
+// k_r2r_post; the DCT / DST forms run a complex FFT of length 2N, 2(N-1) or 2(N+1)).
+struct R2RTables {
+    std::unique_ptr<DevBuf> tw1, tw2;
+};
+static std::map<std::tuple<int, int, long long>, std::shared_ptr<R2RTables>> g_r2r_tw;
+
+static std::shared_ptr<R2RTables> r2r_tables(Arith a, long long N)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto key = std::make_tuple(device_id(), (int)a, N);
+    auto it = g_r2r_tw.find(key);
+    if (it != g_r2r_tw.end()) return it->second;
+    auto t = std::make_shared<R2RTables>();
+    t->tw1.reset(new DevBuf((size_t)(N + 1) * slot_bytes(a)));
+    t->tw2.reset(new DevBuf((size_t)std::max<long long>(N, 1) * slot_bytes(a)));
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::r2r_tw(t->tw1->p, t->tw2->p, N)
+                  : a == A_DF  ? Launch<TagDF>::r2r_tw(t->tw1->p, t->tw2->p, N)
+                               : Launch<TagF64>::r2r_tw(t->tw1->p, t->tw2->p, N);
+    ck(e, "r2r tables");
+    count_launch();
+    ck(cudaDeviceSynchronize(), "r2r tables");
+    g_r2r_tw[key] = t;
+    return t;
+}
+
+static void launch_r2r(Arith a, bool pre, const IODesc &io_in, const R2RDesc &d, cudaStream_t st)
+{
+    IODesc io = io_in;
+    set_line_divs(io);
+    cudaError_t e;
+    if (pre)
+        e = a == A_F32 ? Launch<TagF32>::r2r_pre(io, d, st)
+          : a == A_DF  ? Launch<TagDF>::r2r_pre(io, d, st)
+                       : Launch<TagF64>::r2r_pre(io, d, st);
+    else
+        e = a == A_F32 ? Launch<TagF32>::r2r_post(io, d, st)
+          : a == A_DF  ? Launch<TagDF>::r2r_post(io, d, st)
+                       : Launch<TagF64>::r2r_post(io, d, st);
+    ck(e, "r2r map");
+    count_launch();
+}
+
+// one axis over the lines `ln` (length N along the axis).  mode: R2RMode;
+// COPY runs the halfcomplex FFT in direction fwd with the negations the
+// reference's ExecR2R applies (neg_pre before, neg_post after).
+static void r2r_axis(Arith a, const Lines &ln, long long N, int mode, int ortho, int neg_pre, int neg_post, int fwd,
+                     double fct, cudaStream_t st)
+{
+    if (ln.nlines <= 0 || N <= 0) return;
+    const long long sr = (long long)store_real_bytes(a), ES = 2 * sr, nl = ln.nlines;
+    if (!side_aligned(ln.in, ln.es_in, ln.bn, ln.bsi, sr) || !side_aligned(ln.out, ln.es_out, ln.bn, ln.bso, sr))
+        raise(IG_EINVAL, "data pointer or stride not aligned to the element size");
+    const bool cplx = mode <= R2R_DST4;
+    R2RDesc d{};
+    d.mode = mode;
+    d.ortho = ortho;
+    d.N = N;
+    d.L2 = mode == R2R_DCT1 ? 2 * (N - 1) : mode == R2R_DST1 ? 2 * (N + 1) : cplx ? 2 * N : N;
+    d.fct = fct;
+    std::shared_ptr<R2RTables> tb;
+    if (cplx && mode != R2R_DCT1 && mode != R2R_DST1) {
+        tb = r2r_tables(a, N);
+        d.tw1 = tb->tw1->p;
+        d.tw2 = tb->tw2->p;
+    }
+    char *A = (char *)scratch_for(st).get(6, (size_t)(nl * d.L2 * (cplx ? ES : sr)));
+    d.scr = A;
+    IODesc io = blank_io();
+    io.in = ln.in;
+    io.out = ln.out;
+    io.is = ln.es_in;
+    io.os = ln.es_out;
+    io.nlines = nl;
+    for (int i = 0; i < 3; ++i) {
+        io.bn[i] = ln.bn[i];
+        io.bsi[i] = ln.bsi[i];
+        io.bso[i] = ln.bso[i];
+    }
+    d.neg_even = neg_pre;
+    launch_r2r(a, true, io, d, st);
+    if (cplx) {
+        Lines s = contiguous_lines(A, A, nl, d.L2, d.L2, ES, ES);
+        exec_op(a, OP_C2C, d.L2, s, 1, 1.0, st);
+    } else {
+        Lines s = contiguous_lines(A, A, nl, N, N, sr, sr);
+        exec_op(a, fwd ? OP_R2HC : OP_HC2R, N, s, fwd, fct, st);
+    }
+    d.neg_even = neg_post;
+    launch_r2r(a, false, io, d, st);
+}
+
+static void r2r_nd_device(Arith a, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                          size_t naxes, const size_t *axes, const void *in, void *out, double fct, cudaStream_t st,
+                          int mode, int ortho, int neg_pre, int neg_post, int fwd)
+{
+    for (size_t i = 0; i < naxes; ++i) {
+        const size_t ax = axes[i];
+        const long long N = (long long)shape[ax];
+        if (mode == R2R_DCT1 && N < 2) raise(IG_EZERO_LEN, "zero-length FFT requested");
+        for_lines(ndim, shape, i == 0 ? sin : sout, sout, ax, i == 0 ? (const char *)in : (const char *)out,
+                  (char *)out, [&](const Lines &ln) {
+                      r2r_axis(a, ln, N, mode, ortho, neg_pre, neg_post, fwd, i == 0 ? fct : 1.0, st);
+                  });
+    }
+}
+
+static void hartley_gen_device(Arith a, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                               size_t naxes, const size_t *axes, const void *in, void *out, double fct, cudaStream_t st)
+{
+    if (naxes == 1) {
+        r2r_nd_device(a, ndim, shape, sin, sout, naxes, axes, in, out, fct, st, R2R_HARTLEY, 0, 0, 0, 1);
+        return;
+    }
+    if (ndim > 8) raise(IG_ENDIM, "genuine Hartley over more than 8 dimensions");
+    const size_t last = axes[naxes - 1];
+    std::vector<size_t> tshp(shape, shape + ndim);
+    tshp[last] = shape[last] / 2 + 1;
+    const long long ES = 2 * (long long)store_real_bytes(a);
+    std::vector<ptrdiff_t> tst(ndim);
+    tst[ndim - 1] = (ptrdiff_t)ES;
+    for (size_t d = ndim - 1; d-- > 0;) tst[d] = tst[d + 1] * (ptrdiff_t)tshp[d + 1];
+    DevBuf tmp(prod(ndim, tshp.data()) * (size_t)ES);
+    nd_r2c_device(a, ndim, shape, sin, tst.data(), naxes, axes, 1, in, tmp.p, fct, st);
+    HartleyDesc h{};
+    h.ndim = (int)ndim;
+    h.total = (long long)prod(ndim, tshp.data());
+    for (size_t d = 0; d < ndim; ++d) {
+        h.tshp[d] = (long long)tshp[d];
+        h.shape[d] = (long long)shape[d];
+        h.sout[d] = (long long)sout[d];
+        h.rev[d] = 0;
+    }
+    for (size_t i = 0; i < naxes; ++i) h.rev[axes[i]] = 1;
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::hartley_fold(tmp.p, out, h, st)
+                  : a == A_DF  ? Launch<TagDF>::hartley_fold(tmp.p, out, h, st)
+                               : Launch<TagF64>::hartley_fold(tmp.p, out, h, st);
+    ck(e, "Hartley fold");
+    count_launch();
+    ck(cudaStreamSynchronize(st), "Hartley fold");  // tmp is released on return
+}
+
+enum { R2R_OP_DCT = 0, R2R_OP_DST, R2R_OP_FFTPACK, R2R_OP_HSEP, R2R_OP_HGEN };
+static void r2r_dispatch(int op, Arith a, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                         size_t naxes, const size_t *axes, int type, int ortho, int r2h, int fwd, const void *in,
+                         void *out, double fct, cudaStream_t st)
+{
+    switch (op) {
+    case R2R_OP_DCT:
+    case R2R_OP_DST:
+        r2r_nd_device(a, ndim, shape, sin, sout, naxes, axes, in, out, fct, st,
+                      (op == R2R_OP_DST ? R2R_DST1 : R2R_DCT1) + type - 1, ortho, 0, 0, 1);
+        break;
+    case R2R_OP_FFTPACK:
+        // ExecR2R (pocketfft_hdronly.h:3252-3270)
+        r2r_nd_device(a, ndim, shape, sin, sout, naxes, axes, in, out, fct, st, R2R_COPY, 0, !r2h && fwd,
+                      r2h && !fwd, fwd);
+        break;
+    case R2R_OP_HSEP:
+        r2r_nd_device(a, ndim, shape, sin, sout, naxes, axes, in, out, fct, st, R2R_HARTLEY, 0, 0, 0, 1);
+        break;
+    default: hartley_gen_device(a, ndim, shape, sin, sout, naxes, axes, in, out, fct, st); break;
+    }
+}
+
+static int r2r_entry(int op, int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                     size_t naxes, const size_t *axes, int type, int ortho, int r2h, int fwd, const void *in,
+                     void *out, double fct, bool host, void *stream)
+{
+    return guarded([&] {
+        if ((op == R2R_OP_DCT || op == R2R_OP_DST) && (type < 1 || type > 4))
+            raise(IG_EINVAL, op == R2R_OP_DCT ? "invalid DCT type" : "invalid DST type");
+        if (ndim >= 1 && shape && prod(ndim, shape) == 0) return;
+        nd_checks(dtype, ndim, shape, sin, sout, naxes, axes, in, out, true);
+        Arith a = arith_for(dtype);
+        if (!host) {
+            r2r_dispatch(op, a, ndim, shape, sin, sout, naxes, axes, type, ortho, r2h, fwd, in, out, fct,
+                         as_stream(stream));
+            return;
+        }
+        const size_t sr = store_real_bytes(a);
+        std::vector<size_t> shp(shape, shape + ndim);
+        host_nd_run(ndim, shp, shp, sin, sout, sr, sr, in, out, [&](const void *din, void *dout) {
+            r2r_dispatch(op, a, ndim, shape, sin, sout, naxes, axes, type, ortho, r2h, fwd, din, dout, fct, 0);
+        });
+    });
+}
+
+// ---- adjoints of the real transforms ------------------------------------------// ---- adjoints of the real transforms ------------------------------------------
 static void launch_half_weight(Arith a, void *x, long long lines, long long n_half, long long nreal, double w,
                                int drop_im, cudaStream_t st)
 {
@@ -2638,6 +2842,71 @@ int ig_c2r(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *sin
         nd_checks(dtype, ndim, shape_out, sin, sout, naxes, axes, in, out, false);
         host_nd(2, dtype, ndim, shape_out, sin, sout, naxes, axes, forward, in, out, fct);
     });
+}
+
+// ---- real-to-real transforms ----
+int ig_dct(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
+           const size_t *axes, int type, const void *in, void *out, double fct, int ortho, size_t nthreads)
+{
+    (void)nthreads;
+    return r2r_entry(R2R_OP_DCT, dtype, ndim, shape, sin, sout, naxes, axes, type, ortho, 0, 1, in, out, fct, true,
+                     nullptr);
+}
+int ig_dst(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout, size_t naxes,
+           const size_t *axes, int type, const void *in, void *out, double fct, int ortho, size_t nthreads)
+{
+    (void)nthreads;
+    return r2r_entry(R2R_OP_DST, dtype, ndim, shape, sin, sout, naxes, axes, type, ortho, 0, 1, in, out, fct, true,
+                     nullptr);
+}
+int ig_r2r_fftpack(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                   size_t naxes, const size_t *axes, int real2hermitian, int forward, const void *in, void *out,
+                   double fct, size_t nthreads)
+{
+    (void)nthreads;
+    return r2r_entry(R2R_OP_FFTPACK, dtype, ndim, shape, sin, sout, naxes, axes, 0, 0, real2hermitian, forward, in,
+                     out, fct, true, nullptr);
+}
+int ig_r2r_separable_hartley(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin,
+                             const ptrdiff_t *sout, size_t naxes, const size_t *axes, const void *in, void *out,
+                             double fct, size_t nthreads)
+{
+    (void)nthreads;
+    return r2r_entry(R2R_OP_HSEP, dtype, ndim, shape, sin, sout, naxes, axes, 0, 0, 0, 1, in, out, fct, true, nullptr);
+}
+int ig_r2r_genuine_hartley(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                           size_t naxes, const size_t *axes, const void *in, void *out, double fct, size_t nthreads)
+{
+    (void)nthreads;
+    return r2r_entry(R2R_OP_HGEN, dtype, ndim, shape, sin, sout, naxes, axes, 0, 0, 0, 1, in, out, fct, true, nullptr);
+}
+int ig_dct_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                  size_t naxes, const size_t *axes, int type, const void *in, void *out, double fct, int ortho,
+                  void *stream)
+{
+    return r2r_entry(R2R_OP_DCT, dtype, ndim, shape, sin, sout, naxes, axes, type, ortho, 0, 1, in, out, fct, false,
+                     stream);
+}
+int ig_dst_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                  size_t naxes, const size_t *axes, int type, const void *in, void *out, double fct, int ortho,
+                  void *stream)
+{
+    return r2r_entry(R2R_OP_DST, dtype, ndim, shape, sin, sout, naxes, axes, type, ortho, 0, 1, in, out, fct, false,
+                     stream);
+}
+int ig_r2r_fftpack_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                          size_t naxes, const size_t *axes, int real2hermitian, int forward, const void *in, void *out,
+                          double fct, void *stream)
+{
+    return r2r_entry(R2R_OP_FFTPACK, dtype, ndim, shape, sin, sout, naxes, axes, 0, 0, real2hermitian, forward, in,
+                     out, fct, false, stream);
+}
+int ig_r2r_hartley_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *sin, const ptrdiff_t *sout,
+                          size_t naxes, const size_t *axes, int genuine, const void *in, void *out, double fct,
+                          void *stream)
+{
+    return r2r_entry(genuine ? R2R_OP_HGEN : R2R_OP_HSEP, dtype, ndim, shape, sin, sout, naxes, axes, 0, 0, 0, 1, in,
+                     out, fct, false, stream);
 }
 
 }  // extern "C"

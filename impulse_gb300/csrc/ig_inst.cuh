@@ -149,5 +149,30 @@ cudaError_t Launch<Tag>::half_weight(void *x, long long lines, long long n_half,
     k_half_weight<T><<<map_grid(lines * n_half), 256, 0, st>>>((S2 *)x, lines, n_half, nreal, (S)w, drop_im);
     return cudaGetLastError();
 }
+template <class Tag> cudaError_t Launch<Tag>::r2r_pre(const IODesc &io, const R2RDesc &d, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_r2r_pre<T><<<map_grid(io.nlines * d.L2), 256, 0, st>>>(io, d);
+    return cudaGetLastError();
+}
+template <class Tag> cudaError_t Launch<Tag>::r2r_post(const IODesc &io, const R2RDesc &d, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_r2r_post<T><<<map_grid(io.nlines * d.N), 256, 0, st>>>(io, d);
+    return cudaGetLastError();
+}
+template <class Tag> cudaError_t Launch<Tag>::r2r_tw(void *tw1, void *tw2, long long N)
+{
+    using T = typename TagType<Tag>::T;
+    k_gen_r2r_tw<T><<<(unsigned)((N + 256) / 256), 256>>>((cx<T> *)tw1, (cx<T> *)tw2, N);
+    return cudaGetLastError();
+}
+template <class Tag>
+cudaError_t Launch<Tag>::hartley_fold(const void *X, void *out, const HartleyDesc &h, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    k_hartley_fold<T><<<map_grid(h.total), 256, 0, st>>>((const typename Traits<T>::S2 *)X, (char *)out, h);
+    return cudaGetLastError();
+}
 
 }  // namespace ig

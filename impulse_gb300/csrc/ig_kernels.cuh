@@ -1238,6 +1238,173 @@ __global__ void k_scatter_pair(const __grid_constant__ IODesc io, const __grid_c
 }
 
 // ---------------------------------------------------------------------------
+// real-to-real transforms (DCT / DST I-IV, r2r_fftpack, Hartley)
+// ---------------------------------------------------------------------------
+// With N the length along the axis and U the forward FFT of the scratch line:
+//   DCT-I  (L2 = 2(N-1)): u = even extension of x;            y[k] = Re U[k]
+//   DST-I  (L2 = 2(N+1)): u = (0, x, 0, -reversed x);          y[k] = -Im U[k+1]
+//   DCT-II / DST-II (L2 = 2N): u = x, zero padded;             y[k] = 2 Re(w^k U[k]) / -2 Im(w^(k+1) U[k+1])
+//   DCT-III: u[m] = c_m x[m] w^m (c_0 = 1, else 2);            y[k] = Re U[k]
+//   DST-III: u[m] = c_m x[m-1] w^m, 1 <= m <= N (c_N = 1, else 2); y[k] = -Im U[k]
+//   DCT-IV / DST-IV: u[m] = x[m] w^m;                          y[k] = 2 Re / -2 Im(v^(2k+1) U[k])
+// with w = exp(-i pi / 2N), v = exp(-i pi / 4N), times fct; ortho scales as
+// the reference's steps do (DCT-I: x[0], x[N-1] by sqrt 2 and y[0], y[N-1] by
+// 1/sqrt 2; DCT-II, DST-II: y[0] by 1/sqrt 2; DCT-III, DST-III: x[0] by sqrt 2).
+constexpr double kSqrt2 = 1.4142135623730950488016887;
+template <class T>
+__global__ void k_r2r_pre(const __grid_constant__ IODesc io, const __grid_constant__ R2RDesc d)
+{
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    const long long total = io.nlines * d.L2, N = d.N;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long l = idx / d.L2, m = idx - l * d.L2;
+        const char *base = io.in + line_off(io, l, false);
+        auto X = [&](long long j) { return (double)*reinterpret_cast<const S *>(base + j * io.is); };
+        if (d.mode == R2R_COPY || d.mode == R2R_HARTLEY) {
+            double v = X(m);
+            if (d.neg_even && m >= 2 && (m & 1) == 0) v = -v;
+            reinterpret_cast<S *>(d.scr)[idx] = (S)v;
+            continue;
+        }
+        double v = 0.0, w = 1.0;
+        bool tw = false;
+        switch (d.mode) {
+        case R2R_DCT1: {
+            const long long src = m <= N - 1 ? m : d.L2 - m;
+            v = X(src);
+            if (d.ortho && (src == 0 || src == N - 1)) w = kSqrt2;
+            break;
+        }
+        case R2R_DST1:
+            if (m >= 1 && m <= N) v = X(m - 1);
+            else if (m >= N + 2) v = -X(d.L2 - 1 - m);
+            break;
+        case R2R_DCT2:
+        case R2R_DST2:
+            if (m < N) v = X(m);
+            break;
+        case R2R_DCT3:
+            if (m < N) {
+                v = X(m);
+                w = m == 0 ? (d.ortho ? kSqrt2 : 1.0) : 2.0;
+                tw = true;
+            }
+            break;
+        case R2R_DST3:
+            if (m >= 1 && m <= N) {
+                v = X(m - 1);
+                w = m == N ? 1.0 : 2.0;
+                if (d.ortho && m == 1) w *= kSqrt2;
+                tw = true;
+            }
+            break;
+        default:  // types IV
+            if (m < N) {
+                v = X(m);
+                tw = true;
+            }
+            break;
+        }
+        v *= w;
+        S2 o;
+        if (!tw) {
+            o.x = (S)v;
+            o.y = S(0);
+        } else {
+            Loc<T> lc;
+            lc.fit(v, 0.0);
+            const cx<T> z = cmul(lc.in(v, 0.0), reinterpret_cast<const cx<T> *>(d.tw1)[m]);
+            o.x = (S)lc.out(z.r);
+            o.y = (S)lc.out(z.i);
+        }
+        reinterpret_cast<S2 *>(d.scr)[idx] = o;
+    }
+}
+
+template <class T>
+__global__ void k_r2r_post(const __grid_constant__ IODesc io, const __grid_constant__ R2RDesc d)
+{
+    using S = typename Traits<T>::S;
+    using S2 = typename Traits<T>::S2;
+    const long long N = d.N, total = io.nlines * N;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long l = idx / N, k = idx - l * N;
+        S *dst = reinterpret_cast<S *>(io.out + line_off(io, l, true) + k * io.os);
+        if (d.mode == R2R_COPY) {
+            double v = reinterpret_cast<const S *>(d.scr)[l * d.L2 + k];
+            if (d.neg_even && k >= 2 && (k & 1) == 0) v = -v;
+            *dst = (S)v;
+            continue;
+        }
+        if (d.mode == R2R_HARTLEY) {
+            // h[0]; h[2j-1] +- h[2j] to j and N - j; h[N-1] to N/2 for even N
+            const S *h = reinterpret_cast<const S *>(d.scr) + l * d.L2;
+            S v;
+            if (k == 0) v = h[0];
+            else if (2 * k < N) v = h[2 * k - 1] + h[2 * k];
+            else if (2 * k == N) v = h[N - 1];
+            else v = h[2 * (N - k) - 1] - h[2 * (N - k)];
+            *dst = v;
+            continue;
+        }
+        const S2 *U = reinterpret_cast<const S2 *>(d.scr) + l * d.L2;
+        double y, w = d.fct;
+        const cx<T> *tw1 = reinterpret_cast<const cx<T> *>(d.tw1);
+        const cx<T> *tw2 = reinterpret_cast<const cx<T> *>(d.tw2);
+        auto twisted = [&](S2 a, cx<T> t, bool re) {
+            Loc<T> lc;
+            lc.fit(a.x, a.y);
+            const cx<T> z = cmul(lc.in(a.x, a.y), t);
+            return re ? lc.out(z.r) : lc.out(z.i);
+        };
+        switch (d.mode) {
+        case R2R_DCT1:
+            y = U[k].x;
+            if (d.ortho && (k == 0 || k == N - 1)) w /= kSqrt2;
+            break;
+        case R2R_DST1: y = -(double)U[k + 1].y; break;
+        case R2R_DCT2:
+            y = 2.0 * twisted(U[k], tw1[k], true);
+            if (d.ortho && k == 0) w /= kSqrt2;
+            break;
+        case R2R_DST2:
+            y = -2.0 * twisted(U[k + 1], tw1[k + 1], false);
+            if (d.ortho && k == 0) w /= kSqrt2;
+            break;
+        case R2R_DCT3: y = U[k].x; break;
+        case R2R_DST3: y = -(double)U[k].y; break;
+        case R2R_DCT4: y = 2.0 * twisted(U[k], tw2[k], true); break;
+        default: y = -2.0 * twisted(U[k], tw2[k], false); break;
+        }
+        *dst = (S)(y * w);
+    }
+}
+
+// genuine Hartley fold of an r2c half spectrum (contiguous, shape tshp)
+template <class T>
+__global__ void k_hartley_fold(const typename Traits<T>::S2 *__restrict__ X, char *out, const __grid_constant__ HartleyDesc h)
+{
+    using S = typename Traits<T>::S;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < h.total;
+         e += (long long)gridDim.x * blockDim.x) {
+        long long r = e, o = 0, ro = 0;
+        for (int dd = h.ndim - 1; dd >= 0; --dd) {
+            const long long i = r % h.tshp[dd];
+            r /= h.tshp[dd];
+            const long long ri = (h.rev[dd] && i) ? h.shape[dd] - i : i;
+            o += i * h.sout[dd];
+            ro += ri * h.sout[dd];
+        }
+        const typename Traits<T>::S2 v = X[e];
+        *reinterpret_cast<S *>(out + o) = v.x + v.y;
+        *reinterpret_cast<S *>(out + ro) = v.x - v.y;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FFT-convolution helpers (elementwise; storage type S, arithmetic T)
 // ---------------------------------------------------------------------------
 
@@ -1388,6 +1555,22 @@ template <class T> __global__ void k_gen_stage_tw(typename Bfly<T>::W *tw, int R
         tw[e] = ptw{pk(w.r.h, w.r.h), pk(-w.i.h, w.i.h), pk(w.r.l, w.r.l), pk(-w.i.l, w.i.l)};
     } else {
         tw[e] = to_arith<T>(v);
+    }
+}
+
+// r2r twiddles: tw1[m] = exp(-2 pi i m / 4N) (m <= N), tw2[k] = exp(-2 pi i (2k+1) / 8N) (k < N)
+template <class T> __global__ void k_gen_r2r_tw(cx<T> *tw1, cx<T> *tw2, long long N)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j <= N) {
+        double2 v = exp2pi_frac((unsigned long long)j, 4ull * (unsigned long long)N);
+        v.y = -v.y;
+        tw1[j] = to_arith<T>(v);
+    }
+    if (j < N) {
+        double2 v = exp2pi_frac(2ull * (unsigned long long)j + 1ull, 8ull * (unsigned long long)N);
+        v.y = -v.y;
+        tw2[j] = to_arith<T>(v);
     }
 }
 

@@ -38,6 +38,11 @@ template <class Tag> struct Launch {
                                 int mode, cudaStream_t st);
     static cudaError_t half_weight(void *x, long long lines, long long n_half, long long nreal, double w,
                                    int drop_im, cudaStream_t st);
+    // real-to-real transforms
+    static cudaError_t r2r_pre(const IODesc &io, const R2RDesc &d, cudaStream_t st);
+    static cudaError_t r2r_post(const IODesc &io, const R2RDesc &d, cudaStream_t st);
+    static cudaError_t r2r_tw(void *tw1, void *tw2, long long N);
+    static cudaError_t hartley_fold(const void *X, void *out, const HartleyDesc &h, cudaStream_t st);
 };
 
 // FP64 helpers for Bluestein tables (built in ig_inst_df.cu)

@@ -141,6 +141,37 @@ struct MapDesc {
 };
 
 
+// real-to-real transforms along one axis (pocketfft's dct / dst / r2r_fftpack /
+// Hartley): a pre-map from the user's lines into contiguous scratch lines, one
+// FFT of the scratch lines, a post-map back to the user's lines
+enum R2RMode {
+    R2R_DCT1 = 1, R2R_DCT2, R2R_DCT3, R2R_DCT4,   // complex scratch of length L2, FFT forward
+    R2R_DST1 = 5, R2R_DST2, R2R_DST3, R2R_DST4,
+    R2R_COPY = 9,     // real scratch; halfcomplex FFT; elements 2, 4, ... negated when neg_even
+    R2R_HARTLEY = 10, // real scratch; forward halfcomplex FFT; post-map h[i] +- h[i+1]
+};
+struct R2RDesc {
+    int mode;
+    int ortho;
+    int neg_even;       // R2R_COPY: negate elements 2, 4, ... in this map
+    long long N;        // length along the axis
+    long long L2;       // scratch elements per line
+    char *scr;          // scratch lines (storage type), line l at l * L2
+    const void *tw1;    // cx<T> exp(-2 pi i m / 4N), m <= N
+    const void *tw2;    // cx<T> exp(-2 pi i (2k + 1) / 8N), k < N
+    double fct;         // DCT / DST: scale applied by the post-map
+};
+// genuine Hartley over several axes: the r2c half spectrum (contiguous, shape
+// `tshp`) folded into the real output: out[i] = re + im, out[-i] = re - im
+struct HartleyDesc {
+    int ndim;
+    long long tshp[8];
+    long long shape[8];
+    long long sout[8];  // bytes
+    int rev[8];         // 1: transformed axis (index reversed for the mirror)
+    long long total;
+};
+
 enum Arith { A_F32 = 0, A_DF = 1, A_F64 = 2 };
 
 }  // namespace ig

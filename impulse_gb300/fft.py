@@ -298,8 +298,11 @@ def _nd_call(fn, dtype, shape, sin, sout, axes, forward, pin, pout, fct, nthread
     L.check(rc)
 
 
-def apply(fft: FFTDesc, descOut: DataDesc, descIn: DataDesc):
-    """pocketfft.nim:235-277: compile-time dispatch to c2c / r2c / c2r."""
+def apply(fft, descOut: DataDesc, descIn: DataDesc):
+    """pocketfft.nim:235-277: compile-time dispatch to c2c / r2c / c2r; the
+    DCTDesc overload (pocketfft.nim:279-295) goes to pocketfft::dct."""
+    if isinstance(fft, DCTDesc):
+        return apply_dct(fft, descOut, descIn)
     lib = L.load()
     dt = _dtype_code(descIn.buf)
     if descIn.complex and descOut.complex:
@@ -318,6 +321,64 @@ def apply(fft: FFTDesc, descOut: DataDesc, descIn: DataDesc):
 
 
 # ---- raw C-ABI helpers on numpy arrays (used by tests and the benchmark) ----
+
+class DCTDesc:
+    """pocketfft.nim:151-156, 217-233: axes, DCT type (default 2), ortho, scalingFactor, nthreads."""
+
+    def __init__(self, axes, dctType: int = 2, ortho: bool = False, scalingFactor: float = 1.0, nthreads: int = 1):
+        self.axes = [int(a) for a in axes]
+        if not 1 <= int(dctType) <= 4:
+            raise ValueError("dctType must be in 1..4")
+        self.dctType = int(dctType)
+        self.ortho = bool(ortho)
+        self.scalingFactor = float(scalingFactor)
+        self.nthreads = int(nthreads)
+
+
+def apply_dct(dct: DCTDesc, descOut: DataDesc, descIn: DataDesc):
+    """The DCTDesc overload of apply (pocketfft.nim:279-295): pocketfft::dct over dct.axes."""
+    head = _nd_head(_dtype_code(descIn.buf), descIn.shape, descIn.stride, descOut.stride, dct.axes)
+    L.check(L.load().ig_dct(*head, dct.dctType, descIn.buf.ctypes.data, descOut.buf.ctypes.data,
+                            dct.scalingFactor, int(dct.ortho), dct.nthreads))
+
+
+def _nd_head(dtype, shape, sin, sout, axes):
+    return [dtype, len(shape), L.arr(C.c_size_t, list(shape)), L.arr(C.c_ssize_t, list(sin)),
+            L.arr(C.c_ssize_t, list(sout)), len(axes), L.arr(C.c_size_t, list(axes))]
+
+
+def dct(x: np.ndarray, axes, type=2, fct=1.0, ortho=False, out=None):
+    """pocketfft::dct (pocketfft_hdronly.h:3284-3300) on host arrays."""
+    out = np.empty_like(x) if out is None else out
+    L.check(L.load().ig_dct(*_nd_head(_dtype_code(x), x.shape, x.strides, out.strides, axes), int(type),
+                            x.ctypes.data, out.ctypes.data, float(fct), int(ortho), 1))
+    return out
+
+
+def dst(x: np.ndarray, axes, type=2, fct=1.0, ortho=False, out=None):
+    """pocketfft::dst (pocketfft_hdronly.h:3302-3318) on host arrays."""
+    out = np.empty_like(x) if out is None else out
+    L.check(L.load().ig_dst(*_nd_head(_dtype_code(x), x.shape, x.strides, out.strides, axes), int(type),
+                            x.ctypes.data, out.ctypes.data, float(fct), int(ortho), 1))
+    return out
+
+
+def r2r_fftpack(x: np.ndarray, axes, real2hermitian=True, forward=True, fct=1.0, out=None):
+    """pocketfft::r2r_fftpack (pocketfft_hdronly.h:3392-3403), bound at pocketfft.nim:71-81."""
+    out = np.empty_like(x) if out is None else out
+    L.check(L.load().ig_r2r_fftpack(*_nd_head(_dtype_code(x), x.shape, x.strides, out.strides, axes),
+                                    int(real2hermitian), int(forward), x.ctypes.data, out.ctypes.data, float(fct), 1))
+    return out
+
+
+def hartley(x: np.ndarray, axes, fct=1.0, genuine=False, out=None):
+    """r2r_separable_hartley / r2r_genuine_hartley (pocketfft_hdronly.h:3405-3445)."""
+    out = np.empty_like(x) if out is None else out
+    fn = L.load().ig_r2r_genuine_hartley if genuine else L.load().ig_r2r_separable_hartley
+    L.check(fn(*_nd_head(_dtype_code(x), x.shape, x.strides, out.strides, axes), x.ctypes.data, out.ctypes.data,
+               float(fct), 1))
+    return out
+
 
 def c2c(x: np.ndarray, axes, forward=True, fct=1.0, out=None):
     out = np.empty_like(x) if out is None else out

@@ -205,6 +205,46 @@ int ig_fftconv_forward(ig_fftconv conv, const void *x, const void *k, void *y, v
 int ig_fftconv_backward(ig_fftconv conv, const void *x, const void *k, const void *gy, void *gx, void *gk,
                         void *stream);
 
+/* ---- real-to-real transforms ------------------------------------------------
+ * pocketfft::dct / dst (pocketfft_hdronly.h:3284-3318; DCTDesc.apply at
+ * cpp_pocketfft/pocketfft.nim:279-295), r2r_fftpack, r2r_separable_hartley and
+ * r2r_genuine_hartley (pocketfft_hdronly.h:3392-3445, bound at
+ * cpp_pocketfft/pocketfft.nim:71-106).  Same arguments: shape, byte strides,
+ * axes (transformed in order; fct on the first), DCT/DST type 1-4 and the
+ * ortho flag with the reference's scaling steps, real2hermitian / forward
+ * with the reference's sign conventions.  Real arrays of dtype IG_F64 or
+ * IG_F32, in host memory (nthreads ignored) or, for the _device forms, in
+ * device memory on `stream`.  Errors: "invalid DCT type" / "invalid DST
+ * type" (IG_EINVAL), "zero-length FFT requested" for DCT-I along an axis of
+ * length 1, and the axis / stride errors of ig_c2c. */
+int ig_dct(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in, const ptrdiff_t *stride_out,
+           size_t naxes, const size_t *axes, int type, const void *data_in, void *data_out, double fct, int ortho,
+           size_t nthreads);
+int ig_dst(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in, const ptrdiff_t *stride_out,
+           size_t naxes, const size_t *axes, int type, const void *data_in, void *data_out, double fct, int ortho,
+           size_t nthreads);
+int ig_r2r_fftpack(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in,
+                   const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int real2hermitian, int forward,
+                   const void *data_in, void *data_out, double fct, size_t nthreads);
+int ig_r2r_separable_hartley(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in,
+                             const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, const void *data_in,
+                             void *data_out, double fct, size_t nthreads);
+int ig_r2r_genuine_hartley(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in,
+                           const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, const void *data_in,
+                           void *data_out, double fct, size_t nthreads);
+int ig_dct_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in, const ptrdiff_t *stride_out,
+                  size_t naxes, const size_t *axes, int type, const void *data_in, void *data_out, double fct,
+                  int ortho, void *stream);
+int ig_dst_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in, const ptrdiff_t *stride_out,
+                  size_t naxes, const size_t *axes, int type, const void *data_in, void *data_out, double fct,
+                  int ortho, void *stream);
+int ig_r2r_fftpack_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in,
+                          const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int real2hermitian,
+                          int forward, const void *data_in, void *data_out, double fct, void *stream);
+int ig_r2r_hartley_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_in,
+                          const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int genuine,
+                          const void *data_in, void *data_out, double fct, void *stream);
+
 /* ---- autotuner -----------------------------------------------------------------
  * ig_autotune times every candidate configuration of one transform (kind 0:
  * complex, 1: real halfcomplex forward) -- radix order, elements per thread

@@ -602,7 +602,7 @@ typedef struct {
 } io_nd_job;
 
 /* ------------------------------------------------------------------ */
-/* DCT / DST I-IV by their defining sums (long double), with the       */
+/* DCT / DST I-IV by their defining sums (compensated, exact tables),  */
 /* scaling steps of pocketfft_hdronly.h:2424-2650: fct on every output; */
 /* ortho: DCT-I scales x[0], x[n-1] by sqrt2 and y[0], y[n-1] by       */
 /* 1/sqrt2; types II (DCT and DST) scale y[0] by 1/sqrt2; types III    */
@@ -610,40 +610,55 @@ typedef struct {
 /* ------------------------------------------------------------------ */
 static void io_dcst_line(int type, int cosine, int ortho, size_t n, const double *x, double *y, double fct)
 {
-    const long double PI = 3.14159265358979323846264338327950288L, R2 = 1.41421356237309504880168872420969808L;
-    for (size_t k = 0; k < n; ++k) {
-        long double acc = 0.0L;
-        for (size_t j = 0; j < n; ++j) {
-            long double xj = x[j];
-            long double t;
-            if (type == 1 && cosine) {
-                if (ortho && (j == 0 || j == n - 1)) xj *= R2;
-                long double w = (j == 0 || j == n - 1) ? 1.0L : 2.0L;
-                t = w * xj * cosl(PI * (long double)k * (long double)j / (long double)(n - 1));
-            } else if (type == 1) {
-                t = 2.0L * xj * sinl(PI * (long double)(k + 1) * (long double)(j + 1) / (long double)(n + 1));
-            } else if (type == 2) {
-                long double a = PI * (long double)(cosine ? k : k + 1) * (long double)(2 * j + 1) / (long double)(2 * n);
-                t = 2.0L * xj * (cosine ? cosl(a) : sinl(a));
-            } else if (type == 3 && cosine) {
-                if (ortho && j == 0) xj *= R2;
-                long double w = j == 0 ? 1.0L : 2.0L;
-                t = w * xj * cosl(PI * (long double)j * (long double)(2 * k + 1) / (long double)(2 * n));
-            } else if (type == 3) {
-                if (ortho && j == 0) xj *= R2;
-                long double w = j == n - 1 ? 1.0L : 2.0L;
-                t = w * xj * sinl(PI * (long double)(j + 1) * (long double)(2 * k + 1) / (long double)(2 * n));
-            } else {
-                long double a = PI * (long double)(2 * j + 1) * (long double)(2 * k + 1) / (long double)(4 * n);
-                t = 2.0L * xj * (cosine ? cosl(a) : sinl(a));
-            }
-            acc += t;
-        }
-        acc *= fct;
-        if (ortho && type == 1 && cosine && (k == 0 || k == n - 1)) acc /= R2;
-        if (ortho && type == 2 && k == 0) acc /= R2;
-        y[k] = (double)acc;
+    const long double PI = 3.14159265358979323846264338327950288L;
+    const double R2 = 1.41421356237309504880168872420969808;
+    /* every angle is pi * q / P for an integer q: one table of cos / sin(pi q / P), q < 2P
+       (long double, rounded once); the sums are compensated (Neumaier) in double */
+    size_t P = type == 1 ? (cosine ? n - 1 : n + 1) : type == 4 ? 4 * n : 2 * n;
+    double *cs = (double *)malloc(sizeof(double) * (4 * P + n));
+    if (!cs) { for (size_t k = 0; k < n; ++k) y[k] = 0.0 / 0.0; return; }
+    double *sn = cs + 2 * P, *xs = cs + 4 * P;
+    for (size_t q = 0; q < 2 * P; ++q) {
+        cs[q] = (double)cosl(PI * (long double)q / (long double)P);
+        sn[q] = (double)sinl(PI * (long double)q / (long double)P);
     }
+    for (size_t j = 0; j < n; ++j) {
+        double xj = x[j];
+        if (type == 1 && cosine) {
+            if (ortho && (j == 0 || j == n - 1)) xj *= R2;
+            xj *= (j == 0 || j == n - 1) ? 1.0 : 2.0;
+        } else if (type == 3 && cosine) {
+            if (ortho && j == 0) xj *= R2;
+            xj *= j == 0 ? 1.0 : 2.0;
+        } else if (type == 3) {
+            if (ortho && j == 0) xj *= R2;
+            xj *= j == n - 1 ? 1.0 : 2.0;
+        } else {
+            xj *= 2.0;
+        }
+        xs[j] = xj;
+    }
+    const size_t M2 = 2 * P;
+    const double *tab = cosine ? cs : sn;
+    for (size_t k = 0; k < n; ++k) {
+        double acc = 0.0, comp = 0.0;
+        for (size_t j = 0; j < n; ++j) {
+            size_t q;
+            if (type == 1) q = cosine ? k * j : (k + 1) * (j + 1);
+            else if (type == 2) q = (cosine ? k : k + 1) * (2 * j + 1);
+            else if (type == 3) q = cosine ? j * (2 * k + 1) : (j + 1) * (2 * k + 1);
+            else q = (2 * j + 1) * (2 * k + 1);
+            const double t = xs[j] * tab[q % M2];
+            const double s2 = acc + t;
+            comp += fabs(acc) >= fabs(t) ? (acc - s2) + t : (t - s2) + acc;
+            acc = s2;
+        }
+        double r = (acc + comp) * fct;
+        if (ortho && type == 1 && cosine && (k == 0 || k == n - 1)) r /= R2;
+        if (ortho && type == 2 && k == 0) r /= R2;
+        y[k] = r;
+    }
+    free(cs);
 }
 
 static void *io_nd_worker(void *arg)
