@@ -1,10 +1,10 @@
-// ig_dft.cuh -- register-resident small DFTs (radix 2, 3, 4, 5, 7, 8, 11, 13, 16).
+// ig_dft.cuh -- register-resident small DFTs (radix 2, 3, 4, 5, 7, 8, 9, 11, 13, 16).
 //
 // dft<R, FWD>(v) replaces v[0..R) by V[q] = sum_m v[m] exp(-+2 pi i m q / R)
 // (minus sign for the forward transform), the codelet set that PocketFFT's
 // passes cover (impulse/fft/c_pocketfft/pocketfft.c:300-865 for radix
 // 2/3/4/5/7/11; impulse/fft/cpp_pocketfft/pocketfft_hdronly.h:727-1305 adds
-// radix 8).  Radices 13 and 16 are new here.  The odd prime radices use the symmetric
+// radix 8).  Radices 9 (as 3 x 3), 13 and 16 are new here.  The odd prime radices use the symmetric
 // pair form: with a_k = v_k + v_{R-k} and b_k = v_k - v_{R-k},
 //   V_q = v_0 + sum_k a_k cos(2 pi k q/R) -+ i sum_k b_k sin(2 pi k q/R),
 // and V_{R-q} the same with the sign of the second sum flipped.
@@ -130,6 +130,39 @@ template <bool FWD, class R> IGD void dft16(cx<R> *v)
     t = v[11]; v[11] = v[14]; v[14] = t;
 }
 
+// radix 9 as 3 x 3 (the dft16 scheme): inner DFT3 over m2 of v[m1 + 3 m2],
+// twiddle by w9^(m1 q1), outer DFT3 over m1; V[q1 + 3 q2]
+constexpr double kC9_1 = 0.7660444431189780352023927, kS9_1 = 0.6427876096865393263226434;
+constexpr double kC9_2 = 0.1736481776669303488517166, kS9_2 = 0.9848077530122080593667430;
+constexpr double kC9_4 = -0.9396926207859083840541093, kS9_4 = 0.3420201433256687330440996;
+template <int P, bool FWD, class R> IGD void dft_odd(cx<R> *v);
+template <bool FWD, class R> IGD void dft3r(cx<R> &a, cx<R> &b, cx<R> &c)
+{
+    cx<R> t[3] = {a, b, c};
+    dft_odd<3, FWD>(t);
+    a = t[0];
+    b = t[1];
+    c = t[2];
+}
+template <bool FWD, class R> IGD void dft9(cx<R> *v)
+{
+#pragma unroll
+    for (int m1 = 0; m1 < 3; ++m1) dft3r<FWD>(v[m1], v[m1 + 3], v[m1 + 6]);
+    // now v[m1 + 3 q1] = Y[m1][q1]
+    constexpr double sg = FWD ? -1.0 : 1.0;
+    v[1 + 3 * 1] = cmulk(v[1 + 3 * 1], RealOps<R>::k(kC9_1), RealOps<R>::k(sg * kS9_1));
+    v[1 + 3 * 2] = cmulk(v[1 + 3 * 2], RealOps<R>::k(kC9_2), RealOps<R>::k(sg * kS9_2));
+    v[2 + 3 * 1] = cmulk(v[2 + 3 * 1], RealOps<R>::k(kC9_2), RealOps<R>::k(sg * kS9_2));
+    v[2 + 3 * 2] = cmulk(v[2 + 3 * 2], RealOps<R>::k(kC9_4), RealOps<R>::k(sg * kS9_4));
+#pragma unroll
+    for (int q1 = 0; q1 < 3; ++q1) dft3r<FWD>(v[3 * q1], v[3 * q1 + 1], v[3 * q1 + 2]);
+    // v[3 q1 + q2] = V[q1 + 3 q2] -> transpose the 3x3 index
+    cx<R> t;
+    t = v[1]; v[1] = v[3]; v[3] = t;
+    t = v[2]; v[2] = v[6]; v[6] = t;
+    t = v[5]; v[5] = v[7]; v[7] = t;
+}
+
 template <int P, bool FWD, class R> IGD void dft_odd(cx<R> *v)
 {
     constexpr int H = (P - 1) / 2;
@@ -176,6 +209,7 @@ template <int R, bool FWD, class T> IGD void dft(cx<T> *v)
     else if constexpr (R == 4) dft4<FWD>(v[0], v[1], v[2], v[3]);
     else if constexpr (R == 8) dft8<FWD>(v);
     else if constexpr (R == 16) dft16<FWD>(v);
+    else if constexpr (R == 9) dft9<FWD>(v);
     else dft_odd<R, FWD>(v);
 }
 

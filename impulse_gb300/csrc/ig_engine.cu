@@ -105,7 +105,7 @@ static int max_smem()
 // first, 1 reversed), elements per thread (0 default, 8, 16), lines per CTA
 // (0 default) and the four-step split N1 (0 default).
 struct TuneCfg {
-    int order = 0, E = 0, lpc = 0;
+    int order = 0, E = 0, lpc = 0, no9 = 0;
     long long N1 = 0;
     double ms = 0.0;
 };
@@ -133,7 +133,7 @@ static int elems_per_thread(long long L, int cfgE = 0)
 // Radices for a Stockham length L.  Cores of 8 elements per thread (up to
 // 4096 points by default) use radix 8 at most, since a radix-16 stage would
 // leave half the threads idle.
-static bool gpu_factor(long long L, std::vector<int> &rad, int E = 0, int order = 0)
+static bool gpu_factor(long long L, std::vector<int> &rad, int E = 0, int order = 0, int no9 = 0)
 {
     rad.clear();
     long long n = L;
@@ -143,8 +143,10 @@ static bool gpu_factor(long long L, std::vector<int> &rad, int E = 0, int order 
     if (n % 8 == 0) { rad.push_back(8); n /= 8; }
     if (n % 4 == 0) { rad.push_back(4); n /= 4; }
     if (n % 2 == 0) { rad.push_back(2); n /= 2; }
-    for (int p : {13, 11, 7, 5, 3})
+    for (int p : {13, 11, 7, 5, 9, 3}) {
+        if (p == 9 && no9) continue;  // tuned plans may prefer two radix-3 stages
         while (n % p == 0) { rad.push_back(p); n /= p; }
+    }
     if (order == 1) std::reverse(rad.begin(), rad.end());
     return n == 1;
 }
@@ -358,7 +360,7 @@ static void finish_layout(Core &c, long long L, long long M, const TuneCfg &cfg 
     c.d.lpc_pref = cfg.lpc;
     bool odd35 = false, odd711 = false, full = c.d.blue == 2;
     for (int s = 0; s < c.d.nst; ++s) {
-        odd35 |= c.d.st[s].R == 3 || c.d.st[s].R == 5;
+        odd35 |= c.d.st[s].R == 3 || c.d.st[s].R == 5 || c.d.st[s].R == 9;
         odd711 |= c.d.st[s].R == 7 || c.d.st[s].R == 11;
         full |= c.d.st[s].R == 13;
     }
@@ -464,7 +466,7 @@ static long long primitive_root(long long p)
 static bool rader_single(Arith a, long long M, const TuneCfg &cfg)
 {
     std::vector<int> rad;
-    if (!gpu_factor(M - 1, rad, cfg.E, cfg.order) || !fits_smem(a, M - 1, M)) return false;
+    if (!gpu_factor(M - 1, rad, cfg.E, cfg.order, cfg.no9) || !fits_smem(a, M - 1, M)) return false;
     if (elems_per_thread(M - 1, cfg.E) == 8) return true;
     const long long slots = (M + 1) + ((M + 1) >> 3);
     return 2 * slots * (long long)slot_bytes(a) <= (long long)max_smem() - 4096;
@@ -521,7 +523,7 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
     c->d.M = (int)std::min<long long>(M, 1 << 30);
     const TuneCfg cfg = tune_lookup(a, M);
     std::vector<int> rad;
-    bool smooth = gpu_factor(M, rad, cfg.E, cfg.order);
+    bool smooth = gpu_factor(M, rad, cfg.E, cfg.order, cfg.no9);
     if (real_tw) {
         void *rtw = c->alloc((M + 1) * slot_bytes(a));
         launch_roots_a(a, rtw, M + 1, 1, 2 * (unsigned long long)M);
@@ -543,7 +545,7 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
         // prime length: Rader over the Stockham length M - 1 in one CTA
         c->kind = 0;
         c->d.blue = 2;
-        gpu_factor(M - 1, rad, cfg.E, cfg.order);
+        gpu_factor(M - 1, rad, cfg.E, cfg.order, cfg.no9);
         build_stockham(*c, M - 1, rad);
         finish_layout(*c, M - 1, M, cfg);
         build_rader(*c, M);
@@ -557,7 +559,7 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
     } else if (!smooth) {
         long long L = good_size_gpu(2 * M - 1);
         std::vector<int> radL;
-        gpu_factor(L, radL, cfg.E, cfg.order);
+        gpu_factor(L, radL, cfg.E, cfg.order, cfg.no9);
         if (fits_smem(a, L, M)) {
             c->kind = 0;
             c->d.blue = 1;
@@ -2644,7 +2646,7 @@ static std::string tune_cache_path(const char *path)
     return e ? std::string(e) : std::string();
 }
 
-// one entry per line: gpu<TAB>arith<TAB>length<TAB>order<TAB>E<TAB>lpc<TAB>N1<TAB>ms
+// one entry per line: gpu<TAB>arith<TAB>length<TAB>order<TAB>E<TAB>lpc<TAB>no9<TAB>N1<TAB>ms
 int ig_autotune_save(const char *path)
 {
     return guarded([&] {
@@ -2655,8 +2657,8 @@ int ig_autotune_save(const char *path)
         std::string g = gpu_name();
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &kv : g_tune)
-            fprintf(fp, "%s\t%d\t%lld\t%d\t%d\t%d\t%lld\t%.6f\n", g.c_str(), kv.first.first, kv.first.second,
-                    kv.second.order, kv.second.E, kv.second.lpc, kv.second.N1, kv.second.ms);
+            fprintf(fp, "%s\t%d\t%lld\t%d\t%d\t%d\t%d\t%lld\t%.6f\n", g.c_str(), kv.first.first, kv.first.second,
+                    kv.second.order, kv.second.E, kv.second.lpc, kv.second.no9, kv.second.N1, kv.second.ms);
         fclose(fp);
     });
 }
@@ -2670,17 +2672,18 @@ int ig_autotune_load(const char *path)
         if (!fp) raise(IG_EINVAL, "cannot read " + f);
         std::string g = gpu_name();
         char name[256];
-        int a, order, E, lpc;
+        int a, order, E, lpc, no9;
         long long len, N1;
         double ms;
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        while (fscanf(fp, " %255[^\t]\t%d\t%lld\t%d\t%d\t%d\t%lld\t%lf", name, &a, &len, &order, &E, &lpc, &N1, &ms) ==
-               8) {
+        while (fscanf(fp, " %255[^\t]\t%d\t%lld\t%d\t%d\t%d\t%d\t%lld\t%lf", name, &a, &len, &order, &E, &lpc, &no9,
+                      &N1, &ms) == 9) {
             if (g != name) continue;
             TuneCfg c;
             c.order = order;
             c.E = E;
             c.lpc = lpc;
+            c.no9 = no9;
             c.N1 = N1;
             c.ms = ms;
             g_tune[std::make_pair(a, len)] = c;
@@ -2753,11 +2756,15 @@ int ig_autotune(int dtype, size_t length, int kind, double *best_ms)
                     for (int lpc : {0, 1, 2, 4, 8, 16, 32}) {
                         long long tpl = (L + E - 1) / E;
                         if (lpc * tpl > 512) continue;
-                        TuneCfg c;
-                        c.order = order;
-                        c.E = E;
-                        c.lpc = lpc;
-                        cands.push_back(c);
+                        for (int no9 : {0, 1}) {
+                            if (no9 && L % 9) continue;
+                            TuneCfg c;
+                            c.order = order;
+                            c.E = E;
+                            c.lpc = lpc;
+                            c.no9 = no9;
+                            cands.push_back(c);
+                        }
                     }
                 }
         }

@@ -208,7 +208,7 @@ __device__ __forceinline__ void stage_db(const cx<T> *src, cx<T> *dst, int LS2, 
 // 8-element cores at radix 8)
 template <int E, int RS> __host__ __device__ constexpr bool rs_has(int R)
 {
-    return (R == 2 || R == 4 || R == 8) || (R == 16 && E == 16) || (RS >= RS_P235 && (R == 3 || R == 5)) ||
+    return (R == 2 || R == 4 || R == 8) || (R == 16 && E == 16) || (RS >= RS_P235 && (R == 3 || R == 5 || R == 9)) ||
            (RS >= RS_ALL && (R == 7 || R == 11)) || (RS == RS_FULL && R == 13);
 }
 
@@ -226,6 +226,7 @@ __device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl,
         case 16: if constexpr (rs_has<E, RS>(16)) stage<T, E, 16>(sm, P, s, nl, tpl, g, t); break;
         case 3: if constexpr (rs_has<E, RS>(3)) stage<T, E, 3>(sm, P, s, nl, tpl, g, t); break;
         case 5: if constexpr (rs_has<E, RS>(5)) stage<T, E, 5>(sm, P, s, nl, tpl, g, t); break;
+        case 9: if constexpr (rs_has<E, RS>(9)) stage<T, E, 9>(sm, P, s, nl, tpl, g, t); break;
         case 7: if constexpr (rs_has<E, RS>(7)) stage<T, E, 7>(sm, P, s, nl, tpl, g, t); break;
         case 11: if constexpr (rs_has<E, RS>(11)) stage<T, E, 11>(sm, P, s, nl, tpl, g, t); break;
         case 13: if constexpr (rs_has<E, RS>(13)) stage<T, E, 13>(sm, P, s, nl, tpl, g, t); break;
@@ -250,6 +251,7 @@ __device__ __forceinline__ int run_stages_db(cx<T> *sm, int cur, const CoreDesc 
         case 16: if constexpr (rs_has<E, RS>(16)) stage_db<T, E, 16>(src, dst, LS2, P, s, nl, tpl, g, t); break;
         case 3: if constexpr (rs_has<E, RS>(3)) stage_db<T, E, 3>(src, dst, LS2, P, s, nl, tpl, g, t); break;
         case 5: if constexpr (rs_has<E, RS>(5)) stage_db<T, E, 5>(src, dst, LS2, P, s, nl, tpl, g, t); break;
+        case 9: if constexpr (rs_has<E, RS>(9)) stage_db<T, E, 9>(src, dst, LS2, P, s, nl, tpl, g, t); break;
         case 7: if constexpr (rs_has<E, RS>(7)) stage_db<T, E, 7>(src, dst, LS2, P, s, nl, tpl, g, t); break;
         case 11: if constexpr (rs_has<E, RS>(11)) stage_db<T, E, 11>(src, dst, LS2, P, s, nl, tpl, g, t); break;
         case 13: if constexpr (rs_has<E, RS>(13)) stage_db<T, E, 13>(src, dst, LS2, P, s, nl, tpl, g, t); break;

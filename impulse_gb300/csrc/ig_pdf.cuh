@@ -296,12 +296,37 @@ template <int P> IGP void pdft_odd(pcx *v)
     }
     v[0] = sum;
 }
+IGP void pdft3r(pcx &a, pcx &b, pcx &c)
+{
+    pcx t[3] = {a, b, c};
+    pdft_odd<3>(t);
+    a = t[0];
+    b = t[1];
+    c = t[2];
+}
+// radix 9 as 3 x 3 (scheme of dft9 in ig_dft.cuh), forward
+IGP void pdft9(pcx *v)
+{
+#pragma unroll
+    for (int m1 = 0; m1 < 3; ++m1) pdft3r(v[m1], v[m1 + 3], v[m1 + 6]);
+    v[1 + 3 * 1] = pcmulk(v[1 + 3 * 1], kC9_1, -kS9_1);
+    v[1 + 3 * 2] = pcmulk(v[1 + 3 * 2], kC9_2, -kS9_2);
+    v[2 + 3 * 1] = pcmulk(v[2 + 3 * 1], kC9_2, -kS9_2);
+    v[2 + 3 * 2] = pcmulk(v[2 + 3 * 2], kC9_4, -kS9_4);
+#pragma unroll
+    for (int q1 = 0; q1 < 3; ++q1) pdft3r(v[3 * q1], v[3 * q1 + 1], v[3 * q1 + 2]);
+    pcx t;
+    t = v[1]; v[1] = v[3]; v[3] = t;
+    t = v[2]; v[2] = v[6]; v[6] = t;
+    t = v[5]; v[5] = v[7]; v[7] = t;
+}
 template <int R> IGP void pdft(pcx *v)
 {
     if constexpr (R == 2) pdft2(v[0], v[1]);
     else if constexpr (R == 4) pdft4(v[0], v[1], v[2], v[3]);
     else if constexpr (R == 8) pdft8(v);
     else if constexpr (R == 16) pdft16(v);
+    else if constexpr (R == 9) pdft9(v);
     else pdft_odd<R>(v);
 }
 

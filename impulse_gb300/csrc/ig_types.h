@@ -29,8 +29,8 @@ constexpr int LAY_TW = 4;     // complex in / out with the four-step twiddle or 
 
 // radix classes of the kernel variants
 constexpr int RS_P2 = 0;   // 2, 4, 8, 16
-constexpr int RS_P235 = 1; // 2, 4, 8, 16, 3, 5
-constexpr int RS_ALL = 2;  // 2, 3, 4, 5, 7, 8, 11, 16
+constexpr int RS_P235 = 1; // 2, 4, 8, 16, 3, 5, 9
+constexpr int RS_ALL = 2;  // 2, 3, 4, 5, 7, 8, 9, 11, 16
 constexpr int RS_FULL = 3; // all of RS_ALL, 13, and the Rader steps (also the generic-layout kernels)
 
 enum InKind { IN_C = 0, IN_R = 1, IN_P = 2, IN_HC = 3 };
