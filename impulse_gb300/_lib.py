@@ -89,6 +89,9 @@ SIGNATURES = {
     "ig_dst_device": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, C.c_int, _vp]),
     "ig_r2r_fftpack_device": (C.c_int, _ND_HEAD + [C.c_int, C.c_int, _vp, _vp, C.c_double, _vp]),
     "ig_r2r_hartley_device": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, _vp]),
+    "ig_upfirdn_length": (C.c_int, [_sz, _sz, C.c_int, C.c_int, C.POINTER(_sz)]),
+    "ig_upfirdn": (C.c_int, [C.c_int, _sz, _sz, _vp, _sz, _sz, _vp, C.c_int, C.c_int, _vp, _sz]),
+    "ig_upfirdn_device": (C.c_int, [C.c_int, _sz, _sz, _vp, _sz, _sz, _vp, C.c_int, C.c_int, _vp, _sz, _vp]),
     "ig_autotune": (C.c_int, [C.c_int, _sz, C.c_int, C.POINTER(C.c_double)]),
     "ig_autotune_save": (C.c_int, [C.c_char_p]),
     "ig_autotune_load": (C.c_int, [C.c_char_p]),

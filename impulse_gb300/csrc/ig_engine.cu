@@ -2062,7 +2062,55 @@ static int r2r_entry(int op, int dtype, size_t ndim, const size_t *shape, const 
     });
 }
 
-// ---- adjoints of the real transforms ------------------------------------------// ---- adjoints of the real transforms ------------------------------------------
+// ---- upfirdn (impulse signal.nim:545-594) -----------------------------------------
+// upsample (up - 1 zeros between samples), full convolution with the FIR
+// filter h, every down-th sample: by FFT, the rows and the filter zero-padded
+// to an even smooth length P >= (n - 1) up + nh, r2c, product, c2r (1/P),
+// decimation.  One filter for all rows.
+static long long upfirdn_len(long long n, long long nh, int up, int down)
+{
+    const long long lc = (n - 1) * up + nh;
+    return (lc + down - 1) / down;
+}
+
+static void upfirdn_device(Arith a, long long B, long long n, const void *x, long long dx, long long nh, const void *h,
+                           int up, int down, void *y, long long dy, cudaStream_t st)
+{
+    if (up < 1 || down < 1) raise(IG_EINVAL, "up and down must be >= 1");
+    if (n < 1 || nh < 1) raise(IG_EINVAL, "empty signal or filter");
+    if (B == 0) return;
+    const long long sr = (long long)store_real_bytes(a), lc = (n - 1) * up + nh;
+    const long long P = 2 * good_size_gpu((lc + 1) / 2), PH = P / 2 + 1, ny = upfirdn_len(n, nh, up, down);
+    require_aligned(x, (size_t)sr, "signal");
+    require_aligned(h, (size_t)sr, "filter");
+    require_aligned(y, (size_t)sr, "output");
+    DevBuf U((size_t)(B * P * sr)), H((size_t)(P * sr)), FU((size_t)(B * PH * 2 * sr)), FH((size_t)(PH * 2 * sr));
+    auto pad = [&](const void *src, long long d, long long len, int u, void *dst, long long nb) {
+        cudaError_t e = a == A_F32 ? Launch<TagF32>::upsample_pad(src, d, len, u, dst, P, nb, st)
+                      : a == A_DF  ? Launch<TagDF>::upsample_pad(src, d, len, u, dst, P, nb, st)
+                                   : Launch<TagF64>::upsample_pad(src, d, len, u, dst, P, nb, st);
+        ck(e, "upsample");
+        count_launch();
+    };
+    pad(x, dx, n, up, U.p, B);
+    pad(h, nh, nh, 1, H.p, 1);
+    exec_op(a, OP_R2C, P, contiguous_lines(U.p, FU.p, B, P, PH, sr, 2 * sr), 1, 1.0, st);
+    exec_op(a, OP_R2C, P, contiguous_lines(H.p, FH.p, 1, P, PH, sr, 2 * sr), 1, 1.0, st);
+    cudaError_t e = a == A_F32 ? Launch<TagF32>::spec_mul(FU.p, FH.p, FU.p, B, 1, PH, 0, st)
+                  : a == A_DF  ? Launch<TagDF>::spec_mul(FU.p, FH.p, FU.p, B, 1, PH, 0, st)
+                               : Launch<TagF64>::spec_mul(FU.p, FH.p, FU.p, B, 1, PH, 0, st);
+    ck(e, "spectrum product");
+    count_launch();
+    exec_op(a, OP_C2R, P, contiguous_lines(FU.p, U.p, B, PH, P, 2 * sr, sr), 0, 1.0 / (double)P, st);
+    e = a == A_F32 ? Launch<TagF32>::decimate(U.p, P, down, y, dy, ny, B, st)
+      : a == A_DF  ? Launch<TagDF>::decimate(U.p, P, down, y, dy, ny, B, st)
+                   : Launch<TagF64>::decimate(U.p, P, down, y, dy, ny, B, st);
+    ck(e, "decimate");
+    count_launch();
+    ck(cudaStreamSynchronize(st), "upfirdn");  // temporaries are released on return
+}
+
+// ---- adjoints of the real transforms ------------------------------------------
 static void launch_half_weight(Arith a, void *x, long long lines, long long n_half, long long nreal, double w,
                                int drop_im, cudaStream_t st)
 {
@@ -2848,6 +2896,48 @@ int ig_c2r(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *sin
         if (ndim >= 1 && shape_out && prod(ndim, shape_out) == 0) return;
         nd_checks(dtype, ndim, shape_out, sin, sout, naxes, axes, in, out, false);
         host_nd(2, dtype, ndim, shape_out, sin, sout, naxes, axes, forward, in, out, fct);
+    });
+}
+
+// ---- upfirdn ----
+int ig_upfirdn_length(size_t n, size_t nh, int up, int down, size_t *out_len)
+{
+    return guarded([&] {
+        if (!out_len) raise(IG_EINVAL, "null argument");
+        if (up < 1 || down < 1) raise(IG_EINVAL, "up and down must be >= 1");
+        if (n < 1 || nh < 1) raise(IG_EINVAL, "empty signal or filter");
+        *out_len = (size_t)upfirdn_len((long long)n, (long long)nh, up, down);
+    });
+}
+int ig_upfirdn_device(int dtype, size_t batch, size_t n, const void *x, size_t dist_x, size_t nh, const void *h,
+                      int up, int down, void *y, size_t dist_y, void *stream)
+{
+    return guarded([&] {
+        if (dtype != IG_F64 && dtype != IG_F32) raise(IG_EINVAL, "bad dtype");
+        if (!x || !h || !y) raise(IG_EINVAL, "null argument");
+        upfirdn_device(arith_for(dtype), (long long)batch, (long long)n, x, (long long)dist_x, (long long)nh, h, up,
+                       down, y, (long long)dist_y, as_stream(stream));
+    });
+}
+int ig_upfirdn(int dtype, size_t batch, size_t n, const void *x, size_t dist_x, size_t nh, const void *h, int up,
+               int down, void *y, size_t dist_y)
+{
+    return guarded([&] {
+        if (dtype != IG_F64 && dtype != IG_F32) raise(IG_EINVAL, "bad dtype");
+        if (!x || !h || !y) raise(IG_EINVAL, "null argument");
+        if (up < 1 || down < 1) raise(IG_EINVAL, "up and down must be >= 1");
+        if (n < 1 || nh < 1) raise(IG_EINVAL, "empty signal or filter");
+        if (batch == 0) return;
+        const Arith a = arith_for(dtype);
+        const size_t sr = store_real_bytes(a);
+        const long long ny = upfirdn_len((long long)n, (long long)nh, up, down);
+        DevBuf dx(((batch - 1) * dist_x + n) * sr), dh(nh * sr), dyb(((batch - 1) * dist_y + (size_t)ny) * sr);
+        ck(cudaMemcpy(dx.p, x, dx.bytes, cudaMemcpyHostToDevice), "H2D copy");
+        ck(cudaMemcpy(dh.p, h, dh.bytes, cudaMemcpyHostToDevice), "H2D copy");
+        if (dist_y > (size_t)ny) ck(cudaMemcpy(dyb.p, y, dyb.bytes, cudaMemcpyHostToDevice), "H2D copy (output gaps)");
+        upfirdn_device(a, (long long)batch, (long long)n, dx.p, (long long)dist_x, (long long)nh, dh.p, up, down, dyb.p,
+                       (long long)dist_y, 0);
+        ck(cudaMemcpy(y, dyb.p, dyb.bytes, cudaMemcpyDeviceToHost), "D2H copy");
     });
 }
 

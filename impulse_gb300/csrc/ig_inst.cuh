@@ -168,6 +168,22 @@ template <class Tag> cudaError_t Launch<Tag>::r2r_tw(void *tw1, void *tw2, long 
     return cudaGetLastError();
 }
 template <class Tag>
+cudaError_t Launch<Tag>::upsample_pad(const void *x, long long dx, long long n, int up, void *U, long long P,
+                                      long long B, cudaStream_t st)
+{
+    using S = typename Traits<typename TagType<Tag>::T>::S;
+    k_upsample_pad<S><<<map_grid(B * P), 256, 0, st>>>((const S *)x, dx, n, up, (S *)U, P, B);
+    return cudaGetLastError();
+}
+template <class Tag>
+cudaError_t Launch<Tag>::decimate(const void *C, long long P, int down, void *y, long long dy, long long ny,
+                                  long long B, cudaStream_t st)
+{
+    using S = typename Traits<typename TagType<Tag>::T>::S;
+    k_decimate<S><<<map_grid(B * ny), 256, 0, st>>>((const S *)C, P, down, (S *)y, dy, ny, B);
+    return cudaGetLastError();
+}
+template <class Tag>
 cudaError_t Launch<Tag>::hartley_fold(const void *X, void *out, const HartleyDesc &h, cudaStream_t st)
 {
     using T = typename TagType<Tag>::T;

@@ -1407,6 +1407,35 @@ __global__ void k_hartley_fold(const typename Traits<T>::S2 *__restrict__ X, cha
 }
 
 // ---------------------------------------------------------------------------
+// upfirdn helpers (storage type S)
+// ---------------------------------------------------------------------------
+// U[b, m] = x[b, m / up] when m is a multiple of up and m / up < n, else 0 (m < P)
+template <class S>
+__global__ void k_upsample_pad(const S *__restrict__ x, long long dx, long long n, int up, S *__restrict__ U, long long P,
+                               long long B)
+{
+    const long long total = B * P;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long b = idx / P, m = idx - b * P;
+        const long long q = m / up;
+        U[idx] = (m - q * up == 0 && q < n) ? x[b * dx + q] : S(0);
+    }
+}
+// y[b, j] = C[b, j down], j < ny
+template <class S>
+__global__ void k_decimate(const S *__restrict__ C, long long P, int down, S *__restrict__ y, long long dy, long long ny,
+                           long long B)
+{
+    const long long total = B * ny;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long b = idx / ny, j = idx - b * ny;
+        y[b * dy + j] = C[b * P + j * (long long)down];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FFT-convolution helpers (elementwise; storage type S, arithmetic T)
 // ---------------------------------------------------------------------------
 

@@ -43,6 +43,11 @@ template <class Tag> struct Launch {
     static cudaError_t r2r_post(const IODesc &io, const R2RDesc &d, cudaStream_t st);
     static cudaError_t r2r_tw(void *tw1, void *tw2, long long N);
     static cudaError_t hartley_fold(const void *X, void *out, const HartleyDesc &h, cudaStream_t st);
+    // upfirdn
+    static cudaError_t upsample_pad(const void *x, long long dx, long long n, int up, void *U, long long P,
+                                    long long B, cudaStream_t st);
+    static cudaError_t decimate(const void *C, long long P, int down, void *y, long long dy, long long ny, long long B,
+                                cudaStream_t st);
 };
 
 // FP64 helpers for Bluestein tables (built in ig_inst_df.cu)

@@ -245,6 +245,19 @@ int ig_r2r_hartley_device(int dtype, size_t ndim, const size_t *shape, const ptr
                           const ptrdiff_t *stride_out, size_t naxes, const size_t *axes, int genuine,
                           const void *data_in, void *data_out, double fct, void *stream);
 
+/* ---- upfirdn (impulse signal.nim:545-594) -----------------------------------
+ * upfirdn(t, h, up, down) = t upsampled by `up` (up - 1 zeros between
+ * samples), fully convolved with the FIR filter h, every `down`-th sample
+ * kept; computed by FFT.  `batch` signals of n reals, signal b at
+ * x + b * dist_x; one filter of nh reals; output rows of length
+ * ig_upfirdn_length(n, nh, up, down) = ceil(((n - 1) up + nh) / down) at
+ * y + b * dist_y.  Host memory, or device memory on `stream` for _device. */
+int ig_upfirdn_length(size_t n, size_t nh, int up, int down, size_t *out_len);
+int ig_upfirdn(int dtype, size_t batch, size_t n, const void *x, size_t dist_x, size_t nh, const void *h, int up,
+               int down, void *y, size_t dist_y);
+int ig_upfirdn_device(int dtype, size_t batch, size_t n, const void *x, size_t dist_x, size_t nh, const void *h,
+                      int up, int down, void *y, size_t dist_y, void *stream);
+
 /* ---- autotuner -----------------------------------------------------------------
  * ig_autotune times every candidate configuration of one transform (kind 0:
  * complex, 1: real halfcomplex forward) -- radix order, elements per thread

@@ -957,6 +957,38 @@ int io_r2r_genuine_hartley(size_t ndim, const size_t *shape, const ptrdiff_t *si
     return rc;
 }
 
+/* upfirdn (impulse signal.nim:545-594): upsample by `up` (up - 1 zeros between samples,
+   length (n - 1) up + 1), full convolution with h, every `down`-th sample from index 0;
+   direct sums with compensated accumulation.  Rows b at x + b dx, y + b dy. */
+size_t io_upfirdn_length(size_t n, size_t nh, int up, int down)
+{
+    size_t lc = (n - 1) * (size_t)up + nh;
+    return (lc + (size_t)down - 1) / (size_t)down;
+}
+int io_upfirdn(size_t batch, size_t n, const double *x, size_t dx, size_t nh, const double *h, int up, int down,
+               double *y, size_t dy)
+{
+    if (up < 1 || down < 1 || n < 1 || nh < 1) return -1;
+    size_t ny = io_upfirdn_length(n, nh, up, down);
+    for (size_t b = 0; b < batch; ++b) {
+        const double *xb = x + b * dx;
+        for (size_t j = 0; j < ny; ++j) {
+            size_t m = j * (size_t)down; /* full-convolution index: c[m] = sum_i u[i] h[m - i] */
+            double acc = 0.0, comp = 0.0;
+            for (size_t q = 0; q < n; ++q) {
+                size_t i = q * (size_t)up;
+                if (i > m) break;
+                if (m - i >= nh) continue;
+                double t = xb[q] * h[m - i], s2 = acc + t;
+                comp += fabs(acc) >= fabs(t) ? (acc - s2) + t : (t - s2) + acc;
+                acc = s2;
+            }
+            y[b * dy + j] = acc + comp;
+        }
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* impulse's Nim glue (pocketfft.nim:126-204)                          */
 /* ------------------------------------------------------------------ */

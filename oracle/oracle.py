@@ -62,6 +62,9 @@ def lib():
         L.io_r2r_fftpack.argtypes = nd_head + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int]
         for nm in ("io_r2r_separable_hartley", "io_r2r_genuine_hartley"):
             getattr(L, nm).argtypes = nd_head + [C.c_void_p, C.c_void_p, C.c_double, C.c_int]
+        L.io_upfirdn_length.argtypes = [_sz, _sz, C.c_int, C.c_int]
+        L.io_upfirdn_length.restype = _sz
+        L.io_upfirdn.argtypes = [_sz, _sz, _dp, _sz, _sz, _dp, C.c_int, C.c_int, _dp, _sz]
         L.io_largest_prime_factor.argtypes = [_sz]
         L.io_largest_prime_factor.restype = _sz
         L.io_good_size.argtypes = [_sz]
@@ -224,6 +227,17 @@ def hartley(x, axes, fct=1.0, genuine=False, nthreads=None):
     if rc:
         raise ValueError(f"oracle hartley status {rc}")
     return out
+
+
+def upfirdn(t, h, up=1, down=1):
+    """impulse signal.nim:545-594 by direct sums; t 1-d or rows of a 2-d array."""
+    t = np.ascontiguousarray(np.atleast_2d(np.asarray(t, dtype=np.float64)))
+    h = np.ascontiguousarray(np.asarray(h, dtype=np.float64).ravel())
+    b, n = t.shape
+    ny = lib().io_upfirdn_length(n, h.size, up, down)
+    y = np.empty((b, ny))
+    assert lib().io_upfirdn(b, n, _p(t), n, h.size, _p(h), up, down, _p(y), ny) == 0
+    return y
 
 
 def unpack_fft(hc):

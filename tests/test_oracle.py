@@ -81,6 +81,18 @@ def test_r2r_and_hartley_vs_reference(oracle_lib, gold):
     assert oracle_lib.rel_l2(oracle_lib.hartley(xr, [0, 1, 2], 0.5, genuine=True), gold["hartley_gen_axes012"]) < TOL
 
 
+def test_upfirdn_known_answers(oracle_lib):
+    """The examples of upfirdn's documentation, impulse/signal.nim:560-592."""
+    cases = [(([1, 1, 1], [1, 1, 1], 1, 1), [1, 2, 3, 2, 1]),
+             (([1, 2, 3], [1], 3, 1), [1, 0, 0, 2, 0, 0, 3]),
+             (([1, 2, 3], [1, 1, 1], 3, 1), [1, 1, 1, 2, 2, 2, 3, 3, 3]),
+             (([1.0, 1.0, 1.0], [0.5, 1.0, 0.5], 2, 1), [0.5, 1, 1, 1, 1, 1, 0.5]),
+             ((np.arange(10.0), [1.0], 1, 3), [0, 3, 6, 9]),
+             ((np.arange(10.0), [0.5, 1.0, 0.5], 2, 3), [0, 1, 2.5, 4, 5.5, 7, 8.5])]
+    for (t, h, up, down), want in cases:
+        np.testing.assert_allclose(oracle_lib.upfirdn(t, h, up, down)[0], want, atol=1e-14)
+
+
 def test_known_answers(oracle_lib):
     """tests/test_fft2.nim:7-15 and README.md:41,68,98."""
     x = np.arange(4.0)
