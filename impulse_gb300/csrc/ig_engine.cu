@@ -175,7 +175,7 @@ struct Core {
     // four-step
     long long N1 = 0, N2 = 0;
     std::shared_ptr<Core> c1, c2;
-    const void *whi = nullptr, *wlo = nullptr;
+    const void *whi = nullptr, *wlo = nullptr, *tw4tab = nullptr;
     // Bluestein over a large core
     long long n2 = 0;
     std::shared_ptr<Core> sub;
@@ -619,6 +619,17 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
         launch_roots_a(a, wlo, c->N2, 1, (unsigned long long)M);
         c->whi = whi;
         c->wlo = wlo;
+        // the full twiddle table when it stays modest (one table read per element)
+        if (M <= (1LL << 22)) {
+            const size_t twb = a == A_DF ? 32 : slot_bytes(a);
+            void *tab = c->alloc((size_t)M * twb);
+            cudaError_t e = a == A_F32 ? Launch<TagF32>::tw4_table(tab, c->N1, c->N2)
+                          : a == A_DF  ? Launch<TagDF>::tw4_table(tab, c->N1, c->N2)
+                                       : Launch<TagF64>::tw4_table(tab, c->N1, c->N2);
+            ck(e, "four-step twiddles");
+            count_launch();
+            c->tw4tab = tab;
+        }
     }
     ck(cudaDeviceSynchronize(), "plan tables");
     return c;
@@ -821,6 +832,7 @@ static void fourstep_passes(const Core &c, const IODesc &io, char *B, IODesc &p1
     p1.fdS = make_fdiv((unsigned)N2);
     p1.tw4hi = c.whi;
     p1.tw4lo = c.wlo;
+    p1.tw4tab = c.tw4tab;
     p1.cols_in = 1;
     p1.cols_out = 1;
     // pass 2: rows, transposed write

@@ -96,7 +96,7 @@ template <class Tag> cudaError_t Launch<Tag>::scatter(const IODesc &io, const Ma
 template <class Tag> cudaError_t Launch<Tag>::line_exp(const IODesc &io, int *esc, cudaStream_t st)
 {
     using T = typename TagType<Tag>::T;
-    k_line_exp<T><<<(unsigned)io.nlines, 256, 0, st>>>(io, esc);
+    k_line_exp<T><<<(unsigned)io.nlines, 1024, 0, st>>>(io, esc);
     return cudaGetLastError();
 }
 template <class Tag>
@@ -159,6 +159,13 @@ template <class Tag> cudaError_t Launch<Tag>::r2r_post(const IODesc &io, const R
 {
     using T = typename TagType<Tag>::T;
     k_r2r_post<T><<<map_grid(io.nlines * d.N), 256, 0, st>>>(io, d);
+    return cudaGetLastError();
+}
+template <class Tag> cudaError_t Launch<Tag>::tw4_table(void *tab, long long N1, long long N2)
+{
+    using T = typename TagType<Tag>::T;
+    const long long n = N1 * N2;
+    k_gen_tw4<T><<<(unsigned)((n + 255) / 256), 256>>>((typename Bfly<T>::W *)tab, N1, N2);
     return cudaGetLastError();
 }
 template <class Tag> cudaError_t Launch<Tag>::r2r_tw(void *tw1, void *tw2, long long N)

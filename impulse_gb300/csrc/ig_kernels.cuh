@@ -113,6 +113,22 @@ template <> struct Bfly<df> {
     template <int R> static __device__ __forceinline__ void dft(V *v) { pdft<R>(v); }
 };
 
+// z * w (forward) or z * conj(w) with w in the stage-twiddle format
+template <class T>
+__device__ __forceinline__ cx<T> tw_apply(cx<T> z, const typename Bfly<T>::W *w, int fwd, const CoreDesc &P)
+{
+    if constexpr (std::is_same<T, df>::value) {
+        pcx a = to_p(z);
+        if (!fwd) a = pconj(a);
+        a = pmulw(a, w, bcast(P.neg1));
+        if (!fwd) a = pconj(a);
+        return from_p(a);
+    } else {
+        (void)P;
+        return fwd ? cmul(z, *w) : cmulc(z, *w);
+    }
+}
+
 // One Stockham stage of radix R in shared memory, in place through
 // registers.  Butterfly j (j < L/R) of a line reads x[j + m L/R], twiddles
 // input m by w^(m k) (k = j mod ns, w = exp(-+2 pi i/(ns R))), runs a radix-R
@@ -799,7 +815,11 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 }
                 cx<T> z = sget(line + sp(u, pad));
                 if (cc) z.i = -z.i;
-                if (io.tw4) {
+                if (io.tw4 && io.tw4tab) {
+                    // full table, row n2: w^(n2 u)
+                    const auto *w = reinterpret_cast<const typename Bfly<T>::W *>(io.tw4tab) + (size_t)n2 * io.cnt_out + u;
+                    z = tw_apply<T>(z, w, io.fwd, P);
+                } else if (io.tw4) {
                     // t = n2 u < M: w^t = w_hi[t / S] * w_lo[t mod S]
                     const unsigned tt = (unsigned)n2 * (unsigned)u;
                     const unsigned hi = fdiv(tt, io.fdS), lo = tt - hi * (unsigned)io.tw4S;
@@ -1602,6 +1622,23 @@ template <class T> __global__ void k_gen_r2r_tw(cx<T> *tw1, cx<T> *tw2, long lon
         double2 v = exp2pi_frac(2ull * (unsigned long long)j + 1ull, 8ull * (unsigned long long)N);
         v.y = -v.y;
         tw2[j] = to_arith<T>(v);
+    }
+}
+
+// four-step twiddles, in the stage-twiddle format of the arithmetic:
+// tab[n2 N1 + k1] = exp(-2 pi i n2 k1 / (N1 N2))
+template <class T> __global__ void k_gen_tw4(typename Bfly<T>::W *tab, long long N1, long long N2)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= N1 * N2) return;
+    const long long n2 = e / N1, k1 = e - n2 * N1;
+    double2 v = exp2pi_frac((unsigned long long)(n2 * k1), (unsigned long long)(N1 * N2));
+    v.y = -v.y;
+    if constexpr (std::is_same<T, df>::value) {
+        const cx<df> w = to_arith<df>(v);
+        tab[e] = ptw{pk(w.r.h, w.r.h), pk(-w.i.h, w.i.h), pk(w.r.l, w.r.l), pk(-w.i.l, w.i.l)};
+    } else {
+        tab[e] = to_arith<T>(v);
     }
 }
 

@@ -42,6 +42,8 @@ template <class Tag> struct Launch {
     static cudaError_t r2r_pre(const IODesc &io, const R2RDesc &d, cudaStream_t st);
     static cudaError_t r2r_post(const IODesc &io, const R2RDesc &d, cudaStream_t st);
     static cudaError_t r2r_tw(void *tw1, void *tw2, long long N);
+    // four-step inter-pass twiddles w_M^(n2 k1), row n2 < N2 of N1 entries (M = N1 N2)
+    static cudaError_t tw4_table(void *tab, long long N1, long long N2);
     static cudaError_t hartley_fold(const void *X, void *out, const HartleyDesc &h, cudaStream_t st);
     // upfirdn
     static cudaError_t upsample_pad(const void *x, long long dx, long long n, int up, void *U, long long P,

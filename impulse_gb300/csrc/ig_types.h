@@ -94,6 +94,7 @@ struct IODesc {
     long long tw4N, tw4S;
     FastDiv fdS;            // division by tw4S
     const void *tw4hi, *tw4lo;
+    const void *tw4tab;     // when set: the full table, N1 entries a line (stage-twiddle format)
     // pointwise product on output unit u of line l with tab[(l % bn0) * mul_a + u * mul_b]
     // (conjugated when mul_conj); Bluestein's convolution step on a four-step core
     const void *mul;
