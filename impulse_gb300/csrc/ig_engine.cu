@@ -725,10 +725,13 @@ static Scratch &scratch_for(cudaStream_t st)
     return *p;
 }
 
-static void launch_map(Arith a, bool gather, const IODesc &io_in, const MapDesc &mp, cudaStream_t st)
+static void launch_map(Arith a, bool gather, const IODesc &io_in, const MapDesc &mp_in, cudaStream_t st)
 {
     IODesc io = io_in;
     set_line_divs(io);
+    MapDesc mp = mp_in;
+    mp.fsl = make_fdiv((unsigned)std::max<long long>(1, std::min<long long>(mp.scr_len, 0x7fffffffLL)));
+    mp.fcnt = make_fdiv((unsigned)std::max<long long>(1, std::min<long long>(io.cnt_out, 0x7fffffffLL)));
     cudaError_t e;
     if (gather)
         e = a == A_F32 ? Launch<TagF32>::gather(io, mp, st)
@@ -744,10 +747,13 @@ static void launch_map(Arith a, bool gather, const IODesc &io_in, const MapDesc 
 
 static void run_complex(const Core &c, const IODesc &io, cudaStream_t st);
 
-static void launch_pair_map(Arith a, int which, const IODesc &io_in, const MapDesc &mp, int *esc, cudaStream_t st)
+static void launch_pair_map(Arith a, int which, const IODesc &io_in, const MapDesc &mp_in, int *esc, cudaStream_t st)
 {
     IODesc io = io_in;
     set_line_divs(io);
+    MapDesc mp = mp_in;
+    mp.fsl = make_fdiv((unsigned)std::max<long long>(1, std::min<long long>(mp.scr_len, 0x7fffffffLL)));
+    mp.fcnt = make_fdiv((unsigned)std::max<long long>(1, std::min<long long>(io.cnt_out, 0x7fffffffLL)));
     cudaError_t e;
     if (which == 0)
         e = a == A_F32 ? Launch<TagF32>::line_exp(io, esc, st)
@@ -1926,10 +1932,13 @@ static std::shared_ptr<R2RTables> r2r_tables(Arith a, long long N)
     return t;
 }
 
-static void launch_r2r(Arith a, bool pre, const IODesc &io_in, const R2RDesc &d, cudaStream_t st)
+static void launch_r2r(Arith a, bool pre, const IODesc &io_in, const R2RDesc &d_in, cudaStream_t st)
 {
     IODesc io = io_in;
     set_line_divs(io);
+    R2RDesc d = d_in;
+    d.fL2 = make_fdiv((unsigned)std::max<long long>(1, std::min<long long>(d.L2, 0x7fffffffLL)));
+    d.fN = make_fdiv((unsigned)std::max<long long>(1, std::min<long long>(d.N, 0x7fffffffLL)));
     cudaError_t e;
     if (pre)
         e = a == A_F32 ? Launch<TagF32>::r2r_pre(io, d, st)

@@ -51,6 +51,12 @@ __device__ __forceinline__ unsigned fdiv(unsigned n, FastDiv f)
     return (unsigned)(((unsigned long long)n * f.m) >> f.s);
 }
 
+// n / d for element indices: 32-bit fast division below 2^31, else 64-bit
+__device__ __forceinline__ long long qdiv(long long n, long long d, FastDiv f)
+{
+    return n < 0x7fffffffLL ? (long long)fdiv((unsigned)n, f) : n / d;
+}
+
 // byte offset of line l: from the offset tables when present, else
 // l -> (l mod bn0, (l / bn0) mod bn1, l / (bn0 bn1)) over the batch dims
 __device__ __forceinline__ long long line_off(const IODesc &io, long long l, bool out)
@@ -962,7 +968,7 @@ __global__ void k_gather(const __grid_constant__ IODesc io, const __grid_constan
     const long long total = io.nlines * mp.scr_len;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        long long l = idx / mp.scr_len, u = idx - l * mp.scr_len;
+        long long l = qdiv(idx, mp.scr_len, mp.fsl), u = idx - l * mp.scr_len;
         const char *base = io.in + line_off(io, l, false);
         S2 *dst = reinterpret_cast<S2 *>(mp.scr) + l * mp.scr_len + u;
         double re = 0, im = 0;
@@ -1046,7 +1052,7 @@ __global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_consta
     sc.init(io);
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        long long l = idx / cnt, u = idx - l * cnt;
+        long long l = qdiv(idx, cnt, mp.fcnt), u = idx - l * cnt;
         char *base = io.out + line_off(io, l, true);
         const S2 *src = reinterpret_cast<const S2 *>(mp.scr) + l * mp.scr_len;
         cx<T> z;
@@ -1054,7 +1060,7 @@ __global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_consta
         if (mp.kind == MAP_SPLIT_EVEN) {
             // X[k] = E_k + w^k O_k from Z[k], Z[M-k] (k <= M, Z[M] = Z[0])
             long long M = mp.M;
-            S2 a = src[u % M], b = src[(M - u) % M];
+            S2 a = src[u == M ? 0 : u], b = src[u == 0 ? 0 : M - u];
             lc.fit(a.x, a.y, b.x, b.y);
             cx<T> za = lc.in(a.x, a.y), zb = conjx(lc.in(b.x, b.y));
             cx<T> E = chalf(za + zb);
@@ -1155,7 +1161,7 @@ __global__ void k_gather_pair(const __grid_constant__ IODesc io, const __grid_co
     const long long total = io.nlines * mp.scr_len;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const long long l = idx / mp.scr_len, u = idx - l * mp.scr_len;
+        const long long l = qdiv(idx, mp.scr_len, mp.fsl), u = idx - l * mp.scr_len;
         S2 *dst = reinterpret_cast<S2 *>(mp.scr) + idx;
         cx<T> z{RealOps<T>::k(0.0), RealOps<T>::k(0.0)};
         const char *base = io.in + line_off(io, l, false);
@@ -1216,7 +1222,7 @@ __global__ void k_scatter_pair(const __grid_constant__ IODesc io, const __grid_c
     sc.init(io);
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const long long l = idx / cnt;
+        const long long l = qdiv(idx, cnt, mp.fcnt);
         const int u = (int)(idx - l * cnt);
         char *base = io.out + line_off(io, l, true);
         const bool has_b = 2LL * line_i0(io, l) + 1 < io.pair_n0;
@@ -1281,7 +1287,7 @@ __global__ void k_r2r_pre(const __grid_constant__ IODesc io, const __grid_consta
     const long long total = io.nlines * d.L2, N = d.N;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const long long l = idx / d.L2, m = idx - l * d.L2;
+        const long long l = qdiv(idx, d.L2, d.fL2), m = idx - l * d.L2;
         const char *base = io.in + line_off(io, l, false);
         auto X = [&](long long j) { return (double)*reinterpret_cast<const S *>(base + j * io.is); };
         if (d.mode == R2R_COPY || d.mode == R2R_HARTLEY) {
@@ -1353,7 +1359,7 @@ __global__ void k_r2r_post(const __grid_constant__ IODesc io, const __grid_const
     const long long N = d.N, total = io.nlines * N;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const long long l = idx / N, k = idx - l * N;
+        const long long l = qdiv(idx, N, d.fN), k = idx - l * N;
         S *dst = reinterpret_cast<S *>(io.out + line_off(io, l, true) + k * io.os);
         if (d.mode == R2R_COPY) {
             double v = reinterpret_cast<const S *>(d.scr)[l * d.L2 + k];

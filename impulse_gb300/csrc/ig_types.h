@@ -139,6 +139,7 @@ struct MapDesc {
     const int *ridx;    // MAP_RADER: g^-q (gather) or the discrete log (scatter)
     void *x0buf;        // MAP_RADER: storage complex x[0] of each scratch line
     void *a0buf;        // MAP_RADER: storage complex A[0] of each scratch line
+    FastDiv fsl, fcnt;  // division by scr_len and by the user side's unit count (set by the launchers)
 };
 
 
@@ -161,6 +162,7 @@ struct R2RDesc {
     const void *tw1;    // cx<T> exp(-2 pi i m / 4N), m <= N
     const void *tw2;    // cx<T> exp(-2 pi i (2k + 1) / 8N), k < N
     double fct;         // DCT / DST: scale applied by the post-map
+    FastDiv fL2, fN;    // division by L2 and N (set by the launcher)
 };
 // genuine Hartley over several axes: the r2c half spectrum (contiguous, shape
 // `tshp`) folded into the real output: out[i] = re + im, out[-i] = re - im
