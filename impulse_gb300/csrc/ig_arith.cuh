@@ -311,6 +311,22 @@ template <class R> IGD cx<R> cscale(cx<R> a, R s) { return cx<R>{a.r * s, a.i * 
 IGD cx<float> chalf(cx<float> a) { return cx<float>{a.r * 0.5f, a.i * 0.5f}; }
 IGD cx<double> chalf(cx<double> a) { return cx<double>{a.r * 0.5, a.i * 0.5}; }
 IGD cx<df> chalf(cx<df> a) { return cx<df>{df_scale2(a.r, 0.5f), df_scale2(a.i, 0.5f)}; }
+// times 2^d, d <= 0 (exact; below the float range the value flushes to zero)
+IGD cx<float> cscale_pow2(cx<float> a, int d)
+{
+    if (!d) return a;
+    if (d < -126) return cx<float>{0.0f, 0.0f};
+    const float f = u2f((uint32_t)(127 + d) << 23);
+    return cx<float>{IG_FMUL(a.r, f), IG_FMUL(a.i, f)};
+}
+IGD cx<double> cscale_pow2(cx<double> a, int) { return a; }
+IGD cx<df> cscale_pow2(cx<df> a, int d)
+{
+    if (!d) return a;
+    if (d < -126) return cx<df>{df{0.0f, 0.0f}, df{0.0f, 0.0f}};
+    const float f = u2f((uint32_t)(127 + d) << 23);
+    return cx<df>{df_scale2(a.r, f), df_scale2(a.i, f)};
+}
 // renormalise a double-float complex (no-op for float / double)
 IGD cx<float> crenorm(cx<float> a) { return a; }
 IGD cx<double> crenorm(cx<double> a) { return a; }

@@ -279,6 +279,8 @@ static int choose_layout(Arith a, const IODesc &io)
                                                                                                           : LAY_GEN;
     if (!plain) return LAY_GEN;
     if (!io.pair && io.in_kind == IN_C && io.out_kind == OUT_C && io.post == POST_NONE) return LAY_C2C;
+    // the fused four-step split reads complex rows and has its own epilogue
+    if (!io.pair && io.in_kind == IN_C && io.out_kind == OUT_HC && io.post == POST_SPLIT4) return LAY_C2C;
     if (!io.pair && io.in_kind == IN_C && io.out_kind == OUT_HC && io.post == POST_SPLIT) return LAY_R2HC;
     if (io.pair && io.in_kind == IN_R && io.out_kind == OUT_HC && io.post == POST_PAIR) return LAY_PR2HC;
     return LAY_GEN;
@@ -670,6 +672,7 @@ static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
     long long budget = line_bytes * 3 <= smax ? smax / 3 : line_bytes * 2 <= smax ? smax / 2 : smax;
     lpc = std::min<long long>(lpc, std::max<long long>(1, budget / line_bytes));
     lpc = std::min<long long>(lpc, std::max<long long>(1, io.nlines));
+    if (io.post == POST_SPLIT4) lpc = std::max<long long>(2, lpc & ~1LL);  // whole row pairs per CTA
     io.lpc = (int)lpc;
     io.tpl = (int)tpl;
     set_line_divs(io);
@@ -872,6 +875,50 @@ static void fourstep_passes(const Core &c, const IODesc &io, char *B, IODesc &p1
     p2.keep0_rows = (int)N1;
 }
 
+// Forward real halfcomplex transform over a four-step core of length M = N1 N2
+// (N = 2M reals): column pass into scratch B, then a row pass whose CTAs hold
+// each row r next to its mirror N1 - r and write X[k], X[M - k] directly.
+static bool g_fused_split = getenv("IG_NO_FUSED_SPLIT") == nullptr;
+static void run_fourstep_split(const Core &c, const IODesc &io, char *B, cudaStream_t st)
+{
+    IODesc p1, p2;
+    fourstep_passes(c, io, B, p1, p2);
+    launch_smem(c.a, c.c1->d, p1, st);
+    const long long N1 = c.N1, N2 = c.N2, M = c.M, nl = io.nlines;
+    const long long ES = 2 * (long long)store_real_bytes(c.a);
+    // row slots of one transform: pairs (r, N1 - r) for 0 < r < N1 / 2, (0, 0), and (N1 / 2, N1 / 2)
+    const long long LT = 2 * ((N1 - 1) / 2) + 2 + (N1 % 2 == 0 ? 2 : 0);
+    IODesc q = p2;
+    q.nlines = nl * LT;
+    q.bn[0] = LT;
+    q.bn[1] = io.bn[0];
+    q.bn[2] = io.bn[1];
+    q.bsi[0] = N2 * ES;
+    q.bsi[1] = M * ES;
+    q.bsi[2] = io.bn[0] * M * ES;
+    q.bso[0] = 0;
+    q.bso[1] = io.bso[0];
+    q.bso[2] = io.bso[1];
+    q.loff_in = q.loff_out = nullptr;
+    q.in = B;
+    q.out = io.out;
+    q.in_kind = IN_C;
+    q.is = ES;
+    q.out_kind = OUT_HC;
+    q.os = io.os;
+    q.nreal = io.nreal;
+    q.cnt_in = q.cnt_out = (int)N2;
+    q.post = POST_SPLIT4;
+    q.split_tw = c.rtw;
+    q.split_N1 = (int)N1;
+    q.fct = io.fct;
+    q.cols_in = q.cols_out = 0;
+    q.mul = nullptr;
+    q.keep0 = nullptr;
+    q.tw4 = 0;
+    launch_smem(c.a, c.c2->d, q, st);
+}
+
 // The convolution of Bluestein (kind 2) and Rader (kind 3) on nl contiguous
 // scratch lines of length L, in place: forward FFT_L with the product by the
 // transformed kernel (chirpf / B) fused into its last pass, then the
@@ -990,7 +1037,11 @@ static void run_complex(const Core &c, const IODesc &io_all, cudaStream_t st)
                 f.pre = PRE_NONE;
                 f.cnt_in = (int)M;
             }
-            if (scat) {
+            if (scat && io.post == POST_SPLIT && io.out_kind == OUT_HC && !gath && !io.conj_out && !io.real_out &&
+                !io.loff_out && io.bn[2] == 1 && c.rtw && g_fused_split) {
+                // the real split fused into the row pass: rows paired with their mirrors
+                run_fourstep_split(c, io, B, st);
+            } else if (scat) {
                 char *C = (char *)scr.get(2, (size_t)(nl * M * ES));
                 f.out = C;
                 f.os = ES;

@@ -57,16 +57,31 @@ __device__ __forceinline__ long long qdiv(long long n, long long d, FastDiv f)
     return n < 0x7fffffffLL ? (long long)fdiv((unsigned)n, f) : n / d;
 }
 
+// POST_SPLIT4 row order: slot j of a transform's N1 rows holds row
+// r = j / 2 + 1 (j even) or N1 - r (j odd) while r < N1 / 2, then row 0 twice
+// and, for even N1, row N1 / 2 twice
+__device__ __forceinline__ int split_row(int j, int N1)
+{
+    const int h2 = ((N1 - 1) >> 1) << 1;
+    if (j < h2) {
+        const int r = (j >> 1) + 1;
+        return (j & 1) ? N1 - r : r;
+    }
+    return ((j - h2) >> 1) ? (N1 >> 1) : 0;
+}
+
 // byte offset of line l: from the offset tables when present, else
 // l -> (l mod bn0, (l / bn0) mod bn1, l / (bn0 bn1)) over the batch dims
+// (on the input side of POST_SPLIT4 the first index is a row slot)
 __device__ __forceinline__ long long line_off(const IODesc &io, long long l, bool out)
 {
     if (out ? io.loff_out != nullptr : io.loff_in != nullptr) return out ? io.loff_out[l] : io.loff_in[l];
     const unsigned lu = (unsigned)l;
     const unsigned q0 = fdiv(lu, io.fb0);
-    const unsigned i0 = lu - q0 * (unsigned)io.bn[0];
+    unsigned i0 = lu - q0 * (unsigned)io.bn[0];
     const unsigned q1 = fdiv(q0, io.fb1);
     const unsigned i1 = q0 - q1 * (unsigned)io.bn[1];
+    if (!out && io.split_N1) i0 = (unsigned)split_row((int)i0, io.split_N1);
     return out ? (long long)i0 * io.bso[0] + (long long)i1 * io.bso[1] + (long long)q1 * io.bso[2]
                : (long long)i0 * io.bsi[0] + (long long)i1 * io.bsi[1] + (long long)q1 * io.bsi[2];
 }
@@ -731,6 +746,66 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         }
     }
     if (post_pair) __syncthreads();
+
+    // ---- fused real split of a four-step second pass (POST_SPLIT4) --------------
+    // pair q = lines (2q, 2q + 1) = rows (r, N1 - r) (split_row); element u of row r is
+    // Z[k], k = r + N1 u, and Z[M - k] sits in the mirror row at N2 - 1 - u
+    // (row 0: at N2 - u).  Both rows come to the smaller of their two range
+    // scales; X[k] and X[M - k] are written as halfcomplex.
+    if constexpr (LAY == LAY_GEN || LAY == LAY_C2C) {
+        if (io.post == POST_SPLIT4) {
+            const int N2 = io.cnt_in, N1 = io.split_N1;
+            const long long Mt = (long long)N1 * N2;
+            const int npairs = nl >> 1;
+            const cx<T> *rtw = reinterpret_cast<const cx<T> *>(io.split_tw);
+            OutScale<T> sc;
+            sc.init(io);
+            // element i = q + npairs u, rows fastest (consecutive outputs); the
+            // walk steps (q, u) by blockDim.x without a division per element
+            const int dq = (int)(blockDim.x % (unsigned)npairs), du = (int)(blockDim.x / (unsigned)npairs);
+            int q = (int)(threadIdx.x % (unsigned)npairs), u = (int)(threadIdx.x / (unsigned)npairs);
+            for (; u < N2;) {
+                const int ga = 2 * q, gb = ga + 1;
+                const long long la = line0 + ga;
+                const int ja = line_i0(io, la);
+                const int ra = split_row(ja, N1), rb = split_row(ja + 1, N1);
+                const int u2 = ra == 0 ? (u == 0 ? 0 : N2 - u) : N2 - 1 - u;
+                if (ra != rb || u <= u2) {
+                    cx<T> a = sget(sm + (size_t)ga * LSt + cur + sp(u, pad));
+                    cx<T> b = sget(sm + (size_t)gb * LSt + cur + sp(u2, pad));
+                    int ec = 0;
+                    if (scaled) {
+                        const int ea = s_esc[2 * ga], eb = s_esc[2 * gb];
+                        ec = min(ea, eb);
+                        a = cscale_pow2(a, ec - ea);
+                        b = cscale_pow2(b, ec - eb);
+                    }
+                    const long long k = ra + (long long)N1 * u, km = Mt - k;
+                    char *base = io.out + line_off(io, la, true);
+                    auto split_store = [&](cx<T> za, cx<T> zb, long long kk) {
+                        const cx<T> zc = conjx(zb);
+                        const cx<T> E = chalf(za + zc), D = chalf(za - zc);
+                        const cx<T> X = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[kk]));
+                        if (kk == 0) {
+                            *reinterpret_cast<S *>(base) = sc.apply(X.r, ec);
+                        } else if (kk == Mt) {
+                            *reinterpret_cast<S *>(base + (2 * Mt - 1) * io.os) = sc.apply(X.r, ec);
+                        } else {
+                            char *p = base + (2 * kk - 1) * io.os;
+                            *reinterpret_cast<S *>(p) = sc.apply(X.r, ec);
+                            *reinterpret_cast<S *>(p + io.os) = sc.apply(X.i, ec);
+                        }
+                    };
+                    split_store(a, b, k);
+                    if (km != k) split_store(b, a, km);
+                }
+                q += dq;
+                u += du;
+                if (q >= npairs) { q -= npairs; ++u; }
+            }
+            return;
+        }
+    }
 
     // ---- epilogue: shared memory -> HBM ---------------------------------------
     {

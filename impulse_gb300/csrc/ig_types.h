@@ -36,7 +36,13 @@ constexpr int RS_FULL = 3; // all of RS_ALL, 13, and the Rader steps (also the g
 enum InKind { IN_C = 0, IN_R = 1, IN_P = 2, IN_HC = 3 };
 enum OutKind { OUT_C = 0, OUT_R = 1, OUT_P = 2, OUT_HC = 3 };
 enum PreKind { PRE_NONE = 0, PRE_HERM_EVEN = 1, PRE_HERM_ODD = 2 };
-enum PostKind { POST_NONE = 0, POST_SPLIT = 1, POST_PAIR = 2 };
+enum PostKind { POST_NONE = 0, POST_SPLIT = 1, POST_PAIR = 2, POST_SPLIT4 = 3 };
+// POST_SPLIT4: the real split fused into the second pass of a four-step core:
+// the lines of a CTA come in pairs (row r, row N1 - r) of the transform's
+// N1 x N2 layout (rows 0 and N1/2 paired with themselves), and the epilogue
+// writes X[k], X[M - k] (k = r + N1 u) as halfcomplex.  Line l is row slot
+// l mod bn0 (bn0 = N1 + (1 or 2)) of transform l / bn0; the input offset of a
+// slot is its row times bsi0
 
 struct CoreDesc {
     int M;    // logical complex length of the core transform
@@ -106,6 +112,9 @@ struct IODesc {
     int keep0_rows;  // lines per transform: 1 (one-pass core) or N1 (four-step second pass)
     // per-line byte offsets (device arrays) replacing the batch dims when set
     const long long *loff_in, *loff_out;
+    // POST_SPLIT4 (when split_N1 != 0): the real-split twiddles exp(-2 pi i k / 2M), k <= M, and N1
+    const void *split_tw;
+    int split_N1;
 };
 
 // one group of the persistent work list: a core, a line set, its block count;

@@ -8,6 +8,11 @@ pytestmark = pytest.mark.gpu
 F64_TOL = 1e-12
 
 
+def _dtype_code(dtype):
+    from impulse_gb300 import _lib as L
+    return L.IG_F64 if dtype == np.float64 else L.IG_F32
+
+
 def f32_tol(n):
     return 1e-6 * max(1.0, np.log2(max(n, 2)))
 
@@ -61,3 +66,22 @@ def test_c2c_large_strided_axis(engine, oracle_lib):
     x = rng.uniform(-1, 1, (32768, 4)) + 1j * rng.uniform(-1, 1, (32768, 4))
     got = F.c2c(x, [0], True, 1.0)
     assert oracle_lib.rel_l2(got, oracle_lib.c2c(x, [0])) < F64_TOL
+
+
+@pytest.mark.parametrize("n,dist", [(18144, 18144 + 8), (30800, 30800 + 7), (20000, 20000)])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_halfcomplex_fourstep_gaps(engine, oracle_lib, n, dist, dtype):
+    """Even four-step lengths whose real split is fused into the row pass,
+    written as halfcomplex into lines `dist` apart (gaps left untouched)."""
+    from impulse_gb300 import _lib as L
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(n + dist)
+    batch = 5
+    x = rng.standard_normal((batch, dist)).astype(dtype)
+    h = x.copy()
+    plan = F.FFTPlanReal(n, _dtype_code(dtype))
+    L.check(L.load().ig_rfft_exec_batch(plan.pocket, h.ctypes.data, batch, dist, 1, 0.5))
+    tol = F64_TOL if dtype == np.float64 else f32_tol(n) * 2
+    want = oracle_lib.rfft_hc(x[:, :n].astype(np.float64), True, 0.5)
+    assert oracle_lib.rel_l2(h[:, :n], want) < tol, (n, dist, oracle_lib.rel_l2(h[:, :n], want))
+    assert np.array_equal(h[:, n:], x[:, n:])
