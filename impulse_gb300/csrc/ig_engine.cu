@@ -272,8 +272,10 @@ static void set_fct_parts(IODesc &io)
 // variants compile the common layouts without per-element runtime checks)
 static int choose_layout(Arith a, const IODesc &io)
 {
-    if (a == A_F64 || io.keep0) return LAY_GEN;
+    if (a == A_F64) return LAY_GEN;
     const bool plain = !io.conj_in && !io.conj_out && !io.real_out && io.pre == PRE_NONE;
+    // the twiddle / table variant also keeps Rader's unit 0 (keep0) before the product
+    if (io.keep0 && !(io.tw4 || io.mul)) return LAY_GEN;
     if (io.tw4 || io.mul)
         return (plain && !io.pair && io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C) ? LAY_TW
                                                                                                           : LAY_GEN;
@@ -2870,8 +2872,9 @@ int ig_autotune(int dtype, size_t length, int kind, double *best_ms)
                 }
         } else {
             const long long L = base->d.L;
-            // long single-CTA cores without double buffering also try four-step splits
-            if (!base->d.blue && base->d.E == 16 && !base->d.db) {
+            // long single-CTA cores also try four-step splits (fewer lines per SM
+            // in shared memory against a second pass)
+            if (!base->d.blue && L > 2048) {
                 for (long long d = 2; d * d <= M; ++d)
                     if (M % d == 0 && fits_smem(a, d, d) && fits_smem(a, M / d, M / d)) {
                         std::vector<int> r1, r2;
