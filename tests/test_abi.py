@@ -83,3 +83,14 @@ def test_api_mirror_raises_like_reference(lib):
     from impulse_gb300 import _lib as L
     with pytest.raises(L.FFTError):
         F.FFTPlanComplex(0)
+
+
+def test_device_api_rejects_host_tensors(lib):
+    """The device-resident mirror takes CUDA tensors only; host data goes through impulse_gb300.fft."""
+    torch = pytest.importorskip("torch")
+    from impulse_gb300 import device as D
+    x = torch.zeros(8, dtype=torch.float64)
+    with pytest.raises(TypeError):
+        D.tensor_rfft_packed(x)
+    with pytest.raises(TypeError):
+        D.DataDesc(x, (8,))
