@@ -57,6 +57,12 @@ __device__ __forceinline__ long long qdiv(long long n, long long d, FastDiv f)
     return n < 0x7fffffffLL ? (long long)fdiv((unsigned)n, f) : n / d;
 }
 
+// streaming global accesses of line data: each element is read and written
+// once, so it goes through L1 evict-first and leaves the cache to the
+// twiddle tables
+template <class V> __device__ __forceinline__ V ldg_s(const char *p) { return __ldcs(reinterpret_cast<const V *>(p)); }
+template <class V> __device__ __forceinline__ void stg_s(char *p, V v) { __stcs(reinterpret_cast<V *>(p), v); }
+
 // POST_SPLIT4 row order: slot j of a transform's N1 rows holds row
 // r = j / 2 + 1 (j even) or N1 - r (j odd) while r < N1 / 2, then row 0 twice
 // and, for even N1, row N1 / 2 twice
@@ -337,23 +343,23 @@ template <class S, class S2>
 __device__ __forceinline__ void load_unit(const IODesc &io, const char *base, int u, S &re, S &im)
 {
     if (io.in_kind == IN_C) {
-        S2 z = *reinterpret_cast<const S2 *>(base + (long long)u * io.is);
+        S2 z = ldg_s<S2>(base + (long long)u * io.is);
         re = z.x;
         im = z.y;
     } else if (io.in_kind == IN_R) {
-        re = *reinterpret_cast<const S *>(base + (long long)u * io.is);
+        re = ldg_s<S>(base + (long long)u * io.is);
         im = S(0);
     } else if (io.in_kind == IN_P) {
         const char *p = base + (long long)u * io.is;
-        re = *reinterpret_cast<const S *>(p);
-        im = *reinterpret_cast<const S *>(p + io.ps_in);
+        re = ldg_s<S>(p);
+        im = ldg_s<S>(p + io.ps_in);
     } else {  // IN_HC: unit 0 = (r0, 0); unit k = (r_{2k-1}, r_{2k}); even N: last = (r_{N-1}, 0)
         if (u == 0) {
-            re = *reinterpret_cast<const S *>(base);
+            re = ldg_s<S>(base);
             im = S(0);
         } else {
-            re = *reinterpret_cast<const S *>(base + (2 * (long long)u - 1) * io.is);
-            im = (2 * (long long)u < io.nreal) ? *reinterpret_cast<const S *>(base + (2 * (long long)u) * io.is) : S(0);
+            re = ldg_s<S>(base + (2 * (long long)u - 1) * io.is);
+            im = (2 * (long long)u < io.nreal) ? ldg_s<S>(base + (2 * (long long)u) * io.is) : S(0);
         }
     }
 }
@@ -368,18 +374,18 @@ __device__ __forceinline__ void store_unit(const IODesc &io, char *base, int u, 
         S2 o;
         o.x = sc.apply(z.r, esc);
         o.y = sc.apply(z.i, esc);
-        *reinterpret_cast<S2 *>(base + (long long)u * io.os) = o;
+        stg_s<S2>(base + (long long)u * io.os, o);
     } else if (io.out_kind == OUT_R) {
-        *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, esc);
+        stg_s<S>(base + (long long)u * io.os, sc.apply(z.r, esc));
     } else if (io.out_kind == OUT_P) {
         char *p = base + (long long)u * io.os;
-        *reinterpret_cast<S *>(p) = sc.apply(z.r, esc);
-        *reinterpret_cast<S *>(p + io.ps_out) = sc.apply(z.i, esc);
+        stg_s<S>(p, sc.apply(z.r, esc));
+        stg_s<S>(p + io.ps_out, sc.apply(z.i, esc));
     } else {  // OUT_HC
-        if (u == 0) *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
+        if (u == 0) stg_s<S>(base, sc.apply(z.r, esc));
         else {
-            *reinterpret_cast<S *>(base + (2 * (long long)u - 1) * io.os) = sc.apply(z.r, esc);
-            if (2 * (long long)u < io.nreal) *reinterpret_cast<S *>(base + (2 * (long long)u) * io.os) = sc.apply(z.i, esc);
+            stg_s<S>(base + (2 * (long long)u - 1) * io.os, sc.apply(z.r, esc));
+            if (2 * (long long)u < io.nreal) stg_s<S>(base + (2 * (long long)u) * io.os, sc.apply(z.i, esc));
         }
     }
 }
@@ -491,7 +497,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
 #pragma unroll
                     for (int c = 0; c < CH; ++c) {
                         const int u = u0 + c * tpl;
-                        if (u < cnt) v[c] = *reinterpret_cast<const S2 *>(base + (long long)u * is);
+                        if (u < cnt) v[c] = ldg_s<S2>(base + (long long)u * is);
                     }
 #pragma unroll
                     for (int c = 0; c < CH; ++c) {
@@ -517,8 +523,8 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                         const int u = u0 + c * tpl;
                         va[c] = vb[c] = S(0);
                         if (u < cnt) {
-                            va[c] = *reinterpret_cast<const S *>(base + (long long)u * is);
-                            if (has_b) vb[c] = *reinterpret_cast<const S *>(base_b + (long long)u * is);
+                            va[c] = ldg_s<S>(base + (long long)u * is);
+                            if (has_b) vb[c] = ldg_s<S>(base_b + (long long)u * is);
                         }
                     }
 #pragma unroll
@@ -787,13 +793,13 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                         const cx<T> E = chalf(za + zc), D = chalf(za - zc);
                         const cx<T> X = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[kk]));
                         if (kk == 0) {
-                            *reinterpret_cast<S *>(base) = sc.apply(X.r, ec);
+                            stg_s<S>(base, sc.apply(X.r, ec));
                         } else if (kk == Mt) {
-                            *reinterpret_cast<S *>(base + (2 * Mt - 1) * io.os) = sc.apply(X.r, ec);
+                            stg_s<S>(base + (2 * Mt - 1) * io.os, sc.apply(X.r, ec));
                         } else {
                             char *p = base + (2 * kk - 1) * io.os;
-                            *reinterpret_cast<S *>(p) = sc.apply(X.r, ec);
-                            *reinterpret_cast<S *>(p + io.os) = sc.apply(X.i, ec);
+                            stg_s<S>(p, sc.apply(X.r, ec));
+                            stg_s<S>(p + io.os, sc.apply(X.i, ec));
                         }
                     };
                     split_store(a, b, k);
@@ -838,7 +844,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     S2 o;
                     o.x = sc.apply(z.r, esc);
                     o.y = sc.apply(z.i, esc);
-                    *reinterpret_cast<S2 *>(base + (long long)u * os) = o;
+                    stg_s<S2>(base + (long long)u * os, o);
                 }
                 return;
             }
@@ -848,11 +854,11 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 for (int u = t2; u < cnt; u += tpl) {
                     const cx<T> z = sget(line + sp(u, pad));
                     if (u == 0) {
-                        *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
+                        stg_s<S>(base, sc.apply(z.r, esc));
                     } else {
                         char *p = base + (2 * (long long)u - 1) * os;
-                        *reinterpret_cast<S *>(p) = sc.apply(z.r, esc);
-                        if (2 * (long long)u < nreal) *reinterpret_cast<S *>(p + os) = sc.apply(z.i, esc);
+                        stg_s<S>(p, sc.apply(z.r, esc));
+                        if (2 * (long long)u < nreal) stg_s<S>(p + os, sc.apply(z.i, esc));
                     }
                 }
                 return;
@@ -864,15 +870,15 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     const cx<T> za = u == 0 ? cx<T>{z0.r, zero} : sget(line + sp(u, pad));
                     const cx<T> zb = u == 0 ? cx<T>{z0.i, zero} : sget(line + sp(M - u, pad));
                     if (u == 0) {
-                        *reinterpret_cast<S *>(base) = sc.apply(za.r, esc);
-                        if (has_b) *reinterpret_cast<S *>(base + po) = sc.apply(zb.r, escb);
+                        stg_s<S>(base, sc.apply(za.r, esc));
+                        if (has_b) stg_s<S>(base + po, sc.apply(zb.r, escb));
                     } else {
                         char *p = base + (2 * (long long)u - 1) * os;
-                        *reinterpret_cast<S *>(p) = sc.apply(za.r, esc);
-                        if (has_b) *reinterpret_cast<S *>(p + po) = sc.apply(zb.r, escb);
+                        stg_s<S>(p, sc.apply(za.r, esc));
+                        if (has_b) stg_s<S>(p + po, sc.apply(zb.r, escb));
                         if (2 * (long long)u < nreal) {
-                            *reinterpret_cast<S *>(p + os) = sc.apply(za.i, esc);
-                            if (has_b) *reinterpret_cast<S *>(p + os + po) = sc.apply(zb.i, escb);
+                            stg_s<S>(p + os, sc.apply(za.i, esc));
+                            if (has_b) stg_s<S>(p + os + po, sc.apply(zb.i, escb));
                         }
                     }
                 }
@@ -883,8 +889,8 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     if (io.out_kind == OUT_R) {
                         cx<T> z = sget(line + sp(u, pad));
                         if (cc) z.i = -z.i;
-                        *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, esc);
-                        if (has_b) *reinterpret_cast<S *>(base + io.pair_out + (long long)u * io.os) = sc.apply(z.i, escb);
+                        stg_s<S>(base + (long long)u * io.os, sc.apply(z.r, esc));
+                        if (has_b) stg_s<S>(base + io.pair_out + (long long)u * io.os, sc.apply(z.i, escb));
                     } else {
                         cx<T> za = u == 0 ? cx<T>{z0.r, zero} : sget(line + sp(u, pad));
                         cx<T> zb = u == 0 ? cx<T>{z0.i, zero} : sget(line + sp(M - u, pad));
@@ -1016,19 +1022,19 @@ template <class S, class S2>
 __device__ __forceinline__ void read_unit(const IODesc &io, const char *base, long long u, double &re, double &im)
 {
     if (io.in_kind == IN_C) {
-        S2 z = *reinterpret_cast<const S2 *>(base + u * io.is);
+        S2 z = ldg_s<S2>(base + u * io.is);
         re = z.x; im = z.y;
     } else if (io.in_kind == IN_R) {
-        re = *reinterpret_cast<const S *>(base + u * io.is);
+        re = ldg_s<S>(base + u * io.is);
         im = 0;
     } else if (io.in_kind == IN_P) {
-        re = *reinterpret_cast<const S *>(base + u * io.is);
-        im = *reinterpret_cast<const S *>(base + u * io.is + io.ps_in);
+        re = ldg_s<S>(base + u * io.is);
+        im = ldg_s<S>(base + u * io.is + io.ps_in);
     } else {
-        if (u == 0) { re = *reinterpret_cast<const S *>(base); im = 0; }
+        if (u == 0) { re = ldg_s<S>(base); im = 0; }
         else {
-            re = *reinterpret_cast<const S *>(base + (2 * u - 1) * io.is);
-            im = (2 * u < io.nreal) ? (double)*reinterpret_cast<const S *>(base + (2 * u) * io.is) : 0.0;
+            re = ldg_s<S>(base + (2 * u - 1) * io.is);
+            im = (2 * u < io.nreal) ? (double)ldg_s<S>(base + (2 * u) * io.is) : 0.0;
         }
     }
     if (io.conj_in) im = -im;
@@ -1166,17 +1172,17 @@ __global__ void k_scatter(const __grid_constant__ IODesc io, const __grid_consta
             S2 o;
             o.x = sc.apply(z.r, esc);
             o.y = sc.apply(z.i, esc);
-            *reinterpret_cast<S2 *>(base + u * io.os) = o;
+            stg_s<S2>(base + u * io.os, o);
         } else if (io.out_kind == OUT_R) {
-            *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
+            stg_s<S>(base + u * io.os, sc.apply(z.r, esc));
         } else if (io.out_kind == OUT_P) {
-            *reinterpret_cast<S *>(base + u * io.os) = sc.apply(z.r, esc);
-            *reinterpret_cast<S *>(base + u * io.os + io.ps_out) = sc.apply(z.i, esc);
+            stg_s<S>(base + u * io.os, sc.apply(z.r, esc));
+            stg_s<S>(base + u * io.os + io.ps_out, sc.apply(z.i, esc));
         } else {
-            if (u == 0) *reinterpret_cast<S *>(base) = sc.apply(z.r, esc);
+            if (u == 0) stg_s<S>(base, sc.apply(z.r, esc));
             else {
-                *reinterpret_cast<S *>(base + (2 * u - 1) * io.os) = sc.apply(z.r, esc);
-                if (2 * u < io.nreal) *reinterpret_cast<S *>(base + (2 * u) * io.os) = sc.apply(z.i, esc);
+                stg_s<S>(base + (2 * u - 1) * io.os, sc.apply(z.r, esc));
+                if (2 * u < io.nreal) stg_s<S>(base + (2 * u) * io.os, sc.apply(z.i, esc));
             }
         }
     }
@@ -1319,8 +1325,8 @@ __global__ void k_scatter_pair(const __grid_constant__ IODesc io, const __grid_c
         };
         if (io.out_kind == OUT_R) {
             cx<T> z = fetch(u);
-            *reinterpret_cast<S *>(base + (long long)u * io.os) = sc.apply(z.r, ea);
-            if (has_b) *reinterpret_cast<S *>(base + io.pair_out + (long long)u * io.os) = sc.apply(z.i, eb);
+            stg_s<S>(base + (long long)u * io.os, sc.apply(z.r, ea));
+            if (has_b) stg_s<S>(base + io.pair_out + (long long)u * io.os, sc.apply(z.i, eb));
             continue;
         }
         cx<T> za, zb;
@@ -1364,7 +1370,7 @@ __global__ void k_r2r_pre(const __grid_constant__ IODesc io, const __grid_consta
          idx += (long long)gridDim.x * blockDim.x) {
         const long long l = qdiv(idx, d.L2, d.fL2), m = idx - l * d.L2;
         const char *base = io.in + line_off(io, l, false);
-        auto X = [&](long long j) { return (double)*reinterpret_cast<const S *>(base + j * io.is); };
+        auto X = [&](long long j) { return (double)ldg_s<S>(base + j * io.is); };
         if (d.mode == R2R_COPY || d.mode == R2R_HARTLEY) {
             double v = X(m);
             if (d.neg_even && m >= 2 && (m & 1) == 0) v = -v;
@@ -1502,8 +1508,8 @@ __global__ void k_hartley_fold(const typename Traits<T>::S2 *__restrict__ X, cha
             ro += ri * h.sout[dd];
         }
         const typename Traits<T>::S2 v = X[e];
-        *reinterpret_cast<S *>(out + o) = v.x + v.y;
-        *reinterpret_cast<S *>(out + ro) = v.x - v.y;
+        stg_s<S>(out + o, v.x + v.y);
+        stg_s<S>(out + ro, v.x - v.y);
     }
 }
 
