@@ -408,8 +408,8 @@ static void build_stockham(Core &c, long long L, const std::vector<int> &rad)
         off += ns * (rad[s] - 1);
         ns *= rad[s];
     }
-    // double-float stage twiddles are stored packed (32 bytes an entry)
-    const size_t twb = c.a == A_DF ? 32 : slot_bytes(c.a);
+    // one complex per twiddle (double-float: (wr.h, wi.h, wr.l, wi.l), 16 bytes)
+    const size_t twb = slot_bytes(c.a);
     c.d.neg1 = -1.0f;
     void *tw = c.alloc(std::max<long long>(off, 1) * twb);
     c.d.tw = tw;
@@ -625,7 +625,7 @@ static std::shared_ptr<Core> make_core(Arith a, long long M, bool real_tw)
         c->wlo = wlo;
         // the full twiddle table when it stays modest (one table read per element)
         if (M <= (1LL << 22)) {
-            const size_t twb = a == A_DF ? 32 : slot_bytes(a);
+            const size_t twb = slot_bytes(a);
             void *tab = c->alloc((size_t)M * twb);
             cudaError_t e = a == A_F32 ? Launch<TagF32>::tw4_table(tab, c->N1, c->N2)
                           : a == A_DF  ? Launch<TagDF>::tw4_table(tab, c->N1, c->N2)

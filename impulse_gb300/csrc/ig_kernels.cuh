@@ -122,7 +122,7 @@ __device__ __forceinline__ int sp(int i, int pad) { return i + (i >> pad); }
 
 // Butterfly arithmetic of the stages: plain complexes for float / double,
 // packed pairs (ig_pdf.cuh) for double-float, whose stage twiddle table
-// holds the packed form (32 bytes an entry).
+// holds (wr.h, wi.h, wr.l, wi.l), 16 bytes an entry, paired in registers.
 template <class T> struct Bfly {
     using V = cx<T>;
     using W = cx<T>;
@@ -136,7 +136,7 @@ template <> struct Bfly<df> {
     using W = ptw;
     static __device__ __forceinline__ V ld(const cx<df> *p) { return pld(p); }
     static __device__ __forceinline__ void st(cx<df> *p, V v) { pst(p, prenorm(v)); }
-    static __device__ __forceinline__ V tw(V a, const W *w, const CoreDesc &P) { return pmulw(a, w, bcast(P.neg1)); }
+    static __device__ __forceinline__ V tw(V a, const W *w, const CoreDesc &P) { return pmulw(a, w, P.neg1); }
     template <int R> static __device__ __forceinline__ void dft(V *v) { pdft<R>(v); }
 };
 
@@ -147,7 +147,7 @@ __device__ __forceinline__ cx<T> tw_apply(cx<T> z, const typename Bfly<T>::W *w,
     if constexpr (std::is_same<T, df>::value) {
         pcx a = to_p(z);
         if (!fwd) a = pconj(a);
-        a = pmulw(a, w, bcast(P.neg1));
+        a = pmulw(a, w, P.neg1);
         if (!fwd) a = pconj(a);
         return from_p(a);
     } else {
@@ -1688,9 +1688,8 @@ template <class T> __global__ void k_gen_stage_tw(typename Bfly<T>::W *tw, int R
     double2 v = exp2pi_frac((unsigned long long)m * k, (unsigned long long)ns * R);
     v.y = -v.y;
     if constexpr (std::is_same<T, df>::value) {
-        // packed: (wr, wr), (-wi, wi) for the high and the low parts
         const cx<df> w = to_arith<df>(v);
-        tw[e] = ptw{pk(w.r.h, w.r.h), pk(-w.i.h, w.i.h), pk(w.r.l, w.r.l), pk(-w.i.l, w.i.l)};
+        tw[e] = ptw{w.r.h, w.i.h, w.r.l, w.i.l};
     } else {
         tw[e] = to_arith<T>(v);
     }
@@ -1723,7 +1722,7 @@ template <class T> __global__ void k_gen_tw4(typename Bfly<T>::W *tab, long long
     v.y = -v.y;
     if constexpr (std::is_same<T, df>::value) {
         const cx<df> w = to_arith<df>(v);
-        tab[e] = ptw{pk(w.r.h, w.r.h), pk(-w.i.h, w.i.h), pk(w.r.l, w.r.l), pk(-w.i.l, w.i.l)};
+        tab[e] = ptw{w.r.h, w.i.h, w.r.l, w.i.l};
     } else {
         tab[e] = to_arith<T>(v);
     }

@@ -174,21 +174,22 @@ IGP pcx pcmul(pcx a, cx<df> w)
     return pmulw(a, bcast(w.r.h), pk(-w.i.h, w.i.h), bcast(w.r.l), pk(-w.i.l, w.i.l), bcast(-w.r.h),
                  pk(w.i.h, -w.i.h));
 }
-// stage twiddle in packed form: (W1h, W2h, W1l, W2l), 32 bytes.  The
-// negated high pairs are formed with a product by `neg` = (-1, -1), a value
-// the kernels read from their parameters: a negation the compiler can see
-// would let it cancel the FMA error term against the product it was taken
-// from.
+// stage twiddle w = (wr, wi) as (wr.h, wi.h, wr.l, wi.l), 16 bytes (half the
+// cache footprint of the pairs pmulw takes).  The pairs are formed in
+// registers; the negations are products by `neg1` = -1, a value the kernels
+// read from their parameters: a negation the compiler can see would let it
+// cancel the FMA error term against the product it was taken from.
 struct ptw {
-    f2p W1h, W2h, W1l, W2l;
+    float rh, ih, rl, il;
 };
 #if defined(__CUDACC__)
-IGP pcx pmulw(pcx a, const ptw *w, f2p neg)
+IGP pcx pmulw(pcx a, const ptw *w, float neg1)
 {
-    const ulonglong2 *q = reinterpret_cast<const ulonglong2 *>(w);
-    const ulonglong2 q0 = q[0], q1 = q[1];
-    const f2p W1h{q0.x}, W2h{q0.y};
-    return pmulw(a, W1h, W2h, f2p{q1.x}, f2p{q1.y}, W1h * neg, W2h * neg);
+    const float4 q = *reinterpret_cast<const float4 *>(w);
+    const f2p m = pk(neg1, 1.0f), nn = pk(neg1, neg1);
+    const f2p W1h = pk(q.x, q.x), W1l = pk(q.z, q.z);
+    const f2p W2h = pk(q.y, q.y) * m, W2l = pk(q.w, q.w) * m;  // (-wi, wi)
+    return pmulw(a, W1h, W2h, W1l, W2l, W1h * nn, W2h * nn);
 }
 #endif
 
