@@ -222,13 +222,25 @@ __device__ __forceinline__ void stage_db(const cx<T> *src, cx<T> *dst, int LS2, 
     if (g >= nl) return;
     const cx<T> *in = src + (size_t)g * LS2;
     cx<T> *out = dst + (size_t)g * LS2;
+    // when the element step (nr for the reads, ns for the writes) is a multiple
+    // of the padding period, sp(x + m step) = sp(x) + m sp(step): one add per
+    // element instead of the shift-and-add of each padded index
+    const int pmask = pad >= 31 ? 0 : (1 << pad) - 1;
+    const bool lin_ld = (nr & pmask) == 0, lin_st = (ns & pmask) == 0;
+    const int nrp = sp(nr, pad), nsp = sp(ns, pad);
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
         const int j = t + i * tpl;
         if (j < nr) {
             V v[R];
+            if (lin_ld) {
+                const cx<T> *p0 = in + sp(j, pad);
 #pragma unroll
-            for (int m = 0; m < R; ++m) v[m] = B::ld(in + sp(j + m * nr, pad));
+                for (int m = 0; m < R; ++m) v[m] = B::ld(p0 + m * nrp);
+            } else {
+#pragma unroll
+                for (int m = 0; m < R; ++m) v[m] = B::ld(in + sp(j + m * nr, pad));
+            }
             const int q = (int)fdiv((unsigned)j, fns), k = j - q * ns;
             if (k) {
                 const typename B::W *twk = tw + k * (R - 1) - 1;
@@ -237,8 +249,14 @@ __device__ __forceinline__ void stage_db(const cx<T> *src, cx<T> *dst, int LS2, 
             }
             B::template dft<R>(v);
             const int base = q * ns * R + k;
+            if (lin_st) {
+                cx<T> *p0 = out + sp(base, pad);
 #pragma unroll
-            for (int m = 0; m < R; ++m) B::st(out + sp(base + m * ns, pad), v[m]);
+                for (int m = 0; m < R; ++m) B::st(p0 + m * nsp, v[m]);
+            } else {
+#pragma unroll
+                for (int m = 0; m < R; ++m) B::st(out + sp(base + m * ns, pad), v[m]);
+            }
         }
         asm volatile("" ::: "memory");
     }
