@@ -742,18 +742,37 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         // E_k = (Z[k] + conj(Z[M-k]))/2, O_k = -i (Z[k] - conj(Z[M-k]))/2, w = e^{-2 pi i/2M};
         // thread-owned slot pairs (k, M-k), slot M receives X[M]
         const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
-        for (int k = t; k <= M / 2; k += tpl) {
-            const int k2 = M - k;
-            cx<T> a = sget(myline + sp(k, pad)), b = sget(myline + sp(k == 0 ? 0 : k2, pad));
-            {
-                cx<T> zb = conjx(b);
-                cx<T> E = chalf(a + zb), D = chalf(a - zb);
-                sput(myline + sp(k, pad), crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k])));
+        if constexpr (std::is_same<T, df>::value) {
+            // packed pairs (re, im): X = (a + conj b)/2 + w (-i) (a - conj b)/2
+            const f2p half = bcast(0.5f), cj = pk(1.0f, -1.0f);
+            for (int k = t; k <= M / 2; k += tpl) {
+                const int k2 = M - k;
+                const pcx a = pld((myline + sp(k, pad))), b = pld((myline + sp(k == 0 ? 0 : k2, pad)));
+                {
+                    const pcx zb = plane(b, cj);
+                    const pcx E = plane(a + zb, half), D = plane(a - zb, half);
+                    pst((myline + sp(k, pad)), prenorm(E + pmulw_cx(prot<true>(D), rtw + k, P.neg1)));
+                }
+                if (k2 != k) {
+                    const pcx za = plane(a, cj);
+                    const pcx E = plane(b + za, half), D = plane(b - za, half);
+                    pst((myline + sp(k2, pad)), prenorm(E + pmulw_cx(prot<true>(D), rtw + k2, P.neg1)));
+                }
             }
-            if (k2 != k) {
-                cx<T> zb = conjx(a);
-                cx<T> E = chalf(b + zb), D = chalf(b - zb);
-                sput(myline + sp(k2, pad), crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k2])));
+        } else {
+            for (int k = t; k <= M / 2; k += tpl) {
+                const int k2 = M - k;
+                cx<T> a = sget(myline + sp(k, pad)), b = sget(myline + sp(k == 0 ? 0 : k2, pad));
+                {
+                    cx<T> zb = conjx(b);
+                    cx<T> E = chalf(a + zb), D = chalf(a - zb);
+                    sput(myline + sp(k, pad), crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k])));
+                }
+                if (k2 != k) {
+                    cx<T> zb = conjx(a);
+                    cx<T> E = chalf(b + zb), D = chalf(b - zb);
+                    sput(myline + sp(k2, pad), crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k2])));
+                }
             }
         }
     }
@@ -761,12 +780,22 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     if (post_pair && g < nl) {
         // Z = FFT(a + i b) -> A[k] = (Z[k] + conj(Z[M-k]))/2 at slot k,
         // B[k] = -i (Z[k] - conj(Z[M-k]))/2 at slot M-k; slot 0 keeps (A[0], B[0])
-        for (int k = 1 + t; 2 * k < M + 1; k += tpl) {
-            const int k2 = M - k;
-            cx<T> a = sget(myline + sp(k, pad)), b = conjx(sget(myline + sp(k2, pad)));
-            cx<T> A = chalf(a + b), D = chalf(a - b);
-            sput(myline + sp(k, pad), crenorm(A));
-            sput(myline + sp(k2, pad), crenorm(cx<T>{D.i, -D.r}));
+        if constexpr (std::is_same<T, df>::value) {
+            const f2p half = bcast(0.5f), cj = pk(1.0f, -1.0f);
+            for (int k = 1 + t; 2 * k < M + 1; k += tpl) {
+                const int k2 = M - k;
+                const pcx a = pld((myline + sp(k, pad))), b = plane(pld((myline + sp(k2, pad))), cj);
+                pst((myline + sp(k, pad)), prenorm(plane(a + b, half)));
+                pst((myline + sp(k2, pad)), prenorm(prot<true>(plane(a - b, half))));
+            }
+        } else {
+            for (int k = 1 + t; 2 * k < M + 1; k += tpl) {
+                const int k2 = M - k;
+                cx<T> a = sget(myline + sp(k, pad)), b = conjx(sget(myline + sp(k2, pad)));
+                cx<T> A = chalf(a + b), D = chalf(a - b);
+                sput(myline + sp(k, pad), crenorm(A));
+                sput(myline + sp(k2, pad), crenorm(cx<T>{D.i, -D.r}));
+            }
         }
     }
     if (post_pair) __syncthreads();

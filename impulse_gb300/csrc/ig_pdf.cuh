@@ -191,6 +191,15 @@ IGP pcx pmulw(pcx a, const ptw *w, float neg1)
     const f2p W2h = pk(q.y, q.y) * m, W2l = pk(q.w, q.w) * m;  // (-wi, wi)
     return pmulw(a, W1h, W2h, W1l, W2l, W1h * nn, W2h * nn);
 }
+// a * w, w a cx<df> in memory (r.h, r.l, i.h, i.l), pairs formed as for ptw
+IGP pcx pmulw_cx(pcx a, const cx<df> *w, float neg1)
+{
+    const float4 q = *reinterpret_cast<const float4 *>(w);
+    const f2p m = pk(neg1, 1.0f), nn = pk(neg1, neg1);
+    const f2p W1h = pk(q.x, q.x), W1l = pk(q.y, q.y);
+    const f2p W2h = pk(q.z, q.z) * m, W2l = pk(q.w, q.w) * m;  // (-wi, wi)
+    return pmulw(a, W1h, W2h, W1l, W2l, W1h * nn, W2h * nn);
+}
 #endif
 
 // multiply by the constant c + i s (double constants split into double-float)
