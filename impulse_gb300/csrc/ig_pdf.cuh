@@ -146,6 +146,31 @@ IGP pcx pscale(pcx a, float ch, float cl)
     const f2p h = e - np;             // p + e
     return pcx{h, e - (h + np)};      // e - (h - p)
 }
+// unrenormalised product a (ch + cl): (-np, e) with np = -round(a.h ch) and e
+// its exact error plus the low terms (the renormalisation of pscale is left
+// to the lazy add that consumes it)
+IGP pcx pprod(pcx a, float ch, float cl)
+{
+    const f2p Kh = bcast(ch), Kl = bcast(cl), nKh = bcast(-ch);
+    const f2p np = a.h * nKh;
+    f2p e = pfma(a.h, Kh, np);
+    e = pfma(a.h, Kl, e);
+    e = pfma(a.l, Kh, e);
+    return pcx{bcast(0.0f) - np, e};
+}
+// T + a (ch + cl): the product's high part enters the TwoSum directly and its
+// error terms join the low parts (lazy add, no renormalisation of the product)
+IGP pcx pacc(pcx T, pcx a, float ch, float cl)
+{
+    const f2p Kh = bcast(ch), Kl = bcast(cl), nKh = bcast(-ch);
+    const f2p np = a.h * nKh;         // -p
+    f2p e = pfma(a.h, Kh, np);        // a.h ch - p, exact
+    e = pfma(a.h, Kl, e);
+    e = pfma(a.l, Kh, e);
+    const f2p s = T.h - np, bb = s - T.h;              // TwoSum(T.h, p)
+    const f2p err = (T.h - (s - bb)) - (np + bb);
+    return pcx{s, err + (T.l + e)};
+}
 // a * w with w = (wr, wi) given as the pairs W1 = (wr, wr) and W2 = (-wi, wi)
 // (high and low parts) and the negated high pairs nW1 = -W1h, nW2 = -W2h:
 // lanes (re, im) = a (wr, wr) + (a.im, a.re) (-wi, wi).  The lane sequence is
@@ -295,9 +320,8 @@ template <int P> IGP void pdft_odd(pcx *v)
             const int jj = j <= H ? j : P - j;
             const df ck = df_const(odd_cos(P, jj));
             const df sk = df_const(j <= H ? odd_sin(P, jj) : -odd_sin(P, jj));
-            T = T + pscale(a[k - 1], ck.h, ck.l);
-            const pcx u = pscale(b[k - 1], sk.h, sk.l);
-            U = k == 1 ? u : U + u;
+            T = pacc(T, a[k - 1], ck.h, ck.l);
+            U = k == 1 ? pprod(b[k - 1], sk.h, sk.l) : pacc(U, b[k - 1], sk.h, sk.l);
         }
         // forward: V_q = T - i U, V_{P-q} = T + i U
         const pcx iU = prot<true>(U);
