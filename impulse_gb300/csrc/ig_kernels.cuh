@@ -136,7 +136,8 @@ template <> struct Bfly<df> {
     using W = ptw;
     static __device__ __forceinline__ V ld(const cx<df> *p) { return pld(p); }
     static __device__ __forceinline__ void st(cx<df> *p, V v) { pst(p, prenorm(v)); }
-    static __device__ __forceinline__ V tw(V a, const W *w, const CoreDesc &P) { return pmulw(a, w, P.neg1); }
+    // the stage butterflies add twiddled inputs lazily: products stay unrenormalised
+    static __device__ __forceinline__ V tw(V a, const W *w, const CoreDesc &P) { return pmulw<false>(a, w, P.neg1); }
     template <int R> static __device__ __forceinline__ void dft(V *v) { pdft<R>(v); }
 };
 
@@ -751,12 +752,12 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 {
                     const pcx zb = plane(b, cj);
                     const pcx E = plane(a + zb, half), D = plane(a - zb, half);
-                    pst((myline + sp(k, pad)), prenorm(E + pmulw_cx(prot<true>(D), rtw + k, P.neg1)));
+                    pst((myline + sp(k, pad)), prenorm(E + pmulw_cx<false>(prot<true>(D), rtw + k, P.neg1)));
                 }
                 if (k2 != k) {
                     const pcx za = plane(a, cj);
                     const pcx E = plane(b + za, half), D = plane(b - za, half);
-                    pst((myline + sp(k2, pad)), prenorm(E + pmulw_cx(prot<true>(D), rtw + k2, P.neg1)));
+                    pst((myline + sp(k2, pad)), prenorm(E + pmulw_cx<false>(prot<true>(D), rtw + k2, P.neg1)));
                 }
             }
         } else {

@@ -176,7 +176,9 @@ IGP pcx pacc(pcx T, pcx a, float ch, float cl)
 // lanes (re, im) = a (wr, wr) + (a.im, a.re) (-wi, wi).  The lane sequence is
 // the scalar df_mul_sub / df_mul_add one with the two high products formed
 // negated (-p = a (-w), exactly) and the FMA error terms taken against them,
-// so that no product is negated after the fact.
+// so that no product is negated after the fact.  NORM = false returns the
+// unrenormalised pair (s, T) for a lazy add to consume.
+template <bool NORM = true>
 IGP pcx pmulw(pcx a, f2p W1h, f2p W2h, f2p W1l, f2p W2l, f2p nW1h, f2p nW2h)
 {
     const f2p ash = swp(a.h), asl = swp(a.l);
@@ -190,6 +192,7 @@ IGP pcx pmulw(pcx a, f2p W1h, f2p W2h, f2p W1l, f2p W2l, f2p nW1h, f2p nW2h)
     T = pfma(a.l, W1h, T);
     T = pfma(ash, W2l, T);
     T = pfma(asl, W2h, T);
+    if constexpr (!NORM) return pcx{bcast(0.0f) - ns, T};
     const f2p h = T - ns;                                    // s + T
     return pcx{h, T - (h + ns)};                             // T - (h - s)
 }
@@ -208,22 +211,24 @@ struct ptw {
     float rh, ih, rl, il;
 };
 #if defined(__CUDACC__)
+template <bool NORM = true>
 IGP pcx pmulw(pcx a, const ptw *w, float neg1)
 {
     const float4 q = *reinterpret_cast<const float4 *>(w);
     const f2p m = pk(neg1, 1.0f), nn = pk(neg1, neg1);
     const f2p W1h = pk(q.x, q.x), W1l = pk(q.z, q.z);
     const f2p W2h = pk(q.y, q.y) * m, W2l = pk(q.w, q.w) * m;  // (-wi, wi)
-    return pmulw(a, W1h, W2h, W1l, W2l, W1h * nn, W2h * nn);
+    return pmulw<NORM>(a, W1h, W2h, W1l, W2l, W1h * nn, W2h * nn);
 }
 // a * w, w a cx<df> in memory (r.h, r.l, i.h, i.l), pairs formed as for ptw
+template <bool NORM = true>
 IGP pcx pmulw_cx(pcx a, const cx<df> *w, float neg1)
 {
     const float4 q = *reinterpret_cast<const float4 *>(w);
     const f2p m = pk(neg1, 1.0f), nn = pk(neg1, neg1);
     const f2p W1h = pk(q.x, q.x), W1l = pk(q.y, q.y);
     const f2p W2h = pk(q.z, q.z) * m, W2l = pk(q.w, q.w) * m;  // (-wi, wi)
-    return pmulw(a, W1h, W2h, W1l, W2l, W1h * nn, W2h * nn);
+    return pmulw<NORM>(a, W1h, W2h, W1l, W2l, W1h * nn, W2h * nn);
 }
 #endif
 
@@ -231,7 +236,8 @@ IGP pcx pmulw_cx(pcx a, const cx<df> *w, float neg1)
 IGP pcx pcmulk(pcx a, double c, double s)
 {
     const df C = df_const(c), S = df_const(s);
-    return pmulw(a, bcast(C.h), pk(-S.h, S.h), bcast(C.l), pk(-S.l, S.l), bcast(-C.h), pk(S.h, -S.h));
+    // unrenormalised: the packed DFTs add the result lazily
+    return pmulw<false>(a, bcast(C.h), pk(-S.h, S.h), bcast(C.l), pk(-S.l, S.l), bcast(-C.h), pk(S.h, -S.h));
 }
 
 // ---- packed small DFTs (forward sign only: the stages run forward) --------
@@ -253,12 +259,12 @@ IGP void pdft4(pcx &x0, pcx &x1, pcx &x2, pcx &x3)
 IGP pcx pw8_1(pcx a)
 {
     const df h = df_const(kSqrtHalf);
-    return pscale(a + prot<true>(a), h.h, h.l);
+    return pprod(a + prot<true>(a), h.h, h.l);  // consumed by lazy adds
 }
 IGP pcx pw8_3(pcx a)
 {
     const df h = df_const(kSqrtHalf);
-    return pscale(prot<true>(a) - a, h.h, h.l);
+    return pprod(prot<true>(a) - a, h.h, h.l);
 }
 IGP void pdft8(pcx *v)
 {
