@@ -157,7 +157,9 @@ IGD df df_from_double(double x, int escale = 0)
     const uint32_t sign = hw & 0x80000000u;
     const int e = (int)((hw >> 20) & 0x7ffu);
     const int ef = e + escale - 896;  // float biased exponent of the high part
-    if ((unsigned)(ef - 24) < 231u && e != 0x7ff) {
+    // ef in [24, 254] excludes e = 0x7ff by itself whenever escale >= -896 (a
+    // per-line test the loops hoist)
+    if ((unsigned)(ef - 24) < 231u && (escale >= -896 || e != 0x7ff)) {
         const uint32_t f23 = ((hw << 3) | (lw >> 29)) & 0x7fffffu;
         const uint32_t eb = (uint32_t)ef << 23;
         const float h = u2f(sign | eb | f23);
@@ -246,10 +248,9 @@ IGD double df_to_double(df v, int escale = 0)
 {
     const uint32_t uh = f2u(v.h), ul = f2u(v.l);
     const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
-    const int ed = eh + 896 - escale;  // double biased exponent of the high part
-    const int edl = el + 896 - escale;
-    if ((unsigned)(eh - 1) < 254u && (unsigned)(ed - 1) < 2046u &&
-        (el == 0 || ((unsigned)(el - 1) < 254u && (unsigned)(edl - 1) < 2046u))) {
+    // a normal float part (biased exponent 1..254) rebiased by 896 - escale is a
+    // normal double whenever |escale| <= 896 (a per-line test the loops hoist)
+    if ((unsigned)(escale + 896) <= 1792u && (unsigned)(eh - 1) < 254u && (el == 0 || (unsigned)(el - 1) < 254u)) {
         const uint32_t rebias = (uint32_t)(896 - escale) << 20;
         const double dh = u2d(((uint64_t)((uh & 0x80000000u) | (((uh & 0x7fffffffu) >> 3) + rebias)) << 32) |
                               (uint64_t)(uh << 29));
