@@ -709,7 +709,14 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     __syncthreads();
                     if (g < nl) {
                         if (t == 0) sput(line_a + sp(L, pad), a0);
-                        for (int u = t; u < L; u += tpl) sput(myline + sp(u, pad), conjx(cmul(sget(myline + sp(u, pad)), chf[u])));
+                        if constexpr (std::is_same<T, df>::value) {
+                            for (int u = t; u < L; u += tpl) {
+                                cx<df> *p = myline + sp(u, pad);
+                                pst(p, pconj(prenorm(pmulw_cx<false>(pld(p), chf + u, P.neg1))));
+                            }
+                        } else {
+                            for (int u = t; u < L; u += tpl) sput(myline + sp(u, pad), conjx(cmul(sget(myline + sp(u, pad)), chf[u])));
+                        }
                     }
                 }
             }
@@ -831,15 +838,24 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     if (scaled) {
                         const int ea = s_esc[2 * ga], eb = s_esc[2 * gb];
                         ec = min(ea, eb);
-                        a = cscale_pow2(a, ec - ea);
-                        b = cscale_pow2(b, ec - eb);
+                        if (ea != ec) a = cscale_pow2(a, ec - ea);
+                        if (eb != ec) b = cscale_pow2(b, ec - eb);
                     }
                     const long long k = ra + (long long)N1 * u, km = Mt - k;
                     char *base = io.out + line_off(io, la, true);
                     auto split_store = [&](cx<T> za, cx<T> zb, long long kk) {
-                        const cx<T> zc = conjx(zb);
-                        const cx<T> E = chalf(za + zc), D = chalf(za - zc);
-                        const cx<T> X = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[kk]));
+                        cx<T> X;
+                        if constexpr (std::is_same<T, df>::value) {
+                            // packed pairs (re, im), as the in-CTA real split
+                            const f2p half = bcast(0.5f), cj = pk(1.0f, -1.0f);
+                            const pcx pa = to_p(za), pc = plane(to_p(zb), cj);
+                            const pcx E = plane(pa + pc, half), D = plane(pa - pc, half);
+                            X = from_p(prenorm(E + pmulw_cx<false>(prot<true>(D), rtw + kk, P.neg1)));
+                        } else {
+                            const cx<T> zc = conjx(zb);
+                            const cx<T> E = chalf(za + zc), D = chalf(za - zc);
+                            X = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[kk]));
+                        }
                         if (kk == 0) {
                             stg_s<S>(base, sc.apply(X.r, ec));
                         } else if (kk == Mt) {
