@@ -755,16 +755,16 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const f2p half = bcast(0.5f), cj = pk(1.0f, -1.0f);
             for (int k = t; k <= M / 2; k += tpl) {
                 const int k2 = M - k;
-                const pcx a = pld((myline + sp(k, pad))), b = pld((myline + sp(k == 0 ? 0 : k2, pad)));
+                const pcx a = pld(myline + sp(k, pad)), b = pld(myline + sp(k == 0 ? 0 : k2, pad));
                 {
                     const pcx zb = plane(b, cj);
-                    const pcx E = plane(a + zb, half), D = plane(a - zb, half);
-                    pst((myline + sp(k, pad)), prenorm(E + pmulw_cx<false>(prot<true>(D), rtw + k, P.neg1)));
+                    const pcx Ev = plane(a + zb, half), D = plane(a - zb, half);
+                    pst(myline + sp(k, pad), prenorm(Ev + pmulw_cx<false>(prot<true>(D), rtw + k, P.neg1)));
                 }
                 if (k2 != k) {
                     const pcx za = plane(a, cj);
-                    const pcx E = plane(b + za, half), D = plane(b - za, half);
-                    pst((myline + sp(k2, pad)), prenorm(E + pmulw_cx<false>(prot<true>(D), rtw + k2, P.neg1)));
+                    const pcx Ev = plane(b + za, half), D = plane(b - za, half);
+                    pst(myline + sp(k2, pad), prenorm(Ev + pmulw_cx<false>(prot<true>(D), rtw + k2, P.neg1)));
                 }
             }
         } else {
@@ -773,13 +773,13 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 cx<T> a = sget(myline + sp(k, pad)), b = sget(myline + sp(k == 0 ? 0 : k2, pad));
                 {
                     cx<T> zb = conjx(b);
-                    cx<T> E = chalf(a + zb), D = chalf(a - zb);
-                    sput(myline + sp(k, pad), crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k])));
+                    cx<T> Ev = chalf(a + zb), D = chalf(a - zb);
+                    sput(myline + sp(k, pad), crenorm(Ev + cmul(cx<T>{D.i, -D.r}, rtw[k])));
                 }
                 if (k2 != k) {
                     cx<T> zb = conjx(a);
-                    cx<T> E = chalf(b + zb), D = chalf(b - zb);
-                    sput(myline + sp(k2, pad), crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[k2])));
+                    cx<T> Ev = chalf(b + zb), D = chalf(b - zb);
+                    sput(myline + sp(k2, pad), crenorm(Ev + cmul(cx<T>{D.i, -D.r}, rtw[k2])));
                 }
             }
         }
@@ -792,9 +792,9 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const f2p half = bcast(0.5f), cj = pk(1.0f, -1.0f);
             for (int k = 1 + t; 2 * k < M + 1; k += tpl) {
                 const int k2 = M - k;
-                const pcx a = pld((myline + sp(k, pad))), b = plane(pld((myline + sp(k2, pad))), cj);
-                pst((myline + sp(k, pad)), prenorm(plane(a + b, half)));
-                pst((myline + sp(k2, pad)), prenorm(prot<true>(plane(a - b, half))));
+                const pcx a = pld(myline + sp(k, pad)), b = plane(pld(myline + sp(k2, pad)), cj);
+                pst(myline + sp(k, pad), prenorm(plane(a + b, half)));
+                pst(myline + sp(k2, pad), prenorm(prot<true>(plane(a - b, half))));
             }
         } else {
             for (int k = 1 + t; 2 * k < M + 1; k += tpl) {
@@ -849,12 +849,12 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                             // packed pairs (re, im), as the in-CTA real split
                             const f2p half = bcast(0.5f), cj = pk(1.0f, -1.0f);
                             const pcx pa = to_p(za), pc = plane(to_p(zb), cj);
-                            const pcx E = plane(pa + pc, half), D = plane(pa - pc, half);
-                            X = from_p(prenorm(E + pmulw_cx<false>(prot<true>(D), rtw + kk, P.neg1)));
+                            const pcx Ev = plane(pa + pc, half), D = plane(pa - pc, half);
+                            X = from_p(prenorm(Ev + pmulw_cx<false>(prot<true>(D), rtw + kk, P.neg1)));
                         } else {
                             const cx<T> zc = conjx(zb);
-                            const cx<T> E = chalf(za + zc), D = chalf(za - zc);
-                            X = crenorm(E + cmul(cx<T>{D.i, -D.r}, rtw[kk]));
+                            const cx<T> Ev = chalf(za + zc), D = chalf(za - zc);
+                            X = crenorm(Ev + cmul(cx<T>{D.i, -D.r}, rtw[kk]));
                         }
                         if (kk == 0) {
                             stg_s<S>(base, sc.apply(X.r, ec));
