@@ -147,34 +147,53 @@ IGD df df_scale2(df a, float p2) { return df{IG_FMUL(a.h, p2), IG_FMUL(a.l, p2)}
 // multiplies by 2^escale exactly (per-line range scaling).  High part: the
 // sign, the rebiased exponent and the top 23 fraction bits (truncated); low
 // part: the remaining 29 fraction bits rounded to 23, placed under a power of
-// two with one exact FP32 subtraction.  Relative error <= 2^-47.  Zeros, double
-// subnormals and values below the float range of the scaled high part
-// flush to zero; infinities and NaNs map to float infinities and NaNs.
+// two with one exact FP32 subtraction.  Relative error <= 2^-47.  Double
+// subnormals are normalised first (an exact product by 2^64); values below
+// the float range of the scaled high part flush to zero; infinities and NaNs
+// map to float infinities and NaNs.
+//
+// the fast formula for a normal double (words hw, lw) whose scaled high part
+// has the float biased exponent ef in [24, 254]
+IGD df df_from_fields(uint32_t hw, uint32_t lw, int ef)
+{
+    const uint32_t sign = hw & 0x80000000u;
+    const uint32_t f23 = ((hw << 3) | (lw >> 29)) & 0x7fffffu;
+    const uint32_t eb = (uint32_t)ef << 23;
+    const float h = u2f(sign | eb | f23);
+    // (1 + m / 2^23) 2^(ef-23-127) - 2^(ef-23-127) = m 2^(ef-173), m = fraction bits
+    // 28..0 / 2^6 rounded (m = 2^23 carries into the exponent, which is exact too)
+    const uint32_t lb = eb - (23u << 23);
+    const float l = IG_FSUB(u2f(lb + (((lw & 0x1fffffffu) + 32u) >> 6)), u2f(lb));
+    return df{h, u2f(f2u(l) | sign)};
+}
 IGD df df_from_double(double x, int escale = 0)
 {
-    const uint64_t b = d2u(x);
-    const uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
+    uint64_t b = d2u(x);
+    uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
+    int e = (int)((hw >> 20) & 0x7ffu);
+    int ef = e + escale - 896;  // float biased exponent of the high part
+    // for escale in [-896, 919] (a per-line test the loops hoist) ef in
+    // [24, 254] already excludes zero and subnormal (e = 0) and non-finite
+    // (e = 0x7ff) x; outside that window e is tested as well
+    if ((unsigned)(ef - 24) < 231u && ((unsigned)(escale + 896) <= 1815u || (unsigned)(e - 1) < 2046u))
+        return df_from_fields(hw, lw, ef);
     const uint32_t sign = hw & 0x80000000u;
-    const int e = (int)((hw >> 20) & 0x7ffu);
-    const int ef = e + escale - 896;  // float biased exponent of the high part
-    // ef in [24, 254] excludes e = 0x7ff by itself whenever escale >= -896 (a
-    // per-line test the loops hoist)
-    if ((unsigned)(ef - 24) < 231u && (escale >= -896 || e != 0x7ff)) {
-        const uint32_t f23 = ((hw << 3) | (lw >> 29)) & 0x7fffffu;
-        const uint32_t eb = (uint32_t)ef << 23;
-        const float h = u2f(sign | eb | f23);
-        // (1 + m / 2^23) 2^(ef-23-127) - 2^(ef-23-127) = m 2^(ef-173), m = fraction bits
-        // 28..0 / 2^6 rounded (m = 2^23 carries into the exponent, which is exact too)
-        const uint32_t lb = eb - (23u << 23);
-        const float l = IG_FSUB(u2f(lb + (((lw & 0x1fffffffu) + 32u) >> 6)), u2f(lb));
-        return df{h, u2f(f2u(l) | sign)};
-    }
     if (e == 0x7ff) {  // inf / nan
         const uint32_t frac = ((hw & 0xfffffu) | lw) ? 0x400000u : 0u;
         return df{u2f(sign | 0x7f800000u | frac), 0.0f};
     }
+    if (e == 0) {
+        if (((hw & 0x7fffffffu) | lw) == 0u) return df{u2f(sign), 0.0f};
+        // subnormal double: normalised by an exact product with 2^64
+        b = d2u(x * 18446744073709551616.0);
+        hw = (uint32_t)(b >> 32);
+        lw = (uint32_t)b;
+        e = (int)((hw >> 20) & 0x7ffu);
+        ef = e + escale - 64 - 896;
+        if ((unsigned)(ef - 24) < 231u) return df_from_fields(hw, lw, ef);
+    }
     if (ef >= 255) return df{u2f(sign | 0x7f800000u), 0.0f};
-    if (ef <= 0 || e == 0) return df{u2f(sign), 0.0f};
+    if (ef <= 0) return df{u2f(sign), 0.0f};
     // 0 < ef < 24: high part only (the low part would be a float subnormal)
     const uint32_t f23 = ((hw << 3) | (lw >> 29)) & 0x7fffffu;
     return df{u2f(sign | ((uint32_t)ef << 23) | f23), 0.0f};
@@ -236,7 +255,13 @@ IGD double df_to_double_slow(df v, int escale)
         M <<= (-shift);
     }
     if (ed >= 0x7ff) return u2d(sgn | 0x7ff0000000000000ull);
-    if (ed <= 0) return u2d(sgn);
+    if (ed <= 0) {
+        // subnormal result: M 2^(ed - 1075) = F 2^-1074, F = M >> (1 - ed), rounded
+        // (a carry into bit 52 gives the smallest normal, encoded the same way)
+        const int s = 1 - ed;
+        if (s > 53) return u2d(sgn);
+        return u2d(sgn | ((M + ((uint64_t)1 << (s - 1))) >> s));
+    }
     return u2d(sgn | ((uint64_t)ed << 52) | (M & 0xfffffffffffffull));
 }
 

@@ -85,3 +85,21 @@ def test_halfcomplex_fourstep_gaps(engine, oracle_lib, n, dist, dtype):
     want = oracle_lib.rfft_hc(x[:, :n].astype(np.float64), True, 0.5)
     assert oracle_lib.rel_l2(h[:, :n], want) < tol, (n, dist, oracle_lib.rel_l2(h[:, :n], want))
     assert np.array_equal(h[:, n:], x[:, n:])
+
+
+@pytest.mark.parametrize("n", [4096, 2205, 18144, 29403])
+def test_halfcomplex_range_scaling(engine, oracle_lib, n):
+    """Real lines far outside the float range, with different magnitudes in one
+    batch (and in one pair of lines for odd lengths): single-CTA, paired,
+    fused four-step split and paired four-step paths keep FP64 accuracy."""
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(n + 7)
+    scales = np.array([1e300, 1e-300, 1.0, 1e-200, 1e250, 3.0])[:, None]
+    x = rng.standard_normal((6, n)) * scales
+    hc = F.rfft_batch(x, True, 1.0)
+    want = oracle_lib.rfft_hc(x, True, 1.0)
+    for r in range(6):
+        assert oracle_lib.rel_l2(hc[r], want[r]) < F64_TOL, (n, r)
+    back = F.rfft_batch(hc, False, 1.0 / n)
+    for r in range(6):
+        assert oracle_lib.rel_l2(back[r], x[r]) < 2 * F64_TOL, (n, r)
