@@ -290,6 +290,18 @@ IGD double df_to_double(df v, int escale = 0)
 // sign flip of a double through its bit pattern (no FP64 instruction)
 IGD double dneg(double x) { return u2d(d2u(x) ^ 0x8000000000000000ull); }
 
+// x 2^es exactly, by an add to the exponent field when x and the result are
+// normal doubles; zeros, subnormals, specials and out-of-range results go
+// through the double-float conversions
+IGD double pow2_scale(double x, int es)
+{
+    const uint64_t b = d2u(x);
+    const int e = (int)((b >> 52) & 0x7ffu);
+    if ((unsigned)(e - 1) < 2046u && (unsigned)(e + es - 1) < 2046u)
+        return u2d(b + ((uint64_t)(int64_t)es << 52));
+    return df_to_double(df_from_double(x, es), 0);
+}
+
 // ---------------------------------------------------------------------------
 // generic real helpers: constants, scale by power of two
 // ---------------------------------------------------------------------------

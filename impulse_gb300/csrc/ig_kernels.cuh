@@ -1312,6 +1312,26 @@ __global__ void k_gather_pair(const __grid_constant__ IODesc io, const __grid_co
         const char *base = io.in + line_off(io, l, false);
         const bool has_b = 2LL * line_i0(io, l) + 1 < io.pair_n0;
         const int ea = esc[2 * l], eb = esc[2 * l + 1];
+        if constexpr (std::is_same<T, df>::value) {
+            // real lines into plain or Rader order: the pair (2^ea a, 2^eb b) is an
+            // exact rescale of the stored doubles (no double-float round trip)
+            if (io.in_kind == IN_R && !io.conj_in && (mp.kind == MAP_RADER || mp.kind == MAP_PLAIN)) {
+                const bool neg_b = mp.kind == MAP_RADER && !mp.fwd;  // conjugated for the backward direction
+                auto rz = [&](long long v) {
+                    const double a = ldg_s<double>(base + v * io.is);
+                    const double b = has_b ? ldg_s<double>(base + io.pair_in + v * io.is) : 0.0;
+                    const double sb = pow2_scale(b, eb);
+                    return make_double2(pow2_scale(a, ea), neg_b ? dneg(sb) : sb);
+                };
+                if (mp.kind == MAP_RADER) {
+                    *dst = rz(mp.ridx[u]);
+                    if (u == 0) reinterpret_cast<double2 *>(mp.x0buf)[l] = rz(0);
+                } else {
+                    *dst = u < mp.M ? rz(u) : make_double2(0.0, 0.0);
+                }
+                continue;
+            }
+        }
         // Z at logical index v of the complex line
         auto zat = [&](long long v) {
             const bool mirror = io.in_kind != IN_R && v >= io.cnt_in;
