@@ -100,9 +100,24 @@ class ClockSampler:
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index=0):
-        self.gpu = gpu_index
+        self.gpu = self.smi_id(gpu_index)
         self.proc = None
         self.lines = []
+
+    @staticmethod
+    def smi_id(index):
+        """nvidia-smi's --id for torch device `index`: the device UUID, so the
+        sampled GPU is this process's even when CUDA_VISIBLE_DEVICES renumbers
+        devices; else the physical index mapped through CUDA_VISIBLE_DEVICES."""
+        try:
+            import torch
+            u = str(torch.cuda.get_device_properties(index).uuid)
+            if u:
+                return u if u.startswith("GPU-") else "GPU-" + u
+        except Exception:
+            pass
+        vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+        return vis[index] if index < len(vis) else str(index)
 
     def start(self):
         try:
@@ -142,7 +157,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "gpu": self.gpu}
 
 
 # --------------------------------------------------------------------------

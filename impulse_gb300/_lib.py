@@ -65,6 +65,8 @@ SIGNATURES = {
                                 C.POINTER(_sz), C.c_int, _vp, _vp, C.c_double, _vp]),
     "ig_c2r_device": (C.c_int, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,
                                 C.POINTER(_sz), C.c_int, _vp, _vp, C.c_double, _vp]),
+    "ig_c2c_adjoint_device": (C.c_int, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,
+                                        C.POINTER(_sz), C.c_int, _vp, _vp, C.c_double, _vp]),
     "ig_r2c_adjoint_device": (C.c_int, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,
                                         C.POINTER(_sz), C.c_int, _vp, _vp, C.c_double, _vp]),
     "ig_c2r_adjoint_device": (C.c_int, [C.c_int, _sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,

@@ -212,56 +212,70 @@ IGD double f2d_bits(float f)
 }
 
 // double-float -> double, general case: the two significands are aligned
-// into one 64-bit integer, normalised and rounded (round-half-up on the
-// discarded bits), and the double is assembled with integer instructions.
+// into one 64-bit integer (the larger part's units, 37 bits below its last
+// bit, plus a sticky bit for any discarded low bits), normalised and rounded
+// once to nearest with ties to even, and the double is assembled with integer
+// instructions.
 IGD double df_to_double_slow(df v, int escale)
 {
     uint32_t uh = f2u(v.h), ul = f2u(v.l);
     int eh = (int)((uh >> 23) & 0xff);
     int el = (int)((ul >> 23) & 0xff);
     if (eh == 0xff) return f2d_bits(v.h);
-    if (eh == 0) {
-        if (el == 0 || el == 0xff) return f2d_bits(v.h);
-        // only the low part is non-zero
-        double d = f2d_bits(v.l);
-        uint64_t bd = d2u(d);
-        int ed = (int)((bd >> 52) & 0x7ff) - escale;
-        if (ed <= 0) return u2d(bd & 0x8000000000000000ull);
-        if (ed >= 0x7ff) return u2d((bd & 0x8000000000000000ull) | 0x7ff0000000000000ull);
-        return u2d((bd & 0x800fffffffffffffull) | ((uint64_t)ed << 52));
+    if (el == 0xff) return f2d_bits(v.l);
+    // the sum is symmetric: align to the part with the larger exponent
+    if (el > eh) {
+        const uint32_t tu = uh; uh = ul; ul = tu;
+        const int te = eh; eh = el; el = te;
     }
+    if (eh == 0) return f2d_bits(v.h);  // zeros and float subnormals
     int64_t H = (int64_t)((uh & 0x7fffffu) | 0x800000u);
     if (uh & 0x80000000u) H = -H;
-    int64_t K = H * ((int64_t)1 << 29);  // units of 2^(eh-127-23-29)
+    int64_t K = H * ((int64_t)1 << 37);  // units of 2^(eh-127-23-37)
+    int stk = 0;
     if (el != 0) {
         int64_t L = (int64_t)((ul & 0x7fffffu) | 0x800000u);
         if (ul & 0x80000000u) L = -L;
-        int sh = 29 - (eh - el);  // align L to K's units
-        if (sh >= 0) K += L * ((int64_t)1 << sh);
-        else if (sh > -40) K += (L >> (-sh));
+        const int sh = 37 - (eh - el);  // align L to K's units (sh <= 37)
+        if (sh >= 0) {
+            K += L * ((int64_t)1 << sh);
+        } else if (sh > -62) {
+            const int64_t q = L >> (-sh);  // floor; the remainder is >= 0
+            stk = (L - q * ((int64_t)1 << (-sh))) != 0;
+            K += q;
+        } else {
+            stk = 1;
+            K += L < 0 ? -1 : 0;
+        }
     }
+    // one more bit: K2 = 2 K + sticky lies strictly inside the interval that
+    // holds the exact sum whenever bits were discarded (units 2^(eh-127-61))
+    K = 2 * K + stk;
     if (K == 0) return 0.0;
     uint64_t sgn = K < 0 ? 0x8000000000000000ull : 0;
-    uint64_t M = (uint64_t)(K < 0 ? -K : K);
-    int lz = clz64(M);
+    const uint64_t M0 = (uint64_t)(K < 0 ? -K : K);
+    int lz = clz64(M0);
     int shift = 11 - lz;  // bring the leading one to bit 52
-    // exponent of the result: value = M * 2^(eh - 127 - 52)
-    int ed = eh - 127 + 1023 + shift - escale;
-    if (shift > 0) {
-        uint64_t half = (uint64_t)1 << (shift - 1);
-        M = (M + half) >> shift;
-        if (M >> 53) { M >>= 1; ++ed; }
-    } else if (shift < 0) {
-        M <<= (-shift);
+    // exponent of the result: value = M0 * 2^(eh - 127 - 61), M0 >> shift in [2^52, 2^53)
+    int ed = eh - 127 - 9 + 1023 + shift - escale;
+    // subnormal result: F 2^-1074 with F = M0 >> (shift + 1 - ed), one rounding
+    // from the exact sum (a carry into bit 52 gives the smallest normal, encoded
+    // the same way)
+    const bool sub = ed <= 0;
+    const int s = sub ? shift + 1 - ed : shift;
+    uint64_t M;
+    if (s <= 0) {
+        M = M0 << (-s);
+    } else if (s < 64) {
+        // round to nearest, ties to even
+        const uint64_t q = M0 >> s, rem = M0 & (((uint64_t)1 << s) - 1), half = (uint64_t)1 << (s - 1);
+        M = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+    } else {
+        M = (s == 64 && M0 > ((uint64_t)1 << 63)) ? 1 : 0;
     }
+    if (sub) return u2d(sgn | M);
+    if (M >> 53) { M >>= 1; ++ed; }
     if (ed >= 0x7ff) return u2d(sgn | 0x7ff0000000000000ull);
-    if (ed <= 0) {
-        // subnormal result: M 2^(ed - 1075) = F 2^-1074, F = M >> (1 - ed), rounded
-        // (a carry into bit 52 gives the smallest normal, encoded the same way)
-        const int s = 1 - ed;
-        if (s > 53) return u2d(sgn);
-        return u2d(sgn | ((M + ((uint64_t)1 << (s - 1))) >> s));
-    }
     return u2d(sgn | ((uint64_t)ed << 52) | (M & 0xfffffffffffffull));
 }
 

@@ -1643,13 +1643,13 @@ int ig_cfft_exec_device(ig_cfft_plan plan, const void *in, void *out, size_t bat
 }
 
 // ---- allocation-free complex execution ------------------------------------
-// Some callers cannot allocate device memory at call time: code that runs
-// while a stream is being captured into a CUDA graph, under a memory pool
-// that forbids growth, or in a real-time loop that must not block in the
-// allocator.  ig_cfft_exec_device_noalloc serves them: its four-step scratch
-// is this file-scope device array instead of the cached per-stream
-// workspace.  Every GPU that loads the library holds the array until the
-// process exits.
+// Some callers cannot allocate device memory at call time: a process that
+// reserves its whole device-memory budget up front in a pool that must not
+// grow, or a latency-bound loop where cudaMalloc / cudaFree (which can
+// synchronise the device and take unbounded time) are not allowed.
+// ig_cfft_exec_device_noalloc serves them: its four-step scratch is this
+// file-scope device array instead of the cached per-stream workspace.  Every
+// GPU that loads the library holds the array until the process exits.
 #define IG_NOALLOC_SCRATCH_BYTES (64ull << 20)
 #define IG_NOALLOC_MAX_DEVICES 64
 static __device__ __align__(256) unsigned char g_noalloc_scratch[IG_NOALLOC_SCRATCH_BYTES];
@@ -1676,10 +1676,10 @@ static void *noalloc_scratch()
 // single-CTA plans need no scratch, four-step plans use the static array
 // (at most IG_NOALLOC_SCRATCH_BYTES = batch * length * complex size).  Plans
 // that run Bluestein or Rader over a multi-pass core are rejected.  The first call on
-// a device looks up the array's address there; make that first call before
-// any stream capture.  All calls share the array and it keeps the previous
-// call's contents (this path writes every scratch element before reading
-// it, so nothing needs clearing); calls that overlap on the GPU race.
+// a device (whatever its plan) looks up the array's address there; make that
+// first call before any stream capture.  All calls share the array and it keeps
+// the previous call's contents (this path writes every scratch element before
+// reading it, so nothing needs clearing); calls that overlap on the GPU race.
 int ig_cfft_exec_device_noalloc(ig_cfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in,
                                 size_t dist_out, int forward, double fct, void *stream)
 {
@@ -1689,13 +1689,15 @@ int ig_cfft_exec_device_noalloc(ig_cfft_plan plan, const void *in, void *out, si
         const long long es = 2 * (long long)store_real_bytes(plan->a);
         if (c.kind == 2 || c.kind == 3)
             raise(IG_EINVAL, "no-allocation execution does not cover Bluestein or Rader over a multi-pass core");
+        // the per-device set-up runs on the first call, for every kind of plan
+        char *const arr = (char *)noalloc_scratch();
         if (batch == 0) return;
         char *scr = nullptr;
         if (c.kind == 1) {
             unsigned long long need = (unsigned long long)batch * (unsigned long long)c.M * (unsigned long long)es;
             if (need > IG_NOALLOC_SCRATCH_BYTES)
                 raise(IG_ETOOLARGE, "batch * length * element size exceeds the 64 MiB no-allocation scratch");
-            scr = (char *)noalloc_scratch();
+            scr = arr;
         }
         require_aligned(in, (size_t)es, "input");
         require_aligned(out, (size_t)es, "output");
@@ -2207,6 +2209,21 @@ static void launch_half_weight(Arith a, void *x, long long lines, long long n_ha
                                : Launch<TagF64>::half_weight(x, lines, n_half, nreal, w, drop_im, st);
     ck(e, "Hermitian weighting");
     count_launch();
+}
+
+// adjoint of c2c(axes, forward, fct): c2c(axes, !forward, fct).  The
+// transform is complex-linear with a symmetric matrix F, so its adjoint under
+// the real inner product Re <a, b> is conj(F) = the opposite direction.
+int ig_c2c_adjoint_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_g,
+                          const ptrdiff_t *stride_x, size_t naxes, const size_t *axes, int forward, const void *g,
+                          void *x, double fct, void *stream)
+{
+    return guarded([&] {
+        if (ndim >= 1 && shape && prod(ndim, shape) == 0) return;
+        nd_checks(dtype, ndim, shape, stride_g, stride_x, naxes, axes, g, x, true);
+        nd_c2c_device(arith_for(dtype), ndim, shape, stride_g, stride_x, naxes, axes, forward ? 0 : 1, g, x, fct,
+                      as_stream(stream));
+    });
 }
 
 // adjoint of r2c(axes, forward): halve the inner bins of the last axis (the

@@ -3,7 +3,7 @@
 Nim is not available on this machine, so the layer above the C ABI is
 restated here in Python, name for name, with the reference's argument meaning
 and quirks; the arithmetic all happens in libimpulse_gpu.so.  A Nim user binds
-the same C ABI with ``{.importc, dynlib.}``.
+the same C ABI with ``{.importc, dynlib.}`` (the module nim/impulse_gpu_fft.nim).
 
 C backend (impulse/fft/c_pocketfft/pocketfft.nim, pocketfft_arraymancer.nim):
 

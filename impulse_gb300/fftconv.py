@@ -21,9 +21,9 @@ from . import _lib as L
 
 
 def _code(dt):
-    if dt == torch.float64:
+    if dt in (torch.float64, torch.complex128):
         return L.IG_F64
-    if dt == torch.float32:
+    if dt in (torch.float32, torch.complex64):
         return L.IG_F32
     raise TypeError(f"unsupported dtype {dt}")
 
@@ -93,6 +93,15 @@ def fftconv2d(x, k, recompute=True, pad=None):
 def _nd_args(x_shape, a, b, axes):
     return (len(x_shape), L.arr(C.c_size_t, x_shape), L.arr(C.c_ssize_t, [s * a.element_size() for s in a.stride()]),
             L.arr(C.c_ssize_t, [s * b.element_size() for s in b.stride()]), len(axes), L.arr(C.c_size_t, axes))
+
+
+def c2c_adjoint(g, axes, forward=True, fct=1.0):
+    """Adjoint of c2c(axes, forward, fct): x_bar from the complex gradient g (same shape)."""
+    x = torch.empty_like(g)
+    n, sh, sg, sx, na, ax = _nd_args(list(g.shape), g, x, list(axes))
+    L.check(L.load().ig_c2c_adjoint_device(_code(g.dtype), n, sh, sg, sx, na, ax, int(forward), g.data_ptr(),
+                                           x.data_ptr(), float(fct), _stream()))
+    return x
 
 
 def r2c_adjoint(g, shape_in, axes, forward=True, fct=1.0):

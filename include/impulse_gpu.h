@@ -104,15 +104,18 @@ int ig_rfft_exec_device(ig_rfft_plan plan, const void *in, void *out, size_t bat
 
 /* Allocation-free variant of ig_cfft_exec_device.  No counterpart in the
  * reference (PocketFFT mallocs its scratch on every call).  For callers that
- * must not allocate device memory while they run -- during CUDA-graph stream
- * capture, under a fixed memory pool, in a real-time loop -- this call uses
- * a static device array of 64 MiB (held by every GPU that loads the library)
- * instead of the engine's cached workspace.  Limit: batch * length * complex
- * element size <= 64 MiB for plans longer than one CTA; plans running
- * Bluestein or Rader over a multi-pass core are rejected (IG_EINVAL), and so
- * are pointers not aligned to the complex element size.  The first call
- * on each device looks the array up there and should precede any stream
- * capture.  Calls share the array; calls that overlap on the GPU race. */
+ * cannot allocate device memory while they run: a process that reserves its
+ * whole device-memory budget up front in a pool that must not grow, or a
+ * latency-bound loop where cudaMalloc / cudaFree (which can synchronise the
+ * device and take unbounded time) are not allowed.  Transforms longer than
+ * one CTA take their scratch from a static device array of 64 MiB (held by
+ * every GPU that loads the library) instead of the engine's cached
+ * workspace.  Limit: batch * length * complex element size <= 64 MiB for
+ * plans longer than one CTA (IG_ETOOLARGE beyond); plans running Bluestein or
+ * Rader over a multi-pass core are rejected (IG_EINVAL), and so are pointers
+ * not aligned to the complex element size.  The first call on each device
+ * looks the array up there; make that first call before any stream capture.
+ * Calls share the array; calls that overlap on the GPU race. */
 int ig_cfft_exec_device_noalloc(ig_cfft_plan plan, const void *in, void *out, size_t batch, size_t dist_in,
                                 size_t dist_out, int forward, double fct, void *stream);
 
@@ -171,15 +174,21 @@ int ig_multi_exec_device(ig_multi_plan plan, const void *in, void *out, void *st
 int ig_multi_exec_graph(ig_multi_plan plan, const void *in, void *out, void *stream);
 int ig_multi_exec_loop_device(ig_multi_plan plan, const void *in, void *out, void *stream);
 
-/* ---- adjoints of the real transforms --------------------------------------
- * Gradients of a real loss through r2c / c2r (device pointers).  With g the
- * gradient with respect to (Re X, Im X) packed as complex:
+/* ---- adjoints ----------------------------------------------------------------
+ * Gradients of a real loss through c2c / r2c / c2r (device pointers).  With g
+ * the gradient with respect to (Re X, Im X) packed as complex:
+ *   adjoint of c2c(axes, forward, fct): x_bar = c2c(axes, !forward, fct) of g
+ *     (the DFT matrix is symmetric, so its adjoint is its conjugate);
  *   adjoint of r2c(axes, forward): x_bar = c2r(axes, !forward) of g with the
  *     inner bins of the last axis halved;
  *   adjoint of c2r(axes, forward): g_bar = r2c(axes, !forward) of y_bar with
  *     the inner bins of the last axis doubled (the Hermitian 2x weighting).
  * No counterpart in the reference (PocketFFT has no adjoints); shapes and
- * byte strides follow pocketfft::r2c / c2r (pocketfft_hdronly.h:3334, 3366). */
+ * byte strides follow pocketfft::c2c / r2c / c2r (pocketfft_hdronly.h:3272,
+ * 3334, 3366). */
+int ig_c2c_adjoint_device(int dtype, size_t ndim, const size_t *shape, const ptrdiff_t *stride_g,
+                          const ptrdiff_t *stride_x, size_t naxes, const size_t *axes, int forward, const void *g,
+                          void *x, double fct, void *stream);
 int ig_r2c_adjoint_device(int dtype, size_t ndim, const size_t *shape_in, const ptrdiff_t *stride_g,
                           const ptrdiff_t *stride_x, size_t naxes, const size_t *axes, int forward, const void *g,
                           void *x, double fct, void *stream);

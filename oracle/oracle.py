@@ -30,12 +30,20 @@ _dp = C.POINTER(C.c_double)
 
 
 def build(ref: bool | None = None) -> None:
-    """Compile the oracle (and, when the reference checkout exists, the reference shim)."""
+    """Compile the oracle; with ``ref`` (or, when ``ref`` is None, whenever
+    IMPULSE_REF names an impulse checkout) also the reference shim.
+
+    The reference's location comes only from the IMPULSE_REF environment
+    variable; asking for the shim without it is an error."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    refdir = os.environ.get("IMPULSE_REF", "/root/reference")
+    refdir = os.environ.get("IMPULSE_REF", "")
+    present = bool(refdir) and os.path.isdir(os.path.join(refdir, "impulse", "fft"))
     if ref is None:
-        ref = os.path.isdir(os.path.join(refdir, "impulse", "fft"))
+        ref = present
     if ref:
+        if not present:
+            raise RuntimeError("IMPULSE_REF must name an impulse checkout (with impulse/fft) to build the "
+                               f"reference PocketFFT; got {refdir!r}")
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"IMPULSE_REF={refdir}"], check=True)
 
 

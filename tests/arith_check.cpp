@@ -56,5 +56,21 @@ int main()
         }
         std::printf("to_double_es%d %.3Le %.3e\n", es, worst, 1.0);
     }
+    // exact ties round to even, on the general path (scales outside the hoisted
+    // window): a normal result and a subnormal one
+    {
+        int tbad = 0;
+        // (1 + 2^-53) 2^-1000: halfway between 2^-1000 and its successor -> 2^-1000
+        tbad += df_to_double(df{1.0f, std::ldexp(1.0f, -53)}, 1000) != std::ldexp(1.0, -1000);
+        // (1 + 3 2^-53) 2^-1000: halfway, odd below -> rounds up to (1 + 2^-51) 2^-1000
+        tbad += df_to_double(df{1.0f, 3.0f * std::ldexp(1.0f, -53)}, 1000) != std::ldexp(1.0 + std::ldexp(1.0, -51), -1000);
+        // (1 + 2^-24) 2^-1051 = (2^23 + 1/2) 2^-1074: subnormal tie -> 2^23 2^-1074
+        tbad += df_to_double(df{1.0f, std::ldexp(1.0f, -24)}, 1051) != std::ldexp(1.0, -1051);
+        // (1 + 3 2^-24) 2^-1051 = (2^23 + 3/2) 2^-1074 -> (2^23 + 2) 2^-1074
+        tbad += df_to_double(df{1.0f, 3.0f * std::ldexp(1.0f, -24)}, 1051) != std::ldexp(8388610.0, -1074);
+        // negative subnormal tie
+        tbad += df_to_double(df{-1.0f, -std::ldexp(1.0f, -24)}, 1051) != -std::ldexp(1.0, -1051);
+        std::printf("ties_to_even %d 0\n", tbad);
+    }
     return 0;
 }

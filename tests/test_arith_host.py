@@ -20,6 +20,6 @@ def test_conversions_across_scales():
         subprocess.run([gxx, "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "arith_check.cpp")], check=True)
         out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
     rows = [ln.split() for ln in out.splitlines() if ln.strip()]
-    assert len(rows) == 11 + 1 + 7
+    assert len(rows) == 11 + 1 + 7 + 1
     for name, err, limit in rows:
         assert float(err) <= float(limit), (name, err, limit)

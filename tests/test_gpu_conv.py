@@ -113,3 +113,23 @@ def test_real_transform_adjoints(engine, shape, axes, forward):
     Ga = c2r_adjoint(torch.from_numpy(y).cuda(), axes, forward).cpu().numpy()
     rhs2 = np.sum((G * np.conj(Ga)).real)
     assert abs(lhs2 - rhs2) <= 1e-11 * max(1.0, abs(lhs2))
+
+
+@pytest.mark.parametrize("shape,axes", [((16,), [0]), ((6, 10), [1]), ((6, 10), [0, 1]), ((4, 5, 9), [0, 2]),
+                                        ((3, 4096), [1]), ((97, 5), [0])])
+@pytest.mark.parametrize("forward", [True, False])
+def test_c2c_adjoint(engine, shape, axes, forward):
+    """<c2c(x), G>_R = <x, c2c_adj(G)>_R (dot-product test), FP64 and FP32."""
+    from impulse_gb300 import fft as F
+    from impulse_gb300.fftconv import c2c_adjoint
+    rng = np.random.default_rng(len(shape) + sum(shape) + int(forward))
+    x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    G = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    fct = 0.25
+    lhs = np.sum((F.c2c(x, axes, forward, fct) * np.conj(G)).real)
+    xa = c2c_adjoint(torch.from_numpy(G).cuda(), axes, forward, fct).cpu().numpy()
+    rhs = np.sum((x * np.conj(xa)).real)
+    assert abs(lhs - rhs) <= 1e-12 * max(1.0, abs(lhs))
+    xa32 = c2c_adjoint(torch.from_numpy(G.astype(np.complex64)).cuda(), axes, forward, fct).cpu().numpy()
+    n = int(np.prod([shape[a] for a in axes]))
+    assert np.linalg.norm(xa32 - xa) / np.linalg.norm(xa) < 1e-6 * max(1.0, np.log2(n))

@@ -103,3 +103,25 @@ def test_halfcomplex_range_scaling(engine, oracle_lib, n):
     back = F.rfft_batch(hc, False, 1.0 / n)
     for r in range(6):
         assert oracle_lib.rel_l2(back[r], x[r]) < 2 * F64_TOL, (n, r)
+
+
+@pytest.mark.parametrize("n", [65521, 8191, 29403])
+def test_halfcomplex_range_scaling_rader_and_odd_multipass(engine, oracle_lib, n):
+    """Rader lines (65521 over a multi-pass core, 8191) and an odd four-step
+    length, with rows at 1e300, 1e-300 and double-subnormal 1e-310 paired in
+    one batch, in both directions: the paired-line gather rescales each line by
+    its own exponent, including the negated second line of the backward Rader
+    direction and its kept x[0]."""
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(n + 11)
+    scales = np.array([1e300, 1e-300, 1e-310, 1.0, 1e-310, 1e300, 1e-300])[:, None]
+    x = rng.standard_normal((7, n)) * scales
+    hc = F.rfft_batch(x, True, 1.0)
+    want = oracle_lib.rfft_hc(x, True, 1.0)
+    for r in range(7):
+        assert oracle_lib.rel_l2(hc[r], want[r]) < F64_TOL, (n, r, "forward")
+    spec = want.copy()
+    back = F.rfft_batch(spec, False, 1.0 / n)
+    want_b = oracle_lib.rfft_hc(spec, False, 1.0 / n)
+    for r in range(7):
+        assert oracle_lib.rel_l2(back[r], want_b[r]) < F64_TOL, (n, r, "backward")

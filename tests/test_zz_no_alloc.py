@@ -1,12 +1,14 @@
 """GPU test of ig_cfft_exec_device_noalloc, the allocation-free entry point.
 
-Callers that cannot allocate device memory while they run (stream capture,
-fixed memory pools, real-time loops) use this call; its scratch is a static
-device array instead of the engine's workspace.  The test calls it through
-the C ABI and compares it with ig_cfft_exec_device on the same inputs, twice
-in a row (the array keeps the previous call's contents), for a single-CTA
-length and for four-step lengths, and checks the size limit.  This file is
-collected last so that a first-failure run has already run every other test.
+Callers that cannot allocate device memory while they run -- a process whose
+device-memory budget is reserved up front in a pool that must not grow, or a
+latency-bound loop where cudaMalloc / cudaFree are not allowed -- use this
+call; its scratch is a static device array instead of the engine's cached
+workspace.  The test calls it through the C ABI and compares it with
+ig_cfft_exec_device and with the FP64 oracle on the same inputs, twice in a
+row (the array keeps the previous call's contents), for a single-CTA length
+and for four-step lengths, and checks the size limit.  This file is collected
+last so that a first-failure run has already run every other test.
 """
 import ctypes as C
 
@@ -32,7 +34,7 @@ def _run(lib, fn, plan, x, fwd, fct):
 
 @pytest.mark.parametrize("n,b", [(4096, 8), (32768, 4), (65536, 3), (1 << 20, 2)])
 @pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
-def test_noalloc_matches_exec_device(engine, n, b, dtype):
+def test_noalloc_matches_exec_device(engine, oracle_lib, n, b, dtype):
     from impulse_gb300 import _lib as L
     lib = engine
     code = L.IG_F64 if dtype == np.complex128 else L.IG_F32
@@ -49,6 +51,11 @@ def test_noalloc_matches_exec_device(engine, n, b, dtype):
             assert rc1 == 0, lib.ig_last_error_string()
             err = np.linalg.norm(got - want) / np.linalg.norm(want)
             assert err <= TOL[dtype], (n, b, call, err)
+            # and against the FP64 oracle on the same input
+            ref = oracle_lib.cfft(x.astype(np.complex128), fwd, 0.5)
+            tol = 1e-12 if dtype == np.complex128 else 1e-6 * np.log2(n)
+            err_o = oracle_lib.rel_l2(got, ref)
+            assert err_o <= tol, (n, b, call, err_o)
     finally:
         lib.ig_destroy_cfft_plan(plan)
 
