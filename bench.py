@@ -294,7 +294,7 @@ def run_ours(args, rank, world):
 
     # FP32 form of the same workload, and its error against the FP64 result
     items32 = make("f32")
-    ms32, _, _ = timed(items32, args.steps, args.warmup)
+    ms32, _, per32 = timed(items32, args.steps, args.warmup, per_length=True)
     ms32 = max_over_ranks(ms32)
     errs = []
     for (n, b, x64, y64, _), (_, _, x32, y32, _) in zip(items64, items32):
@@ -401,16 +401,22 @@ def run_ours(args, rank, world):
                  "ms_per_step": round(ms32 / args.steps, 4),
                  "speedup_vs_f64": round(ms64 / ms32, 3),
                  "max_rel_l2_vs_f64": max(e for _, e in errs),
-                 "bound_1e-6_log2N": all(e <= 1e-6 * math.log2(n) for n, e in errs)},
+                 "bound_1e-6_log2N": all(e <= 1e-6 * math.log2(n) for n, e in errs),
+                 "per_length_gbs": [(n, round(2 * 4 * n * b / (t / 1e3) / 1e9, 1))
+                                    for (n, b, *_), t in zip(items32, per32)]},
         "per_length_gbs": slow,
     }
+    keep = [] if (rank == 0 and world == 1 and not args.no_cpu) else None
     if not args.no_extra:
+        result.update(run_nd(lib, dev, args, peak, keep))
         result["uneven"] = run_uneven(lib, dev, world, args)
-        result["conv"] = run_conv(dev, args)
+        result["conv"] = run_conv(dev, args, peak)
     if rank == 0 and world == 1 and not args.no_cpu:
         gbs, nth, sample, _ = cpu_sample_run(lengths, min_seconds=args.cpu_seconds)
         result["cpu_baseline"] = {"value": round(gbs, 3), "unit": "GB/s", "cores": nth, "kind": "port",
                                   "sample": sample}
+        if keep:
+            result["cpu_baseline"]["configs_1_3"] = cpu_nd_check(keep)
     return result
 
 
@@ -467,7 +473,7 @@ def run_uneven(lib, dev, world, args):
     return out
 
 
-def run_conv(dev, args):
+def run_conv(dev, args, peak):
     """64 images 2048x2048 f32 convolved ('same') with 31x31 filters (one per
     image), zero padded to 4096x4096: forward + backward (adjoints wrt image and
     filter, spectra recomputed)."""
@@ -500,11 +506,162 @@ def run_conv(dev, args):
     fwd = e0.elapsed_time(e1) / reps
     bwd = e1.elapsed_time(e2) / reps
     io_bytes = 2 * 4 * B * H * H + 4 * B * K * K  # images in, result out, filters
+    # FFT-pipeline bytes of one forward call, per image: pad (image in, padded
+    # out), 2-D r2c of the padded image and of the padded filter (row pass:
+    # reals in, half spectrum out; column pass: half spectrum in and out), the
+    # spectrum product (two spectra in, one out), 2-D c2r (column pass, then
+    # row pass: half spectrum in, reals out), crop (region in and out)
+    real_p, half_p = 4 * P * P, 8 * P * (P // 2 + 1)
+    r2c2d = (real_p + half_p) + 2 * half_p
+    per_image = (4 * H * H + real_p) + r2c2d + real_p + r2c2d + 3 * half_p + r2c2d + 2 * 4 * H * H
+    pipe_gbs = B * per_image / (fwd / 1e3) / 1e9
     del op, x, k, gy
     torch.cuda.empty_cache()
     return {"workload": "64 x 2048^2 f32, 31x31 filter per image, padded to 4096^2", "forward_ms": round(fwd, 2),
             "backward_ms": round(bwd, 2), "images_per_s_fwd_bwd": round(B / ((fwd + bwd) / 1e3), 1),
-            "forward_io_gbs": round(io_bytes / (fwd / 1e3) / 1e9, 1)}
+            "forward_io_gbs": round(io_bytes / (fwd / 1e3) / 1e9, 1),
+            "forward_pipeline_bytes": B * per_image, "forward_pipeline_gbs": round(pipe_gbs, 1),
+            "forward_pipeline_frac": round(pipe_gbs / peak, 4)}
+
+
+def _nd_call(lib, kind, code, x, y, axes, fwd, fct, stream):
+    """ig_{kind}_device on torch tensors (byte strides from the tensors)."""
+    shp = list(y.shape) if kind == "c2r" else list(x.shape)
+    si = [st * x.element_size() for st in x.stride()]
+    so = [st * y.element_size() for st in y.stride()]
+    arr = lambda t, v: (t * len(v))(*v)
+    rc = getattr(lib, f"ig_{kind}_device")(code, len(shp), arr(C.c_size_t, shp), arr(C.c_ssize_t, si),
+                                           arr(C.c_ssize_t, so), len(axes), arr(C.c_size_t, list(axes)), int(fwd),
+                                           x.data_ptr(), y.data_ptr(), float(fct), stream)
+    if rc:
+        raise RuntimeError(lib.ig_last_error_string().decode())
+
+
+def _event_ms(fn, reps, stream):
+    import torch
+    for _ in range(2):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_nd(lib, dev, args, peak, keep=None):
+    """Configs 1 and 3 through the N-d device entry points (pocketfft::c2c / r2c
+    mirrors), device-resident, event-timed.  GB/s counts one read and one write
+    of the whole array per call whatever the number of axes (a call that makes
+    P passes over HBM is capped at 1/P of the roofline); `launches` is the
+    engine's kernel count per call.  `keep` collects (name, input, output,
+    axes, kind) on the host for the oracle check of the CPU leg."""
+    import torch
+    from impulse_gb300 import _lib as L
+    stream = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    reps = max(3, args.steps)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    out = {}
+
+    def uniform_c(shape, dt):
+        rdt = torch.float64 if dt == torch.complex128 else torch.float32
+        return torch.complex(torch.rand(shape, generator=g, device=dev, dtype=rdt) * 2 - 1,
+                             torch.rand(shape, generator=g, device=dev, dtype=rdt) * 2 - 1)
+
+    # config 1: c128, N = 4096, 1024 lines (both axis orders) and 16384 lines (2^26 elements)
+    c1 = {}
+    for name, shape, axes in (("4096x1024_axes0", (4096, 1024), [0]), ("1024x4096_axes1", (1024, 4096), [1]),
+                              ("16384x4096_axes1", (16384, 4096), [1])):
+        x = uniform_c(shape, torch.complex128)
+        y = torch.empty_like(x)
+        z = torch.empty_like(x)
+        nb = 2 * 16 * x.numel()
+        lib.ig_launch_count(1)
+        _nd_call(lib, "c2c", L.IG_F64, x, y, axes, True, 1.0, sp)
+        torch.cuda.synchronize()
+        launches = int(lib.ig_launch_count(0))
+        tf = _event_ms(lambda: _nd_call(lib, "c2c", L.IG_F64, x, y, axes, True, 1.0, sp), reps, stream)
+        tb = _event_ms(lambda: _nd_call(lib, "c2c", L.IG_F64, y, z, axes, False, 1.0 / 4096, sp), reps, stream)
+        rt = float(torch.linalg.vector_norm(z - x) / torch.linalg.vector_norm(x))
+        gf, gb = nb / tf / 1e6, nb / tb / 1e6
+        c1[name] = {"forward_ms": round(tf, 4), "backward_ms": round(tb, 4), "forward_gbs": round(gf, 1),
+                    "backward_gbs": round(gb, 1), "frac_forward": round(gf / peak, 4),
+                    "frac_backward": round(gb / peak, 4), "launches": launches,
+                    "round_trip_rel_l2": rt, "round_trip_ok_1e-10": rt <= 1e-10}
+        if keep is not None and name != "16384x4096_axes1":
+            keep.append(("config1_" + name, x.cpu().numpy(), y.cpu().numpy(), axes, "c2c"))
+        del x, y, z
+        torch.cuda.empty_cache()
+    out["config1"] = {"dtype": "c128 (double-float butterflies)", "api": "ig_c2c_device", **c1}
+
+    # config 3: multi-axis
+    c3 = {}
+    for name, shape, axes, dt in (("c128_4096x4096_axes01", (4096, 4096), [0, 1], torch.complex128),
+                                  ("c64_4096x4096_axes01", (4096, 4096), [0, 1], torch.complex64),
+                                  ("c64_256x256x256_axes012", (256, 256, 256), [0, 1, 2], torch.complex64)):
+        code = L.IG_F64 if dt == torch.complex128 else L.IG_F32
+        x = uniform_c(shape, dt)
+        y = torch.empty_like(x)
+        nb = 2 * x.element_size() * x.numel()
+        lib.ig_launch_count(1)
+        _nd_call(lib, "c2c", code, x, y, axes, True, 1.0, sp)
+        torch.cuda.synchronize()
+        launches = int(lib.ig_launch_count(0))
+        t = _event_ms(lambda: _nd_call(lib, "c2c", code, x, y, axes, True, 1.0, sp), reps, stream)
+        c3[name] = {"ms": round(t, 4), "gbs": round(nb / t / 1e6, 1), "frac": round(nb / t / 1e6 / peak, 4),
+                    "launches": launches}
+        if keep is not None:
+            keep.append(("config3_" + name, x.cpu().numpy(), y.cpu().numpy(), axes, "c2c"))
+        del x, y
+        torch.cuda.empty_cache()
+    x = torch.rand((4096, 4096), generator=g, device=dev) * 2 - 1
+    y = torch.empty((4096, 2049), dtype=torch.complex64, device=dev)
+    z = torch.empty_like(x)
+    nb = 4 * x.numel() + 8 * y.numel()
+    lib.ig_launch_count(1)
+    _nd_call(lib, "r2c", L.IG_F32, x, y, [0, 1], True, 1.0, sp)
+    torch.cuda.synchronize()
+    launches = int(lib.ig_launch_count(0))
+    t = _event_ms(lambda: _nd_call(lib, "r2c", L.IG_F32, x, y, [0, 1], True, 1.0, sp), reps, stream)
+    tb = _event_ms(lambda: _nd_call(lib, "c2r", L.IG_F32, y, z, [0, 1], False, 1.0 / 4096 ** 2, sp), reps, stream)
+    rt = float(torch.linalg.vector_norm(z - x) / torch.linalg.vector_norm(x))
+    c3["r2c_f32_4096x4096_axes01"] = {"ms": round(t, 4), "gbs": round(nb / t / 1e6, 1),
+                                      "frac": round(nb / t / 1e6 / peak, 4), "launches": launches,
+                                      "c2r_ms": round(tb, 4), "c2r_gbs": round(nb / tb / 1e6, 1),
+                                      "round_trip_rel_l2": rt}
+    if keep is not None:
+        keep.append(("config3_r2c_f32_4096x4096_axes01", x.cpu().numpy(), y.cpu().numpy(), [0, 1], "r2c"))
+    del x, y, z
+    torch.cuda.empty_cache()
+    out["config3"] = {"api": "ig_c2c_device / ig_r2c_device / ig_c2r_device",
+                      "note": "one read + one write of the array credited per call; a call of P passes is "
+                              "capped at 1/P of the roofline", **c3}
+    return out
+
+
+def cpu_nd_check(keep):
+    """CPU-baseline leg of configs 1 and 3: the oracle on the same inputs on
+    all host cores -- its time (GB/s on the same algorithmic bytes) and the
+    GPU result's relative L2 error against it."""
+    from oracle import oracle as O  # CPU-baseline leg only
+    nth = os.cpu_count() or 1
+    res = {}
+    for name, x, y, axes, kind in keep:
+        t0 = time.perf_counter()
+        if kind == "c2c":
+            want = O.c2c(x.astype(np.complex128), axes, True, nthreads=nth)
+        else:
+            want = O.r2c(x.astype(np.float64), axes, True, nthreads=nth)
+        el = time.perf_counter() - t0
+        nb = x.nbytes + y.nbytes
+        res[name] = {"cpu_gbs": round(nb / el / 1e9, 3), "cpu_cores": nth, "kind": "port",
+                     "gpu_rel_l2_vs_oracle": O.rel_l2(y, want)}
+    return res
 
 
 PROFILE_CASES = {

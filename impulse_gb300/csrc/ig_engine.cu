@@ -429,7 +429,9 @@ static void build_chirp(Core &c, long long M, long long L, void *&chirp, void *&
     count_launch();
     ck(launch_pad_chirp64(bk64.p, pad.p, M, L), "chirp padding");
     count_launch();
-    auto dfcore = get_core(A_DF, L, false);
+    // the padded chirp's spectrum in FP64-class arithmetic: native FP64 for
+    // native-FP64 plans, double-float otherwise
+    auto dfcore = get_core(c.a == A_F64 ? A_F64 : A_DF, L, false);
     run_core_on_device(*dfcore, pad.p, pad.p, 1, 1, 1.0, 0);
     chirp = c.alloc(M * slot_bytes(c.a));
     chirpf = c.alloc(L * slot_bytes(c.a));
@@ -522,7 +524,7 @@ static void build_rader(Core &c, long long M)
     ck(cudaMemcpy(dout, rout.data(), M * sizeof(int), cudaMemcpyHostToDevice), "rader tables");
     DevBuf b64(L * 16);
     ck(cudaMemcpy(b64.p, b.data(), L * 16, cudaMemcpyHostToDevice), "rader tables");
-    auto dfcore = get_core(A_DF, L, false);
+    auto dfcore = get_core(c.a == A_F64 ? A_F64 : A_DF, L, false);
     run_core_on_device(*dfcore, b64.p, b64.p, 1, 1, 1.0 / (double)L, 0);
     void *bf = c.alloc(L * slot_bytes(c.a));
     launch_convert_a(c.a, b64.p, bf, L);
@@ -658,12 +660,28 @@ static std::shared_ptr<Core> get_core(Arith a, long long M, bool real_tw)
 // --------------------------------------------------------------------------
 // launching the shared-memory kernel
 // --------------------------------------------------------------------------
-static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
+// k_fft_line serves Stockham cores of two or more stages on lines addressed
+// by the batch dimensions (rows: consecutive threads walk a line's units)
+// with the plain complex layout or the even real -> halfcomplex one
+static const bool g_line_kernel = getenv("IG_NO_LINE_KERNEL") == nullptr;
+static bool line_kernel_ok(Arith a, const CoreDesc &d, const IODesc &io)
 {
-    if (io.nlines <= 0) return;
+    if (!g_line_kernel || (a != A_F32 && a != A_DF) || d.blue != 0 || d.nst < 2 || d.L != d.M) return false;
+    if (d.rs == RS_FULL || !line_edge_ok(d.st[0].R) || !line_edge_ok(d.st[d.nst - 1].R)) return false;
+    if (io.cols_in || io.cols_out || io.loff_in || io.loff_out || io.pair || io.split_N1) return false;
+    if (io.lay == LAY_C2C) return io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C;
+    if (io.lay == LAY_R2HC)
+        return io.post == POST_SPLIT && io.in_kind == IN_C && io.out_kind == OUT_HC && io.nreal == 2LL * d.M &&
+               line_r2hc_last_ok(d.st[d.nst - 1].R);
+    return false;
+}
+
+// lines per CTA of a shared-memory launch of core d
+static long long smem_lpc(Arith a, const CoreDesc &d, const IODesc &io, long long &line_bytes)
+{
     const long long tpl = (d.L + d.E - 1) / d.E;
     // double-buffered stages: two line buffers
-    const long long line_bytes = (long long)d.LS * (long long)slot_bytes(a) * (d.db ? 2 : 1);
+    line_bytes = (long long)d.LS * (long long)slot_bytes(a) * (d.db ? 2 : 1);
     const int smax = max_smem();
     long long lpc = std::max<long long>(1, 256 / tpl);
     if (io.cols_in || io.cols_out) lpc = std::max<long long>(lpc, 8);
@@ -673,7 +691,38 @@ static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
     // keep three (or two) CTAs per SM when a line is small enough
     long long budget = line_bytes * 3 <= smax ? smax / 3 : line_bytes * 2 <= smax ? smax / 2 : smax;
     lpc = std::min<long long>(lpc, std::max<long long>(1, budget / line_bytes));
-    lpc = std::min<long long>(lpc, std::max<long long>(1, io.nlines));
+    return std::min<long long>(lpc, std::max<long long>(1, io.nlines));
+}
+
+static void launch_smem(Arith a, const CoreDesc &d_in, IODesc io, cudaStream_t st)
+{
+    if (io.nlines <= 0) return;
+    CoreDesc dv = d_in;
+    long long line_bytes = 0;
+    long long lpc = smem_lpc(a, dv, io, line_bytes);
+    // lines walked across (strided axes): each row of a CTA's lines should fill
+    // a 32-byte sector; when double buffering or 8 elements per thread leave
+    // room for fewer lines, single-buffered 16-element stages take more
+    if ((io.cols_in || io.cols_out) && d_in.lpc_pref <= 0 && (dv.E == 8 || dv.db)) {
+        const long long ue = io.in_kind == IN_C || io.in_kind == IN_P ? 2 * (long long)store_real_bytes(a)
+                                                                      : (long long)store_real_bytes(a);
+        const long long want = std::max<long long>(1, 32 / ue);
+        if (lpc < want && lpc < io.nlines) {
+            CoreDesc d2 = dv;
+            d2.E = 16;
+            d2.db = 0;
+            long long lb2 = 0;
+            const long long lpc2 = smem_lpc(a, d2, io, lb2);
+            if (lpc2 > lpc) {
+                dv = d2;
+                lpc = lpc2;
+                line_bytes = lb2;
+            }
+        }
+    }
+    const CoreDesc &d = dv;
+    const long long tpl = (d.L + d.E - 1) / d.E;
+    const int smax = max_smem();
     if (io.post == POST_SPLIT4) lpc = std::max<long long>(2, lpc & ~1LL);  // whole row pairs per CTA
     io.lpc = (int)lpc;
     io.tpl = (int)tpl;
@@ -690,9 +739,13 @@ static void launch_smem(Arith a, const CoreDesc &d, IODesc io, cudaStream_t st)
     });
     long long grid = (io.nlines + lpc - 1) / lpc;
     if (grid > 0x7fffffffLL) raise(IG_ETOOLARGE, "too many lines for one launch");
-    cudaError_t e = a == A_F32 ? Launch<TagF32>::fft_smem(d, io, smem, st)
-                  : a == A_DF  ? Launch<TagDF>::fft_smem(d, io, smem, st)
-                               : Launch<TagF64>::fft_smem(d, io, smem, st);
+    cudaError_t e;
+    if (line_kernel_ok(a, d, io))
+        e = a == A_F32 ? Launch<TagF32>::fft_line(d, io, smem, st) : Launch<TagDF>::fft_line(d, io, smem, st);
+    else
+        e = a == A_F32 ? Launch<TagF32>::fft_smem(d, io, smem, st)
+          : a == A_DF  ? Launch<TagDF>::fft_smem(d, io, smem, st)
+                       : Launch<TagF64>::fft_smem(d, io, smem, st);
     ck(e, "fft kernel launch");
     count_launch();
 }

@@ -16,6 +16,9 @@ template <> struct TagType<TagF64> { using T = double; };
 template <class T, int E, bool DB>
 cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
 template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes);
+template <class T, int E, bool DB>
+cudaError_t launch_line_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
+template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes);
 
 template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
@@ -23,6 +26,17 @@ template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const 
     return d.E == 8 ? launch_fft_E<T, 8, true>(d, io, smem, st)
          : d.db     ? launch_fft_E<T, 16, true>(d, io, smem, st)
                     : launch_fft_E<T, 16, false>(d, io, smem, st);
+}
+template <class Tag> cudaError_t Launch<Tag>::fft_line(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    if constexpr (std::is_same<T, double>::value) {
+        return cudaErrorNotSupported;  // native FP64 runs k_fft_smem only
+    } else {
+        return d.E == 8 ? launch_line_E<T, 8, true>(d, io, smem, st)
+             : d.db     ? launch_line_E<T, 16, true>(d, io, smem, st)
+                        : launch_line_E<T, 16, false>(d, io, smem, st);
+    }
 }
 template <class K> static cudaError_t set_smem_attr(K kernel, int bytes)
 {
@@ -39,6 +53,11 @@ template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
     if ((e = set_smem_E<T, 8, true>(bytes)) != cudaSuccess) return e;
     if ((e = set_smem_E<T, 16, false>(bytes)) != cudaSuccess) return e;
     if ((e = set_smem_E<T, 16, true>(bytes)) != cudaSuccess) return e;
+    if constexpr (!std::is_same<T, double>::value) {
+        if ((e = set_smem_line_E<T, 8, true>(bytes)) != cudaSuccess) return e;
+        if ((e = set_smem_line_E<T, 16, false>(bytes)) != cudaSuccess) return e;
+        if ((e = set_smem_line_E<T, 16, true>(bytes)) != cudaSuccess) return e;
+    }
     return set_smem_attr(k_fft_worklist<T, 16>, bytes);
 }
 template <class Tag>

@@ -16,6 +16,9 @@ struct TagF64 {};
 template <class Tag> struct Launch {
     // k_fft_smem with `lpc` lines of `tpl` threads per CTA and `smem` bytes
     static cudaError_t fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
+    // k_fft_line (first / last stages fused with the HBM reads / writes): the
+    // same descriptors, for complex lines and even real lines to halfcomplex
+    static cudaError_t fft_line(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
     static cudaError_t set_max_smem(int bytes);
     static cudaError_t fft_worklist(const WorkGroup *groups, const long long *prefix, int ngroups,
                                     unsigned long long total, unsigned long long *counter, const void *in, void *out,

@@ -1,0 +1,416 @@
+// ig_line.cuh -- k_fft_line: single-CTA Stockham transforms of whole lines
+// with the HBM traffic fused into the first and last stages.
+//
+// k_fft_smem stages a line into shared memory in a prologue pass, runs every
+// Stockham stage shared memory -> registers -> shared memory, and writes the
+// line back in an epilogue pass (with one more pass for the real split).  For
+// the two layouts that carry the bulk of the work -- complex lines
+// (pocketfft::c2c, pocketfft_hdronly.h:3272; cfft_forward / cfft_backward,
+// impulse/fft/c_pocketfft/pocketfft.c:2160-2170) and real lines of even
+// length written as halfcomplex (rfft_forward, pocketfft.c:2184) -- this
+// kernel:
+//   * runs the first stage (ns = 1, no twiddles) on units loaded straight from
+//     HBM into registers: butterfly j of a line reads units j + m L/R, so
+//     consecutive threads read consecutive units;
+//   * runs the last stage from shared memory straight to HBM: its outputs
+//     j + m L/R are the natural order, again consecutive per warp;
+//   * for the halfcomplex layout, gives each thread the mirror butterflies j
+//     and L/R - j of the last stage: their outputs are the partner bins Z[k]
+//     and Z[M - k] of the real split, which is computed in registers and
+//     written as X[k], X[M - k] (T = w^k (-i)(Z[k] - conj Z[M-k]),
+//     X[k] = Z[k] + conj Z[M-k] + T, X[M-k] = conj(Z[k] + conj Z[M-k] - T),
+//     the 1/2 folded into the output scale).
+// Two shared-memory round trips and two barriers per line go away; the middle
+// stages are k_fft_smem's.  Double-float lines are range-checked on the
+// loaded values: a line whose largest element lies outside 2^+-40 gets an
+// exact power-of-two scale, as in k_fft_smem.
+#pragma once
+#include "ig_kernels.cuh"
+
+namespace ig {
+
+constexpr int LK_C2C = 0;   // complex units in, complex units out
+constexpr int LK_R2HC = 1;  // real pairs in (as complex units), halfcomplex out
+
+// biased double exponent field, from the high word only
+__device__ __forceinline__ unsigned dexpw(double x)
+{
+    return ((unsigned)(__double_as_longlong(x) >> 32) >> 20) & 0x7ffu;
+}
+
+// First stage: load, (double-float: range check), convert, radix-R DFT, write
+// the Stockham positions j R + m of buffer `line`.  Returns the line's
+// exponent scale (0 for FP32).
+template <class T, int E, int R>
+__device__ __forceinline__ int line_first(cx<T> *line, const char *base, long long is, const CoreDesc &P, int tpl,
+                                          int t, bool act, bool cc, int g, int *s_emax, int *s_flag)
+{
+    using S2 = typename Traits<T>::S2;
+    using B = Bfly<T>;
+    using V = typename B::V;
+    constexpr bool RAW = Traits<T>::kRaw;
+    constexpr int NB = (E + R - 1) / R;
+    const int nr = P.L / R, pad = P.pad;
+    S2 raw[NB][R];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        const int j = t + i * tpl;
+        if (act && j < nr) {
+            const char *p = base + (long long)j * is;
+            const long long step = (long long)nr * is;
+#pragma unroll
+            for (int m = 0; m < R; ++m) raw[i][m] = ldg_s<S2>(p + m * step);
+        }
+    }
+    int esc = 0;
+    if constexpr (RAW) {
+        unsigned emax = 0;
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            const int j = t + i * tpl;
+            if (act && j < nr) {
+#pragma unroll
+                for (int m = 0; m < R; ++m) emax = max(emax, max(dexpw(raw[i][m].x), dexpw(raw[i][m].y)));
+            }
+        }
+        // common case: every thread's largest exponent inside the safe window
+        // (all-zero and non-finite maxima are left alone); otherwise the CTA
+        // takes the exact per-line maximum
+        const bool out = emax != 0 && emax != 0x7ffu && (emax > 1023u + 40u || emax < 1023u - 40u);
+        if (out) *s_flag = 1;
+        __syncthreads();
+        if (*s_flag) {
+            if (act && emax != 0x7ffu) atomicMax(&s_emax[g], (int)emax);
+            __syncthreads();
+            const int ea = act ? s_emax[g] : 0;
+            if (ea != 0 && (ea > 1023 + 40 || ea < 1023 - 40)) esc = 1023 - ea;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        const int j = t + i * tpl;
+        if (act && j < nr) {
+            V v[R];
+#pragma unroll
+            for (int m = 0; m < R; ++m) {
+                cx<T> z{Store<T>::in(raw[i][m].x, esc), Store<T>::in(raw[i][m].y, esc)};
+                if (cc) z = conjx(z);
+                if constexpr (std::is_same<T, df>::value) v[m] = to_p(z);
+                else v[m] = z;
+            }
+            B::template dft<R>(v);
+            const int base_i = j * R;
+#pragma unroll
+            for (int m = 0; m < R; ++m) B::st(line + sp(base_i + m, pad), v[m]);
+        }
+        asm volatile("" ::: "memory");
+    }
+    return esc;
+}
+
+// value of a butterfly output as a plain complex (double-float renormalised)
+template <class T> __device__ __forceinline__ cx<T> line_val(const typename Bfly<T>::V &v)
+{
+    if constexpr (std::is_same<T, df>::value) return from_p(prenorm(v));
+    else return v;
+}
+
+// Last stage of a complex line: butterfly j (q = 0, k = j) reads units
+// j + m nr of `src`, twiddles, DFT, and writes units j + m nr of the output
+// line with the output scale (conjugated for a backward transform).
+template <class T, int E, int R>
+__device__ __forceinline__ void line_last_c2c(const cx<T> *src, char *obase, long long os, const CoreDesc &P, int si,
+                                              int tpl, int t, bool act, bool cc, const OutScale<T> &sc, int esc)
+{
+    using S2 = typename Traits<T>::S2;
+    using B = Bfly<T>;
+    using V = typename B::V;
+    constexpr int NB = (E + R - 1) / R;
+    const int nr = P.L / R, pad = P.pad;
+    const typename B::W *tw = reinterpret_cast<const typename B::W *>(P.tw) + P.st[si].tw;
+    if (!act) return;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        const int j = t + i * tpl;
+        if (j < nr) {
+            V v[R];
+#pragma unroll
+            for (int m = 0; m < R; ++m) v[m] = B::ld(src + sp(j + m * nr, pad));
+            if (j) {
+                const typename B::W *twk = tw + j * (R - 1) - 1;
+#pragma unroll
+                for (int m = 1; m < R; ++m) v[m] = B::tw(v[m], twk + m, P);
+            }
+            B::template dft<R>(v);
+            char *p = obase + (long long)j * os;
+            const long long step = (long long)nr * os;
+#pragma unroll
+            for (int m = 0; m < R; ++m) {
+                cx<T> z = line_val<T>(v[m]);
+                if (cc) z.i = -z.i;
+                S2 o;
+                o.x = sc.apply(z.r, esc);
+                o.y = sc.apply(z.i, esc);
+                stg_s<S2>(p + m * step, o);
+            }
+        }
+        asm volatile("" ::: "memory");
+    }
+}
+
+// real split of the partner bins a = Z[k], b = Z[M - k] and the halfcomplex
+// stores of X[k] and X[M - k]; sc carries fct / 2
+template <class T>
+__device__ __forceinline__ void line_split_store(cx<T> a, cx<T> b, int k, int M, const cx<T> *rtw, char *obase,
+                                                 long long os, const OutScale<T> &sc, int esc, const CoreDesc &P)
+{
+    using S = typename Traits<T>::S;
+    cx<T> X, Y;  // X[k], X[M - k]
+    if constexpr (std::is_same<T, df>::value) {
+        const f2p cj = pk(1.0f, -1.0f);
+        const pcx pa = to_p(a), pc = plane(to_p(b), cj);  // a, conj b
+        const pcx Ev = pa + pc, D = pa - pc;
+        const pcx Tm = pmulw_cx<true>(prot<true>(D), rtw + k, P.neg1);  // w^k (-i) D
+        X = from_p(prenorm(Ev + Tm));
+        Y = from_p(prenorm(plane(Ev - Tm, cj)));
+    } else {
+        const cx<T> c{b.r, -b.i};
+        const cx<T> Ev = a + c, D = a - c;
+        const cx<T> Tm = cmul(cx<T>{D.i, -D.r}, rtw[k]);
+        X = Ev + Tm;
+        const cx<T> Z = Ev - Tm;
+        Y = cx<T>{Z.r, -Z.i};
+    }
+    const int k2 = M - k;
+    if (k == 0) {
+        stg_s<S>(obase, sc.apply(X.r, esc));
+    } else {
+        char *p = obase + (2 * (long long)k - 1) * os;
+        stg_s<S>(p, sc.apply(X.r, esc));
+        stg_s<S>(p + os, sc.apply(X.i, esc));
+    }
+    if (k2 != k) {
+        if (k2 == M) {
+            stg_s<S>(obase + (2 * (long long)M - 1) * os, sc.apply(Y.r, esc));
+        } else {
+            char *p = obase + (2 * (long long)k2 - 1) * os;
+            stg_s<S>(p, sc.apply(Y.r, esc));
+            stg_s<S>(p + os, sc.apply(Y.i, esc));
+        }
+    }
+}
+
+// Last stage of an even real line (M = L complex points of the packed line):
+// pair slot p holds butterflies p and nr - p; output m of butterfly p is
+// Z[p + m nr], whose partner Z[M - p - m nr] is output R - 1 - m of butterfly
+// nr - p (for p = 0: output R - m of butterfly 0; for 2p = nr: output
+// R - 1 - m of butterfly p itself).
+template <class T, int E, int R>
+__device__ __forceinline__ void line_last_r2hc(const cx<T> *src, char *obase, long long os, const CoreDesc &P,
+                                               int si, int tpl, int t, bool act, const OutScale<T> &sc, int esc)
+{
+    using B = Bfly<T>;
+    using V = typename B::V;
+    const int M = P.L, nr = M / R, pad = P.pad, nslot = nr / 2 + 1;
+    const typename B::W *tw = reinterpret_cast<const typename B::W *>(P.tw) + P.st[si].tw;
+    const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
+    if (!act) return;
+    for (int p = t; p < nslot; p += tpl) {
+        const int pb = nr - p;
+        const bool two = p != 0 && 2 * p != nr;
+        V va[R], vb[R];
+#pragma unroll
+        for (int m = 0; m < R; ++m) va[m] = B::ld(src + sp(p + m * nr, pad));
+        if (two) {
+#pragma unroll
+            for (int m = 0; m < R; ++m) vb[m] = B::ld(src + sp(pb + m * nr, pad));
+        }
+        if (p) {
+            const typename B::W *twk = tw + p * (R - 1) - 1;
+#pragma unroll
+            for (int m = 1; m < R; ++m) va[m] = B::tw(va[m], twk + m, P);
+        }
+        if (two) {
+            const typename B::W *twk = tw + pb * (R - 1) - 1;
+#pragma unroll
+            for (int m = 1; m < R; ++m) vb[m] = B::tw(vb[m], twk + m, P);
+        }
+        B::template dft<R>(va);
+        if (two) {
+            B::template dft<R>(vb);
+#pragma unroll
+            for (int m = 0; m < R; ++m)
+                line_split_store<T>(line_val<T>(va[m]), line_val<T>(vb[R - 1 - m]), p + m * nr, M, rtw, obase, os, sc,
+                                    esc, P);
+        } else if (p == 0) {
+            // k = m nr, partner (R - m) nr (m = 0: k = 0 with itself)
+#pragma unroll
+            for (int m = 0; m < R; ++m) {
+                const int mp = m == 0 ? 0 : R - m;
+                if (m <= mp)
+                    line_split_store<T>(line_val<T>(va[m]), line_val<T>(va[mp]), m * nr, M, rtw, obase, os, sc, esc, P);
+            }
+        } else {
+            // 2 p = nr: k = p + m nr, partner p + (R - 1 - m) nr
+#pragma unroll
+            for (int m = 0; m < R; ++m) {
+                const int mp = R - 1 - m;
+                if (m <= mp)
+                    line_split_store<T>(line_val<T>(va[m]), line_val<T>(va[mp]), p + m * nr, M, rtw, obase, os, sc,
+                                        esc, P);
+            }
+        }
+        asm volatile("" ::: "memory");
+    }
+}
+
+#define IG_LINE_RADIX_SWITCH(RV, CALL)                                                \
+    switch (RV) {                                                                      \
+    case 2: { constexpr int R_ = 2; CALL; } break;                                     \
+    case 4: { constexpr int R_ = 4; CALL; } break;                                     \
+    case 8: { constexpr int R_ = 8; CALL; } break;                                     \
+    case 16: if constexpr (rs_has<E, RS>(16)) { constexpr int R_ = 16; CALL; } break;  \
+    case 3: if constexpr (rs_has<E, RS>(3)) { constexpr int R_ = 3; CALL; } break;     \
+    case 5: if constexpr (rs_has<E, RS>(5)) { constexpr int R_ = 5; CALL; } break;     \
+    case 9: if constexpr (rs_has<E, RS>(9)) { constexpr int R_ = 9; CALL; } break;     \
+    case 7: if constexpr (rs_has<E, RS>(7)) { constexpr int R_ = 7; CALL; } break;     \
+    case 11: if constexpr (rs_has<E, RS>(11)) { constexpr int R_ = 11; CALL; } break;  \
+    case 13: if constexpr (rs_has<E, RS>(13)) { constexpr int R_ = 13; CALL; } break;  \
+    default: break;                                                                    \
+    }
+
+// first / last stages: radices 2, 4, 8, 16 and 3, 5 (plans with another first
+// or last radix run k_fft_smem, see line_edge_ok)
+#define IG_LINE_EDGE_SWITCH(RV, CALL)                                                \
+    switch (RV) {                                                                      \
+    case 2: { constexpr int R_ = 2; CALL; } break;                                     \
+    case 4: { constexpr int R_ = 4; CALL; } break;                                     \
+    case 8: { constexpr int R_ = 8; CALL; } break;                                     \
+    case 16: if constexpr (rs_has<E, RS>(16)) { constexpr int R_ = 16; CALL; } break;  \
+    case 3: if constexpr (rs_has<E, RS>(3)) { constexpr int R_ = 3; CALL; } break;     \
+    case 5: if constexpr (rs_has<E, RS>(5)) { constexpr int R_ = 5; CALL; } break;     \
+    default: break;                                                                    \
+    }
+
+// register caps: 512-thread CTAs (lines of 4096 / 8192 units) must fit the
+// 64 K register file; FP32 8-element complex lines run two such CTAs per SM
+template <class T, int E, int RS, int K, bool DB> constexpr int fft_line_regs()
+{
+    if constexpr (std::is_same<T, df>::value) return 128;
+    return E == 8 ? (K == LK_C2C ? 64 : 72) : 128;
+}
+
+// One CTA: `lpc` lines of `tpl` threads; shared memory lpc * LSt complex slots
+// (LSt = 2 LS with double-buffered middle stages).  Requires a Stockham core
+// (no Bluestein / Rader steps) of at least two stages, lines addressed by the
+// batch dimensions, complex units in (contiguous reals as pairs for LK_R2HC)
+// and complex units (LK_C2C) or halfcomplex reals (LK_R2HC) out, and first and
+// last radices with line_edge_ok (LK_R2HC: last radix with line_r2hc_last_ok).
+template <class T, int E, int RS, int K, bool DB>
+__global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, DB>()))
+    k_fft_line(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
+{
+    constexpr bool RAW = Traits<T>::kRaw;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cx<T> *sm = reinterpret_cast<cx<T> *>(smraw);
+    __shared__ int s_emax[kMaxLinesPerCta];
+    __shared__ int s_flag;
+    const int LS = P.LS, LSt = DB ? 2 * LS : LS;
+    const int lpc = io.lpc, tpl = io.tpl;
+    const long long line0 = (long long)blockIdx.x * lpc;
+    const int nl = (int)min((long long)lpc, io.nlines - line0);
+    const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
+    const bool act = g < nl;
+    const bool cc = K == LK_C2C && !io.fwd;  // backward: forward stages on conjugated data
+    cx<T> *const line = sm + (size_t)(act ? g : 0) * LSt;
+    const char *ibase = io.in + (act ? line_off(io, line0 + g, false) : 0);
+    if constexpr (RAW) {
+        for (int i = threadIdx.x; i < lpc; i += blockDim.x) s_emax[i] = 0;
+        if (threadIdx.x == 0) s_flag = 0;
+        __syncthreads();
+    }
+    int esc = 0;
+    IG_LINE_EDGE_SWITCH(P.st[0].R,
+                        (esc = line_first<T, E, R_>(line, ibase, io.is, P, tpl, t, act, cc, g, s_emax, &s_flag)))
+    __syncthreads();
+    int cur = 0;
+    const int nst = P.nst;
+    for (int s = 1; s < nst - 1; ++s) {
+        if constexpr (DB) {
+            const cx<T> *src = sm + cur;
+            cx<T> *dst = sm + (LS - cur);
+            IG_LINE_RADIX_SWITCH(P.st[s].R, (stage_db<T, E, R_>(src, dst, 2 * LS, P, s, nl, tpl, g, t)))
+            cur = LS - cur;
+            __syncthreads();
+        } else {
+            IG_LINE_RADIX_SWITCH(P.st[s].R, (stage<T, E, R_>(sm, P, s, nl, tpl, g, t)))
+        }
+    }
+    OutScale<T> sc;
+    sc.init(io);
+    char *obase = io.out + (act ? line_off(io, line0 + g, true) : 0);
+    const cx<T> *src = line + cur;
+    if constexpr (K == LK_C2C) {
+        IG_LINE_EDGE_SWITCH(P.st[nst - 1].R,
+                            (line_last_c2c<T, E, R_>(src, obase, io.os, P, nst - 1, tpl, t, act, cc, sc, esc)))
+    } else {
+        // the split's 1/2 joins the output scale
+        if constexpr (std::is_same<T, df>::value) sc.e -= 1;
+        else sc.f *= 0.5f;
+        switch (P.st[nst - 1].R) {
+        case 2: line_last_r2hc<T, E, 2>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc); break;
+        case 4: line_last_r2hc<T, E, 4>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc); break;
+        case 8: line_last_r2hc<T, E, 8>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc); break;
+        case 3:
+            if constexpr (rs_has<E, RS>(3)) line_last_r2hc<T, E, 3>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc);
+            break;
+        case 5:
+            if constexpr (rs_has<E, RS>(5)) line_last_r2hc<T, E, 5>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc);
+            break;
+        default: break;  // other last radices are not sent here (line_r2hc_last_ok)
+        }
+    }
+}
+
+// launch of one (arithmetic, elements per thread, buffering) family: radix
+// class x kind; the radix-13 class has no line variant (line_edge_ok)
+template <class T, int E, bool DB, int RS>
+static void launch_line_rs(const CoreDesc &d, const IODesc &io, unsigned grid, unsigned blk, size_t smem,
+                           cudaStream_t st)
+{
+    if (io.lay == LAY_R2HC) k_fft_line<T, E, RS, LK_R2HC, DB><<<grid, blk, smem, st>>>(d, io);
+    else k_fft_line<T, E, RS, LK_C2C, DB><<<grid, blk, smem, st>>>(d, io);
+}
+
+template <class T, int E, bool DB>
+cudaError_t launch_line_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
+{
+    const unsigned grid = (unsigned)((io.nlines + io.lpc - 1) / io.lpc), blk = (unsigned)(io.lpc * io.tpl);
+    if (d.rs == RS_P2) launch_line_rs<T, E, DB, RS_P2>(d, io, grid, blk, smem, st);
+    else if (E == 8 && d.rs == RS_P235) launch_line_rs<T, E, DB, (E == 8 ? RS_P235 : RS_ALL)>(d, io, grid, blk, smem, st);
+    else if (d.rs == RS_ALL || d.rs == RS_P235) launch_line_rs<T, E, DB, RS_ALL>(d, io, grid, blk, smem, st);
+    else return cudaErrorNotSupported;
+    return cudaGetLastError();
+}
+
+template <class K> static cudaError_t line_smem_attr(K kernel, int bytes)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes - (int)fa.sharedSizeBytes);
+}
+template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes)
+{
+    cudaError_t e = cudaSuccess;
+#define IG_SL(RS_)                                                                                        \
+    if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_C2C, DB>, bytes);                     \
+    if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC, DB>, bytes);
+    IG_SL(RS_P2)
+    IG_SL(RS_ALL)
+    if constexpr (E == 8) { IG_SL(RS_P235) }
+#undef IG_SL
+    return e;
+}
+
+}  // namespace ig

@@ -1,0 +1,8 @@
+// ig_line_df_e8.cu -- k_fft_line variants, double-float arithmetic, 8 elements per thread, double-buffered.
+#include "ig_inst.cuh"
+#include "ig_line.cuh"
+
+namespace ig {
+template cudaError_t launch_line_E<df, 8, true>(const CoreDesc &, const IODesc &, size_t, cudaStream_t);
+template cudaError_t set_smem_line_E<df, 8, true>(int);
+}  // namespace ig

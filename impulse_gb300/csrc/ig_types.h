@@ -33,6 +33,12 @@ constexpr int RS_P235 = 1; // 2, 4, 8, 16, 3, 5, 9
 constexpr int RS_ALL = 2;  // 2, 3, 4, 5, 7, 8, 9, 11, 16
 constexpr int RS_FULL = 3; // all of RS_ALL, 13, and the Rader steps (also the generic-layout kernels)
 
+// last radices of k_fft_line's halfcomplex variant: the two mirror
+// butterflies of a pair slot stay in registers, so larger radices would spill
+constexpr bool line_r2hc_last_ok(int R) { return R == 2 || R == 3 || R == 4 || R == 5 || R == 8; }
+// first and last radices k_fft_line compiles
+constexpr bool line_edge_ok(int R) { return R == 2 || R == 3 || R == 4 || R == 5 || R == 8 || R == 16; }
+
 enum InKind { IN_C = 0, IN_R = 1, IN_P = 2, IN_HC = 3 };
 enum OutKind { OUT_C = 0, OUT_R = 1, OUT_P = 2, OUT_HC = 3 };
 enum PreKind { PRE_NONE = 0, PRE_HERM_EVEN = 1, PRE_HERM_ODD = 2 };
