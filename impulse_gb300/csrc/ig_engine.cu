@@ -670,9 +670,10 @@ static bool line_kernel_ok(Arith a, const CoreDesc &d, const IODesc &io)
     if (d.rs == RS_FULL || !line_edge_ok(d.st[0].R) || !line_edge_ok(d.st[d.nst - 1].R)) return false;
     if (io.cols_in || io.cols_out || io.loff_in || io.loff_out || io.pair || io.split_N1) return false;
     if (io.lay == LAY_C2C) return io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C;
+    // halfcomplex lines: FP32 only (double-float ones measured faster on k_fft_smem)
     if (io.lay == LAY_R2HC)
-        return io.post == POST_SPLIT && io.in_kind == IN_C && io.out_kind == OUT_HC && io.nreal == 2LL * d.M &&
-               line_r2hc_last_ok(d.st[d.nst - 1].R);
+        return a == A_F32 && io.post == POST_SPLIT && io.in_kind == IN_C && io.out_kind == OUT_HC &&
+               io.nreal == 2LL * d.M && line_r2hc_last_ok(d.st[d.nst - 1].R);
     return false;
 }
 

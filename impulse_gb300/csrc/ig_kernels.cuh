@@ -99,6 +99,29 @@ __device__ __forceinline__ int line_i0(const IODesc &io, long long l)
 
 __device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
 
+// Line-scale keys: the biased exponent of |x| as if x were normal (double
+// subnormals get their true exponent below the normal range, down to -51;
+// float subnormals down to -22), plus kKeyOff, so that 0 stays "no value"
+// (zeros, infinities and NaN).  A line's exact power-of-two scale is
+// (bias + kKeyOff) - (largest key of the line).
+constexpr int kKeyOff = 64;
+__device__ __forceinline__ int dkey(double x)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    const int e = (int)(u >> 52);
+    if (e != 0 && e != 0x7ff) return e + kKeyOff;
+    if (e == 0x7ff || u == 0) return 0;
+    return (63 - __clzll((long long)u)) - 51 + kKeyOff;
+}
+__device__ __forceinline__ int fkey(float x)
+{
+    const unsigned u = __float_as_uint(x) & 0x7fffffffu;
+    const int e = (int)(u >> 23);
+    if (e != 0 && e != 0xff) return e + kKeyOff;
+    if (e == 0xff || u == 0) return 0;
+    return (31 - __clz((int)u)) - 22 + kKeyOff;
+}
+
 // slot read with optional raw-double conversion
 template <class T, bool RAW> __device__ __forceinline__ cx<T> sload(const cx<T> *p, int esc)
 {
@@ -523,8 +546,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                         const int u = u0 + c * tpl;
                         if (u >= cnt) break;
                         if constexpr (RAW) {
-                            int e1 = dexp(v[c].x), e2 = dexp(v[c].y);
-                            emax = max(emax, max(e1 == 0x7ff ? 0 : e1, e2 == 0x7ff ? 0 : e2));
+                            emax = max(emax, max(dkey(v[c].x), dkey(v[c].y)));
                         }
                         cx<T> z{Store<T>::in(v[c].x, esc), Store<T>::in(v[c].y, esc)};
                         sput(line + sp(u, pad), cc ? conjx(z) : z);
@@ -551,13 +573,11 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                         const int u = u0 + c * tpl;
                         if (u >= cnt) break;
                         if constexpr (RAW) {
-                            int e1 = dexp(va[c]), e2 = dexp(vb[c]);
-                            emax = max(emax, e1 == 0x7ff ? 0 : e1);
-                            emaxb = max(emaxb, e2 == 0x7ff ? 0 : e2);
+                            emax = max(emax, dkey(va[c]));
+                            emaxb = max(emaxb, dkey(vb[c]));
                         } else {
-                            int e1 = fexp(va[c]), e2 = fexp(vb[c]);
-                            emax = max(emax, e1 == 0xff ? 0 : e1);
-                            emaxb = max(emaxb, e2 == 0xff ? 0 : e2);
+                            emax = max(emax, fkey(va[c]));
+                            emaxb = max(emaxb, fkey(vb[c]));
                         }
                         sput(line + sp(u, pad), cx<T>{Store<T>::in(va[c], esc), Store<T>::in(vb[c], escb)});
                     }
@@ -586,13 +606,11 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     if (io.pre != PRE_NONE && (u == 0 || (io.pre == PRE_HERM_EVEN && u == M))) { im = S(0); ib = S(0); }
                     if (scaled) {
                         if constexpr (RAW) {
-                            int e1 = dexp(re), e2 = dexp(im), e3 = dexp(rb), e4 = dexp(ib);
-                            emax = max(emax, max(e1 == 0x7ff ? 0 : e1, e2 == 0x7ff ? 0 : e2));
-                            emaxb = max(emaxb, max(e3 == 0x7ff ? 0 : e3, e4 == 0x7ff ? 0 : e4));
+                            emax = max(emax, max(dkey(re), dkey(im)));
+                            emaxb = max(emaxb, max(dkey(rb), dkey(ib)));
                         } else {
-                            int e1 = fexp((float)re), e2 = fexp((float)im), e3 = fexp((float)rb), e4 = fexp((float)ib);
-                            emax = max(emax, max(e1 == 0xff ? 0 : e1, e2 == 0xff ? 0 : e2));
-                            emaxb = max(emaxb, max(e3 == 0xff ? 0 : e3, e4 == 0xff ? 0 : e4));
+                            emax = max(emax, max(fkey((float)re), fkey((float)im)));
+                            emaxb = max(emaxb, max(fkey((float)rb), fkey((float)ib)));
                         }
                     }
                     if (!paired) {
@@ -620,20 +638,24 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             if (act && emaxb > 0) atomicMax(&s_emax[2 * gi + 1], emaxb);
             __syncthreads();
             for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-                const int ea = s_emax[2 * l], eb = s_emax[2 * l + 1];
+                const int ea = s_emax[2 * l], eb = s_emax[2 * l + 1];  // line-scale keys
                 if (RAW) {
                     // safe window: largest element within 2^+-40 (all-zero lines are safe)
-                    if (ea != 0 && (ea > 1023 + 40 || ea < 1023 - 40)) { s_esc[2 * l] = 1023 - ea; s_rescale = 1; }
-                    if (paired && eb != 0 && (eb > 1023 + 40 || eb < 1023 - 40)) { s_esc[2 * l + 1] = 1023 - eb; s_rescale = 1; }
+                    constexpr int c = 1023 + kKeyOff;
+                    if (ea != 0 && (ea > c + 40 || ea < c - 40)) { s_esc[2 * l] = c - ea; s_rescale = 1; }
+                    if (paired && eb != 0 && (eb > c + 40 || eb < c - 40)) { s_esc[2 * l + 1] = c - eb; s_rescale = 1; }
                     if (paired && ea != 0 && eb != 0 && abs(ea - eb) > 8) {
-                        s_esc[2 * l] = 1023 - ea;
-                        s_esc[2 * l + 1] = 1023 - eb;
+                        s_esc[2 * l] = c - ea;
+                        s_esc[2 * l + 1] = c - eb;
                         s_rescale = 1;
                     }
-                } else if (paired && ea != 0 && eb != 0 && (abs(ea - eb) > 8 || abs(ea - 127) > 40 || abs(eb - 127) > 40)) {
-                    s_esc[2 * l] = 127 - ea;
-                    s_esc[2 * l + 1] = 127 - eb;
-                    s_rescale = 1;
+                } else if (paired && ea != 0 && eb != 0) {
+                    constexpr int c = 127 + kKeyOff;
+                    if (abs(ea - eb) > 8 || abs(ea - c) > 40 || abs(eb - c) > 40) {
+                        s_esc[2 * l] = c - ea;
+                        s_esc[2 * l + 1] = c - eb;
+                        s_rescale = 1;
+                    }
                 }
             }
             __syncthreads();
@@ -1064,8 +1086,8 @@ template <> struct Loc<df> {
     int esc = 0;
     __device__ void fit(double a, double b, double c = 0.0, double d = 0.0)
     {
-        int e = max(max(dexp(a), dexp(b)), max(dexp(c), dexp(d)));
-        esc = e > 0 ? 1023 - e : 0;
+        const int e = max(max(dkey(a), dkey(b)), max(dkey(c), dkey(d)));
+        esc = e > 0 ? 1023 + kKeyOff - e : 0;
     }
     __device__ cx<df> in(double re, double im) const { return cx<df>{df_from_double(re, esc), df_from_double(im, esc)}; }
     __device__ double out(df v) const { return df_to_double(v, esc); }
@@ -1275,22 +1297,21 @@ __global__ void k_line_exp(const __grid_constant__ IODesc io, int *__restrict__ 
         S re, im, rb = S(0), ib = S(0);
         load_unit<S, S2>(io, base, u, re, im);
         if (has_b) load_unit<S, S2>(io, base + io.pair_in, u, rb, ib);
-        int e1, e2, e3, e4, inf;
         if constexpr (sizeof(S) == 8) {
-            e1 = dexp((double)re); e2 = dexp((double)im); e3 = dexp((double)rb); e4 = dexp((double)ib); inf = 0x7ff;
+            ea = max(ea, max(dkey((double)re), dkey((double)im)));
+            eb = max(eb, max(dkey((double)rb), dkey((double)ib)));
         } else {
-            e1 = fexp((float)re); e2 = fexp((float)im); e3 = fexp((float)rb); e4 = fexp((float)ib); inf = 0xff;
+            ea = max(ea, max(fkey((float)re), fkey((float)im)));
+            eb = max(eb, max(fkey((float)rb), fkey((float)ib)));
         }
-        ea = max(ea, max(e1 == inf ? 0 : e1, e2 == inf ? 0 : e2));
-        eb = max(eb, max(e3 == inf ? 0 : e3, e4 == inf ? 0 : e4));
     }
     if (ea) atomicMax(&s_e[0], ea);
     if (eb) atomicMax(&s_e[1], eb);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const int bias = sizeof(S) == 8 ? 1023 : 127;
-        esc[2 * l] = s_e[0] ? bias - s_e[0] : 0;
-        esc[2 * l + 1] = s_e[1] ? bias - s_e[1] : 0;
+        const int c = (sizeof(S) == 8 ? 1023 : 127) + kKeyOff;
+        esc[2 * l] = s_e[0] ? c - s_e[0] : 0;
+        esc[2 * l + 1] = s_e[1] ? c - s_e[1] : 0;
     }
 }
 

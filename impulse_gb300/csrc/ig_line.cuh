@@ -32,12 +32,6 @@ namespace ig {
 constexpr int LK_C2C = 0;   // complex units in, complex units out
 constexpr int LK_R2HC = 1;  // real pairs in (as complex units), halfcomplex out
 
-// biased double exponent field, from the high word only
-__device__ __forceinline__ unsigned dexpw(double x)
-{
-    return ((unsigned)(__double_as_longlong(x) >> 32) >> 20) & 0x7ffu;
-}
-
 // First stage: load, (double-float: range check), convert, radix-R DFT, write
 // the Stockham positions j R + m of buffer `line`.  Returns the line's
 // exponent scale (0 for FP32).
@@ -64,26 +58,27 @@ __device__ __forceinline__ int line_first(cx<T> *line, const char *base, long lo
     }
     int esc = 0;
     if constexpr (RAW) {
-        unsigned emax = 0;
+        int emax = 0;  // largest line-scale key (dkey) of the thread's values
 #pragma unroll
         for (int i = 0; i < NB; ++i) {
             const int j = t + i * tpl;
             if (act && j < nr) {
 #pragma unroll
-                for (int m = 0; m < R; ++m) emax = max(emax, max(dexpw(raw[i][m].x), dexpw(raw[i][m].y)));
+                for (int m = 0; m < R; ++m) emax = max(emax, max(dkey(raw[i][m].x), dkey(raw[i][m].y)));
             }
         }
-        // common case: every thread's largest exponent inside the safe window
-        // (all-zero and non-finite maxima are left alone); otherwise the CTA
-        // takes the exact per-line maximum
-        const bool out = emax != 0 && emax != 0x7ffu && (emax > 1023u + 40u || emax < 1023u - 40u);
+        // common case: every thread's largest value inside the safe window
+        // 2^+-40 (all-zero threads are safe); otherwise the CTA takes the
+        // exact per-line maximum
+        constexpr int c = 1023 + kKeyOff;
+        const bool out = emax != 0 && (emax > c + 40 || emax < c - 40);
         if (out) *s_flag = 1;
         __syncthreads();
         if (*s_flag) {
-            if (act && emax != 0x7ffu) atomicMax(&s_emax[g], (int)emax);
+            if (act && emax != 0) atomicMax(&s_emax[g], emax);
             __syncthreads();
             const int ea = act ? s_emax[g] : 0;
-            if (ea != 0 && (ea > 1023 + 40 || ea < 1023 - 40)) esc = 1023 - ea;
+            if (ea != 0 && (ea > c + 40 || ea < c - 40)) esc = c - ea;
         }
     }
 #pragma unroll
@@ -378,8 +373,15 @@ template <class T, int E, bool DB, int RS>
 static void launch_line_rs(const CoreDesc &d, const IODesc &io, unsigned grid, unsigned blk, size_t smem,
                            cudaStream_t st)
 {
-    if (io.lay == LAY_R2HC) k_fft_line<T, E, RS, LK_R2HC, DB><<<grid, blk, smem, st>>>(d, io);
-    else k_fft_line<T, E, RS, LK_C2C, DB><<<grid, blk, smem, st>>>(d, io);
+    // double-float halfcomplex lines stay on k_fft_smem: the fused split's two
+    // live butterflies cost a CTA per SM (line_kernel_ok)
+    if constexpr (!std::is_same<T, df>::value) {
+        if (io.lay == LAY_R2HC) {
+            k_fft_line<T, E, RS, LK_R2HC, DB><<<grid, blk, smem, st>>>(d, io);
+            return;
+        }
+    }
+    k_fft_line<T, E, RS, LK_C2C, DB><<<grid, blk, smem, st>>>(d, io);
 }
 
 template <class T, int E, bool DB>
@@ -405,7 +407,8 @@ template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes)
     cudaError_t e = cudaSuccess;
 #define IG_SL(RS_)                                                                                        \
     if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_C2C, DB>, bytes);                     \
-    if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC, DB>, bytes);
+    if constexpr (!std::is_same<T, df>::value)                                                            \
+        if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC, DB>, bytes);
     IG_SL(RS_P2)
     IG_SL(RS_ALL)
     if constexpr (E == 8) { IG_SL(RS_P235) }
