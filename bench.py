@@ -456,6 +456,23 @@ def run_uneven(lib, dev, world, args):
     out["paths"] = p32.info
     ms32 = timed(p32, x32, y32, "graph", max(3, args.steps // 2))
     ms32_loop = timed(p32, x32, y32, "loop", 2)
+
+    def part_ms(plan, x, y, parts, reps=3):
+        with torch.cuda.stream(s):
+            plan.run_part(x.data_ptr(), y.data_ptr(), parts, s.cuda_stream)
+            s.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                plan.run_part(x.data_ptr(), y.data_ptr(), parts, s.cuda_stream)
+            e1.record(s)
+            s.synchronize()
+        return round(e0.elapsed_time(e1) / reps, 3)
+
+    # per-path device time of the FP32 plan (each part alone, not in a graph)
+    out["fp32_path_ms"] = {"worklist_phase0": part_ms(p32, x32, y32, 1), "worklist_phase1": part_ms(p32, x32, y32, 2),
+                           "general": part_ms(p32, x32, y32, 4)}
     x64 = x32.to(torch.complex128)
     y64 = torch.empty_like(x64)
     p64 = MultiFFT(lengths, L.IG_F64)

@@ -82,6 +82,7 @@ SIGNATURES = {
     "ig_multi_exec_device": (C.c_int, [_vp, _vp, _vp, _vp]),
     "ig_multi_exec_graph": (C.c_int, [_vp, _vp, _vp, _vp]),
     "ig_multi_exec_loop_device": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "ig_multi_exec_part": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
     "ig_dct": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, C.c_int, _sz]),
     "ig_dst": (C.c_int, _ND_HEAD + [C.c_int, _vp, _vp, C.c_double, C.c_int, _sz]),
     "ig_r2r_fftpack": (C.c_int, _ND_HEAD + [C.c_int, C.c_int, _vp, _vp, C.c_double, _sz]),

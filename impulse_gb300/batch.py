@@ -92,6 +92,10 @@ class MultiFFT:
             L.load().ig_destroy_multi_plan(self.h)
             self.h = None
 
+    def run_part(self, x_ptr, y_ptr, parts, stream=None):
+        """One part of the sequence: mask of 1 (work-list phase 0), 2 (phase 1), 4 (general path)."""
+        L.check(L.load().ig_multi_exec_part(self.h, x_ptr, y_ptr, int(parts), stream))
+
     def run(self, x_ptr, y_ptr, stream=None, mode="worklist"):
         lib = L.load()
         fn = {"worklist": lib.ig_multi_exec_device, "graph": lib.ig_multi_exec_graph,

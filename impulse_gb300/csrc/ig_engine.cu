@@ -2564,6 +2564,11 @@ struct ig_multi_plan_i {
     MultiPhase ph[2];
     std::vector<std::unique_ptr<DevBuf>> tables;
     std::vector<long long> general;
+    // general transforms run on side streams (fork / join around the work
+    // list): their launches are small, so several run at once
+    std::vector<int> gstream;  // side stream of general[k]
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> ev;  // ev[0] fork, ev[1 + i] join of side[i]
     std::unique_ptr<DevBuf> scratch, counter;
     size_t n_wl = 0, n_4s = 0;
     cudaGraphExec_t gexec = nullptr;
@@ -2573,8 +2578,12 @@ struct ig_multi_plan_i {
     ~ig_multi_plan_i()
     {
         if (gexec) cudaGraphExecDestroy(gexec);
+        for (cudaStream_t s : side) cudaStreamDestroy(s);
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
     }
 };
+
+static const int kMultiSide = 8;
 
 static const int kWorklistThreads = 512;
 
@@ -2616,8 +2625,22 @@ static void finish_phase(Arith a, MultiPhase &ph)
        "work list upload");
 }
 
-static void multi_launch(ig_multi_plan_i &m, const void *in, void *out, cudaStream_t st)
+// parts: 1 work-list phase 0 (single-CTA groups, four-step column passes),
+// 2 phase 1 (four-step row passes), 4 general transforms
+static void multi_launch(ig_multi_plan_i &m, const void *in, void *out, cudaStream_t st, int parts = 7)
 {
+    const long long es = 2 * (long long)store_real_bytes(m.a);
+    const bool gen = (parts & 4) && !m.general.empty();
+    if (gen) {
+        ck(cudaEventRecord(m.ev[0], st), "fork");
+        for (cudaStream_t s : m.side) ck(cudaStreamWaitEvent(s, m.ev[0], 0), "fork");
+        for (size_t k = 0; k < m.general.size(); ++k) {
+            const long long i = m.general[k];
+            Lines ln = contiguous_lines((const char *)in + m.off[i] * es, (char *)out + m.off[i] * es, 1, m.len[i],
+                                        m.len[i], es, es);
+            exec_op(m.a, OP_C2C, m.len[i], ln, m.fwd, m.fct, m.side[m.gstream[k]]);
+        }
+    }
     const int smcount = [] {
         int v = 0;
         cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device_id());
@@ -2626,7 +2649,7 @@ static void multi_launch(ig_multi_plan_i &m, const void *in, void *out, cudaStre
     ck(cudaMemsetAsync(m.counter->p, 0, 2 * sizeof(unsigned long long), st), "work list counter");
     for (int k = 0; k < 2; ++k) {
         MultiPhase &ph = m.ph[k];
-        if (!ph.total) continue;
+        if (!ph.total || !(parts & (1 << k))) continue;
         int grid = (int)std::min<unsigned long long>((unsigned long long)smcount, ph.total);
         unsigned long long *ctr = (unsigned long long *)m.counter->p + k;
         void *scr = m.scratch ? m.scratch->p : nullptr;
@@ -2643,11 +2666,11 @@ static void multi_launch(ig_multi_plan_i &m, const void *in, void *out, cudaStre
         ck(e, "work list launch");
         count_launch();
     }
-    const long long es = 2 * (long long)store_real_bytes(m.a);
-    for (long long i : m.general) {
-        Lines ln = contiguous_lines((const char *)in + m.off[i] * es, (char *)out + m.off[i] * es, 1, m.len[i],
-                                    m.len[i], es, es);
-        exec_op(m.a, OP_C2C, m.len[i], ln, m.fwd, m.fct, st);
+    if (gen) {
+        for (size_t i = 0; i < m.side.size(); ++i) {
+            ck(cudaEventRecord(m.ev[1 + i], m.side[i]), "join");
+            ck(cudaStreamWaitEvent(st, m.ev[1 + i], 0), "join");
+        }
     }
 }
 
@@ -2747,6 +2770,33 @@ ig_multi_plan ig_make_multi_plan(int dtype, size_t count, const size_t *lengths,
         }
         finish_phase(m->a, m->ph[0]);
         finish_phase(m->a, m->ph[1]);
+        if (!m->general.empty()) {
+            // longest first onto the least loaded side stream (cost ~ N log N)
+            const int ns = (int)std::min<size_t>(kMultiSide, m->general.size());
+            for (int i = 0; i < ns; ++i) {
+                cudaStream_t sst;
+                ck(cudaStreamCreateWithFlags(&sst, cudaStreamNonBlocking), "side stream");
+                m->side.push_back(sst);
+            }
+            for (int i = 0; i <= ns; ++i) {
+                cudaEvent_t e;
+                ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "side event");
+                m->ev.push_back(e);
+            }
+            std::vector<size_t> order(m->general.size());
+            for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+            std::sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+                return m->len[m->general[x]] > m->len[m->general[y]];
+            });
+            std::vector<double> load(ns, 0.0);
+            m->gstream.assign(m->general.size(), 0);
+            for (size_t k : order) {
+                const int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+                const double n = (double)m->len[m->general[k]];
+                load[best] += n * std::log2(n + 1.0);
+                m->gstream[k] = best;
+            }
+        }
         m->counter.reset(new DevBuf(2 * sizeof(unsigned long long)));
         int optin = max_smem() + 1024;
         static std::once_flag once[3];
@@ -2819,6 +2869,19 @@ int ig_multi_exec_graph(ig_multi_plan plan, const void *in, void *out, void *str
         }
         ck(cudaGraphLaunch(plan->gexec, st), "graph launch");
         count_launch();
+    });
+}
+
+// One part of the sequence (bit mask: 1 work-list phase 0, 2 phase 1, 4 the
+// general transforms), for timing the parts apart.
+int ig_multi_exec_part(ig_multi_plan plan, const void *in, void *out, int parts, void *stream)
+{
+    return guarded([&] {
+        if (!plan || !in || !out) raise(IG_EINVAL, "null argument");
+        if (parts < 0 || parts > 7) raise(IG_EINVAL, "parts must be a mask of 1, 2 and 4");
+        require_aligned(in, 2 * store_real_bytes(plan->a), "input");
+        require_aligned(out, 2 * store_real_bytes(plan->a), "output");
+        multi_launch(*plan, in, out, as_stream(stream), parts);
     });
 }
 

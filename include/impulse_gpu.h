@@ -160,7 +160,8 @@ int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff
  * fit one CTA and runs them, with the column passes of longer four-step
  * lengths, through one persistent work-list launch; a second launch runs the
  * row passes; lengths needing Bluestein or Rader over a multi-pass core use
- * the general path.  ig_multi_exec_graph captures that sequence into a CUDA graph
+ * the general path, on up to eight side streams forked from and joined back
+ * into the caller's stream.  ig_multi_exec_graph captures that sequence into a CUDA graph
  * on its first call for given pointers and replays it afterwards;
  * ig_multi_exec_loop_device is the one-call-per-transform pattern, for
  * comparison.  The reference transforms one line per call
@@ -173,6 +174,12 @@ int ig_multi_info(ig_multi_plan plan, size_t *n_worklist, size_t *n_fourstep, si
 int ig_multi_exec_device(ig_multi_plan plan, const void *in, void *out, void *stream);
 int ig_multi_exec_graph(ig_multi_plan plan, const void *in, void *out, void *stream);
 int ig_multi_exec_loop_device(ig_multi_plan plan, const void *in, void *out, void *stream);
+/* One part of ig_multi_exec_device's sequence, for timing the paths apart:
+ * parts is a mask of 1 (work-list phase 0: single-CTA lengths and four-step
+ * column passes), 2 (phase 1: four-step row passes, after phase 0) and 4
+ * (lengths on the general path, on the plan's side streams joined back into
+ * `stream`).  No counterpart in the reference. */
+int ig_multi_exec_part(ig_multi_plan plan, const void *in, void *out, int parts, void *stream);
 
 /* ---- adjoints ----------------------------------------------------------------
  * Gradients of a real loss through c2c / r2c / c2r (device pointers).  With g
