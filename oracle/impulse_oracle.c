@@ -154,6 +154,9 @@ typedef struct io_cplan {
     size_t fct[IO_MAXFCT];
     oc_t *tw;             /* tw[t] = exp(-2 pi i t/n), t < n (Stockham plans) */
     size_t maxr;          /* largest radix, for generic-radix scratch */
+    oc_t *stw;            /* stage twiddles: stage s at stw + twoff[s], entry
+                             k (r-1) + m - 1 = exp(-2 pi i m k / (ns r)), k < ns */
+    size_t twoff[IO_MAXFCT];
     /* Bluestein */
     size_t n2;
     oc_t *bk;             /* exp(+i pi m^2/n), m < n */
@@ -163,9 +166,11 @@ typedef struct io_cplan {
 
 static void io_factorize(io_cplan *p)
 {
-    /* 4s first, then a single 2 moved to the front, then odd divisors
-       (pocketfft.c:954-983). */
+    /* 8s, then 4s, then a single 2 moved to the front, then odd divisors
+       (the C++ backend's cfftp::factorize, pocketfft_hdronly.h:1360-1381;
+       the C backend's pocketfft.c:954-983 takes 4s only) */
     size_t n = p->n, nf = 0;
+    while (n % 8 == 0) { p->fct[nf++] = 8; n /= 8; }
     while (n % 4 == 0) { p->fct[nf++] = 4; n /= 4; }
     if (n % 2 == 0) {
         n /= 2;
@@ -195,6 +200,20 @@ static io_cplan *io_make_stockham(size_t n)
         io_sincos_2pi(t, n, &c, &s);
         p->tw[t].r = c;
         p->tw[t].i = -s;
+    }
+    /* per-stage tables, read in order by the k-major stage loops: the same
+       values as tw[m k n/(ns r)] */
+    size_t tot = 0, ns = 1;
+    for (size_t f = 0; f < p->nfct; ++f) { p->twoff[f] = tot; tot += ns * (p->fct[f] - 1); ns *= p->fct[f]; }
+    p->stw = (oc_t *)malloc(sizeof(oc_t) * (tot ? tot : 1));
+    if (!p->stw) { free(p->tw); free(p); return NULL; }
+    ns = 1;
+    for (size_t f = 0; f < p->nfct; ++f) {
+        const size_t r = p->fct[f], step = n / (ns * r);
+        oc_t *t = p->stw + p->twoff[f];
+        for (size_t k = 0; k < ns; ++k)
+            for (size_t m = 1; m < r; ++m) t[k * (r - 1) + m - 1] = p->tw[(m * k * step) % n];
+        ns *= r;
     }
     return p;
 }
@@ -241,6 +260,7 @@ void io_destroy_cplan(io_cplan *p)
 {
     if (!p) return;
     free(p->tw);
+    free(p->stw);
     free(p->bk);
     free(p->bkf);
     if (p->sub) io_destroy_cplan(p->sub);
@@ -254,68 +274,173 @@ size_t io_cplan_fct(const io_cplan *p, size_t k) { return p->blue ? p->sub->fct[
 static inline oc_t cmul(oc_t a, oc_t b) { oc_t r = { a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r }; return r; }
 static inline oc_t cmulc(oc_t a, oc_t b) { oc_t r = { a.r * b.r + a.i * b.i, a.i * b.r - a.r * b.i }; return r; } /* a*conj(b) */
 
-/* One Stockham stage of radix r: x -> y.  ns = product of the radices
-   already applied.  Butterfly j (j < n/r) reads x[j + m*n/r], twiddles
-   input m by w^(m*k) with k = j mod ns and w = exp(-+2 pi i/(ns r)), runs a
-   radix-r DFT and writes y[(j/ns)*ns*r + k + m*ns]. */
-static void io_stage(const io_cplan *p, size_t r, size_t ns, const oc_t *x, oc_t *y, int forward, oc_t *v, oc_t *w)
+/* One Stockham stage of radix r (stage s of the plan): x -> y.  ns = product
+   of the radices already applied.  Butterfly j = q ns + k (j < n/r) reads
+   x[j + m n/r], twiddles input m by w^(m k) (w = exp(-+2 pi i/(ns r)), from
+   the stage table), runs a radix-r DFT and writes y[q ns r + k + m ns].  The
+   loops run k outermost so that one butterfly's twiddles serve all q.  The
+   DFTs: radix 2 and 4 directly, odd radices in the symmetric-pair form
+   V[q] = v0 + sum_k a_k cos(2 pi k q/r) -+ i sum_k b_k sin(2 pi k q/r),
+   V[r-q] with the second sum's sign flipped (a_k = v_k + v_{r-k},
+   b_k = v_k - v_{r-k}), written out for 3 and 5 (pocketfft.c:300-865 covers
+   radices 2, 3, 4, 5, 7, 11 with passes of the same arithmetic). */
+static void io_stage(const io_cplan *p, size_t s, size_t ns, const oc_t *x, oc_t *y, int forward, oc_t *v, oc_t *tk)
 {
-    const size_t n = p->n, nr = n / r, tstep = n / (ns * r);
+    const size_t r = p->fct[s], n = p->n, nr = n / r, nq = nr / ns;
+    const oc_t *tws = p->stw + p->twoff[s];
     const double sg = forward ? 1.0 : -1.0; /* sign of the imaginary part of the table */
-    for (size_t j = 0; j < nr; ++j) {
-        size_t k = j % ns;
-        for (size_t m = 0; m < r; ++m) {
-            oc_t a = x[j + m * nr];
-            if (m && k) {
-                oc_t t = p->tw[m * k * tstep];
-                t.i *= sg;
-                a = cmul(a, t);
-            }
-            v[m] = a;
-        }
-        /* radix-r DFT: V[q] = sum_m v[m] exp(-+2 pi i m q / r) */
-        if (r == 2) {
-            oc_t a = v[0], b = v[1];
-            v[0].r = a.r + b.r; v[0].i = a.i + b.i;
-            v[1].r = a.r - b.r; v[1].i = a.i - b.i;
-        } else if (r == 4) {
-            oc_t t0 = { v[0].r + v[2].r, v[0].i + v[2].i }, t1 = { v[0].r - v[2].r, v[0].i - v[2].i };
-            oc_t t2 = { v[1].r + v[3].r, v[1].i + v[3].i }, t3 = { v[1].r - v[3].r, v[1].i - v[3].i };
-            /* multiply t3 by -i (forward) or +i (backward) */
-            oc_t t3r = forward ? (oc_t){ t3.i, -t3.r } : (oc_t){ -t3.i, t3.r };
-            v[0].r = t0.r + t2.r; v[0].i = t0.i + t2.i;
-            v[2].r = t0.r - t2.r; v[2].i = t0.i - t2.i;
-            v[1].r = t1.r + t3r.r; v[1].i = t1.i + t3r.i;
-            v[3].r = t1.r - t3r.r; v[3].i = t1.i - t3r.i;
-        } else {
-            /* direct DFT with the plan's own table: exp(-2 pi i mq/r) = tw[(mq mod r) * n/r] */
-            for (size_t q = 0; q < r; ++q) {
-                oc_t acc = v[0];
-                for (size_t m = 1; m < r; ++m) {
-                    oc_t t = p->tw[((m * q) % r) * nr];
-                    t.i *= sg;
-                    oc_t pr = cmul(v[m], t);
-                    acc.r += pr.r; acc.i += pr.i;
-                }
-                w[q] = acc;
-            }
-            memcpy(v, w, r * sizeof(oc_t));
-        }
-        size_t base = (j / ns) * ns * r + k;
-        for (size_t m = 0; m < r; ++m) y[base + m * ns] = v[m];
+    /* odd radices: cos / sin (2 pi t / r), t < r, from the plan's table */
+    double cs[IO_MAXFCT + 2], sn[IO_MAXFCT + 2];
+    double *cr = cs, *sr = sn, *heap = NULL;
+    if (r % 2 == 1 && r > IO_MAXFCT + 2) {
+        heap = (double *)malloc(2 * r * sizeof(double));
+        cr = heap;
+        sr = heap + r;
     }
+    if (r % 2 == 1)
+        for (size_t t = 0; t < r; ++t) { cr[t] = p->tw[t * nr].r; sr[t] = -p->tw[t * nr].i; }
+    for (size_t k = 0; k < ns; ++k) {
+        for (size_t m = 1; m < r; ++m) {
+            oc_t t = k ? tws[k * (r - 1) + m - 1] : (oc_t){ 1.0, 0.0 };
+            t.i *= sg;
+            tk[m] = t;
+        }
+        if (r == 8) {
+            /* radix 8 = radix-2 butterflies (m, m + 4), w8^m on the
+               differences, two radix-4 DFTs on the sums and differences */
+            const double h = 0.70710678118654752440; /* sqrt(1/2) */
+            for (size_t q = 0; q < nq; ++q) {
+                const size_t j = q * ns + k;
+                const oc_t *xi = x + j;
+                oc_t *yo = y + q * ns * r + k;
+                oc_t w[8];
+                w[0] = xi[0];
+                if (k) for (size_t m = 1; m < 8; ++m) w[m] = cmul(xi[m * nr], tk[m]);
+                else for (size_t m = 1; m < 8; ++m) w[m] = xi[m * nr];
+                oc_t a[4], b[4];
+                for (size_t m = 0; m < 4; ++m) {
+                    a[m].r = w[m].r + w[m + 4].r; a[m].i = w[m].i + w[m + 4].i;
+                    b[m].r = w[m].r - w[m + 4].r; b[m].i = w[m].i - w[m + 4].i;
+                }
+                /* b1 w8, b2 w8^2 = -+i, b3 w8^3 (forward: w8 = (1 - i)/sqrt 2) */
+                oc_t t1, t2, t3;
+                if (forward) {
+                    t1.r = h * (b[1].r + b[1].i); t1.i = h * (b[1].i - b[1].r);
+                    t2.r = b[2].i; t2.i = -b[2].r;
+                    t3.r = h * (b[3].i - b[3].r); t3.i = -h * (b[3].r + b[3].i);
+                } else {
+                    t1.r = h * (b[1].r - b[1].i); t1.i = h * (b[1].i + b[1].r);
+                    t2.r = -b[2].i; t2.i = b[2].r;
+                    t3.r = -h * (b[3].r + b[3].i); t3.i = h * (b[3].r - b[3].i);
+                }
+                b[1] = t1; b[2] = t2; b[3] = t3;
+                for (int half = 0; half < 2; ++half) {
+                    const oc_t *u = half ? b : a;
+                    oc_t s0 = { u[0].r + u[2].r, u[0].i + u[2].i }, s1 = { u[0].r - u[2].r, u[0].i - u[2].i };
+                    oc_t s2 = { u[1].r + u[3].r, u[1].i + u[3].i }, s3 = { u[1].r - u[3].r, u[1].i - u[3].i };
+                    oc_t s3r = forward ? (oc_t){ s3.i, -s3.r } : (oc_t){ -s3.i, s3.r };
+                    oc_t *o = yo + (size_t)half * ns;
+                    o[0].r = s0.r + s2.r; o[0].i = s0.i + s2.i;
+                    o[4 * ns].r = s0.r - s2.r; o[4 * ns].i = s0.i - s2.i;
+                    o[2 * ns].r = s1.r + s3r.r; o[2 * ns].i = s1.i + s3r.i;
+                    o[6 * ns].r = s1.r - s3r.r; o[6 * ns].i = s1.i - s3r.i;
+                }
+            }
+            continue;
+        }
+        for (size_t q = 0; q < nq; ++q) {
+            const size_t j = q * ns + k;
+            const oc_t *xi = x + j;
+            oc_t *yo = y + q * ns * r + k;
+            v[0] = xi[0];
+            if (k) for (size_t m = 1; m < r; ++m) v[m] = cmul(xi[m * nr], tk[m]);
+            else for (size_t m = 1; m < r; ++m) v[m] = xi[m * nr];
+            if (r == 2) {
+                yo[0].r = v[0].r + v[1].r; yo[0].i = v[0].i + v[1].i;
+                yo[ns].r = v[0].r - v[1].r; yo[ns].i = v[0].i - v[1].i;
+            } else if (r == 4) {
+                oc_t t0 = { v[0].r + v[2].r, v[0].i + v[2].i }, t1 = { v[0].r - v[2].r, v[0].i - v[2].i };
+                oc_t t2 = { v[1].r + v[3].r, v[1].i + v[3].i }, t3 = { v[1].r - v[3].r, v[1].i - v[3].i };
+                /* t3 times -i (forward) or +i (backward) */
+                oc_t t3r = forward ? (oc_t){ t3.i, -t3.r } : (oc_t){ -t3.i, t3.r };
+                yo[0].r = t0.r + t2.r; yo[0].i = t0.i + t2.i;
+                yo[2 * ns].r = t0.r - t2.r; yo[2 * ns].i = t0.i - t2.i;
+                yo[ns].r = t1.r + t3r.r; yo[ns].i = t1.i + t3r.i;
+                yo[3 * ns].r = t1.r - t3r.r; yo[3 * ns].i = t1.i - t3r.i;
+            } else if (r == 3) {
+                const double c1 = cr[1], s1 = sg * sr[1];
+                oc_t a = { v[1].r + v[2].r, v[1].i + v[2].i }, b = { v[1].r - v[2].r, v[1].i - v[2].i };
+                oc_t u = { v[0].r + c1 * a.r, v[0].i + c1 * a.i };
+                yo[0].r = v[0].r + a.r; yo[0].i = v[0].i + a.i;
+                /* -+ i s1 b */
+                yo[ns].r = u.r + s1 * b.i; yo[ns].i = u.i - s1 * b.r;
+                yo[2 * ns].r = u.r - s1 * b.i; yo[2 * ns].i = u.i + s1 * b.r;
+            } else if (r == 5) {
+                const double c1 = cr[1], c2 = cr[2], s1 = sg * sr[1], s2 = sg * sr[2];
+                oc_t a1 = { v[1].r + v[4].r, v[1].i + v[4].i }, b1 = { v[1].r - v[4].r, v[1].i - v[4].i };
+                oc_t a2 = { v[2].r + v[3].r, v[2].i + v[3].i }, b2 = { v[2].r - v[3].r, v[2].i - v[3].i };
+                yo[0].r = v[0].r + a1.r + a2.r; yo[0].i = v[0].i + a1.i + a2.i;
+                oc_t u1 = { v[0].r + c1 * a1.r + c2 * a2.r, v[0].i + c1 * a1.i + c2 * a2.i };
+                oc_t w1 = { s1 * b1.r + s2 * b2.r, s1 * b1.i + s2 * b2.i };
+                oc_t u2 = { v[0].r + c2 * a1.r + c1 * a2.r, v[0].i + c2 * a1.i + c1 * a2.i };
+                oc_t w2 = { s2 * b1.r - s1 * b2.r, s2 * b1.i - s1 * b2.i };
+                yo[ns].r = u1.r + w1.i; yo[ns].i = u1.i - w1.r;
+                yo[4 * ns].r = u1.r - w1.i; yo[4 * ns].i = u1.i + w1.r;
+                yo[2 * ns].r = u2.r + w2.i; yo[2 * ns].i = u2.i - w2.r;
+                yo[3 * ns].r = u2.r - w2.i; yo[3 * ns].i = u2.i + w2.r;
+            } else if (r % 2 == 1) {
+                const size_t h = (r - 1) / 2;
+                oc_t *a = v + r, *b = v + r + h; /* a_k, b_k at index k - 1 */
+                oc_t y0 = v[0];
+                for (size_t kk = 1; kk <= h; ++kk) {
+                    a[kk - 1].r = v[kk].r + v[r - kk].r; a[kk - 1].i = v[kk].i + v[r - kk].i;
+                    b[kk - 1].r = v[kk].r - v[r - kk].r; b[kk - 1].i = v[kk].i - v[r - kk].i;
+                    y0.r += a[kk - 1].r; y0.i += a[kk - 1].i;
+                }
+                yo[0] = y0;
+                for (size_t qq = 1; qq <= h; ++qq) {
+                    oc_t u = v[0], w = { 0.0, 0.0 };
+                    size_t t = 0;
+                    for (size_t kk = 1; kk <= h; ++kk) {
+                        t += qq;
+                        if (t >= r) t -= r;
+                        u.r += cr[t] * a[kk - 1].r; u.i += cr[t] * a[kk - 1].i;
+                        w.r += sr[t] * b[kk - 1].r; w.i += sr[t] * b[kk - 1].i;
+                    }
+                    w.r *= sg; w.i *= sg;
+                    yo[qq * ns].r = u.r + w.i; yo[qq * ns].i = u.i - w.r;
+                    yo[(r - qq) * ns].r = u.r - w.i; yo[(r - qq) * ns].i = u.i + w.r;
+                }
+            } else {
+                /* other even radices (the planner makes none but 2, 4 and 8): direct DFT */
+                for (size_t qq = 0; qq < r; ++qq) {
+                    oc_t acc = v[0];
+                    for (size_t m = 1; m < r; ++m) {
+                        oc_t t = p->tw[((m * qq) % r) * nr];
+                        t.i *= sg;
+                        oc_t pr = cmul(v[m], t);
+                        acc.r += pr.r; acc.i += pr.i;
+                    }
+                    yo[qq * ns] = acc;
+                }
+            }
+        }
+    }
+    free(heap);
 }
 
 static int io_stockham_exec(const io_cplan *p, oc_t *x, oc_t *scratch, int forward, double fct)
 {
     size_t n = p->n;
     if (n == 1) { x[0].r *= fct; x[0].i *= fct; return 0; }
-    oc_t *v = (oc_t *)malloc(sizeof(oc_t) * 2 * p->maxr);
+    /* butterfly values (r), symmetric-pair sums (r - 1) and twiddles (r) */
+    oc_t vbuf[64];
+    oc_t *v = 3 * p->maxr <= 64 ? vbuf : (oc_t *)malloc(sizeof(oc_t) * 3 * p->maxr);
     if (!v) return -1;
     oc_t *a = x, *b = scratch;
     size_t ns = 1;
     for (size_t s = 0; s < p->nfct; ++s) {
-        io_stage(p, p->fct[s], ns, a, b, forward, v, v + p->maxr);
+        io_stage(p, s, ns, a, b, forward, v, v + 2 * p->maxr);
         ns *= p->fct[s];
         oc_t *t = a; a = b; b = t;
     }
@@ -324,8 +449,49 @@ static int io_stockham_exec(const io_cplan *p, oc_t *x, oc_t *scratch, int forwa
     } else if (fct != 1.0) {
         for (size_t i = 0; i < n; ++i) { x[i].r *= fct; x[i].i *= fct; }
     }
-    free(v);
+    if (v != vbuf) free(v);
     return 0;
+}
+
+/* per-thread scratch of at least `count` complex values, kept between calls
+   (freed at thread exit by io_scratch_release in the batch workers) */
+static __thread oc_t *io_tls_buf = NULL;
+static __thread size_t io_tls_len = 0;
+static oc_t *io_scratch(size_t count)
+{
+    if (count > io_tls_len) {
+        free(io_tls_buf);
+        io_tls_buf = (oc_t *)malloc(sizeof(oc_t) * count);
+        io_tls_len = io_tls_buf ? count : 0;
+    }
+    return io_tls_buf;
+}
+/* a second one for the real transforms' packed line (the complex plan
+   uses the first) */
+static __thread oc_t *io_tls_buf2 = NULL;
+static __thread size_t io_tls_len2 = 0;
+static oc_t *io_scratch2(size_t count)
+{
+    if (count > io_tls_len2) {
+        free(io_tls_buf2);
+        io_tls_buf2 = (oc_t *)malloc(sizeof(oc_t) * count);
+        io_tls_len2 = io_tls_buf2 ? count : 0;
+    }
+    return io_tls_buf2;
+}
+static __thread oc_t *io_tls_blue = NULL;
+static __thread size_t io_tls_blue_len = 0;
+static void io_scratch_release(void)
+{
+    free(io_tls_buf);
+    io_tls_buf = NULL;
+    io_tls_len = 0;
+    free(io_tls_buf2);
+    io_tls_buf2 = NULL;
+    io_tls_len2 = 0;
+    free(io_tls_blue);
+    io_tls_blue = NULL;
+    io_tls_blue_len = 0;
 }
 
 /* Bluestein (pocketfft.c:1945-2008): premultiply by the chirp, convolve with
@@ -333,18 +499,23 @@ static int io_stockham_exec(const io_cplan *p, oc_t *x, oc_t *scratch, int forwa
 static int io_blue_exec(const io_cplan *p, oc_t *c, int forward, double fct)
 {
     size_t n = p->n, n2 = p->n2;
-    oc_t *akf = (oc_t *)calloc(2 * n2, sizeof(oc_t));
+    if (2 * n2 > io_tls_blue_len) {  /* per-thread, kept between calls */
+        free(io_tls_blue);
+        io_tls_blue = (oc_t *)malloc(sizeof(oc_t) * 2 * n2);
+        io_tls_blue_len = io_tls_blue ? 2 * n2 : 0;
+    }
+    oc_t *akf = io_tls_blue;
     if (!akf) return -1;
     oc_t *scr = akf + n2;
     for (size_t m = 0; m < n; ++m)
         akf[m] = forward ? cmulc(c[m], p->bk[m]) : cmul(c[m], p->bk[m]);
+    memset(akf + n, 0, (n2 - n) * sizeof(oc_t));
     io_stockham_exec(p->sub, akf, scr, 1, fct);
     for (size_t m = 0; m < n2; ++m)
         akf[m] = forward ? cmul(akf[m], p->bkf[m]) : cmulc(akf[m], p->bkf[m]);
     io_stockham_exec(p->sub, akf, scr, 0, 1.0);
     for (size_t m = 0; m < n; ++m)
         c[m] = forward ? cmulc(akf[m], p->bk[m]) : cmul(akf[m], p->bk[m]);
-    free(akf);
     return 0;
 }
 
@@ -352,11 +523,9 @@ static int io_blue_exec(const io_cplan *p, oc_t *c, int forward, double fct)
 int io_cplan_exec(const io_cplan *p, double *c, int forward, double fct)
 {
     if (p->blue) return io_blue_exec(p, (oc_t *)c, forward, fct);
-    oc_t *scr = (oc_t *)malloc(sizeof(oc_t) * p->n);
+    oc_t *scr = io_scratch(p->n);
     if (!scr) return -1;
-    int rc = io_stockham_exec(p, (oc_t *)c, scr, forward, fct);
-    free(scr);
-    return rc;
+    return io_stockham_exec(p, (oc_t *)c, scr, forward, fct);
 }
 
 /* ------------------------------------------------------------------ */
@@ -407,7 +576,7 @@ int io_rplan_exec(const io_rplan *p, double *c, int forward, double fct)
     size_t n = p->n;
     if (n == 1) { c[0] *= fct; return 0; }
     if (n % 2 == 1) {
-        oc_t *z = (oc_t *)malloc(sizeof(oc_t) * n);
+        oc_t *z = io_scratch2(n);
         if (!z) return -1;
         if (forward) {
             for (size_t m = 0; m < n; ++m) { z[m].r = c[m]; z[m].i = 0.0; }
@@ -423,27 +592,29 @@ int io_rplan_exec(const io_rplan *p, double *c, int forward, double fct)
             io_cplan_exec(p->cp, (double *)z, 0, fct);
             for (size_t m = 0; m < n; ++m) c[m] = z[m].r;
         }
-        free(z);
         return 0;
     }
     size_t h = n / 2;
-    oc_t *z = (oc_t *)malloc(sizeof(oc_t) * h);
+    oc_t *z = io_scratch2(h);
     if (!z) return -1;
     if (forward) {
-        /* z[m] = x[2m] + i x[2m+1]; Z = FFT_h(z); split into X[0..h] */
-        for (size_t m = 0; m < h; ++m) { z[m].r = c[2 * m]; z[m].i = c[2 * m + 1]; }
-        io_cplan_exec(p->cp, (double *)z, 1, 1.0);
+        /* z[m] = x[2m] + i x[2m+1] is the line itself read as complex values:
+           Z = FFT_h(z) in place, split into X[0..h] through the packed buffer */
+        oc_t *zc = (oc_t *)c;
+        if (io_cplan_exec(p->cp, c, 1, 1.0)) return -1;
+        double *xo = (double *)z;
         for (size_t k = 0; k <= h; ++k) {
-            oc_t zk = z[k % h], zm = z[(h - k) % h];
+            oc_t zk = zc[k == h ? 0 : k], zm = zc[k == 0 ? 0 : h - k];
             /* E = (zk + conj(zm))/2, O = (zk - conj(zm))/(2i) */
             oc_t e = { 0.5 * (zk.r + zm.r), 0.5 * (zk.i - zm.i) };
             oc_t o = { 0.5 * (zk.i + zm.i), -0.5 * (zk.r - zm.r) };
             oc_t t = cmul(o, p->wn[k]);
             double xr = (e.r + t.r) * fct, xi = (e.i + t.i) * fct;
-            if (k == 0) c[0] = xr;
-            else if (k == h) c[n - 1] = xr;
-            else { c[2 * k - 1] = xr; c[2 * k] = xi; }
+            if (k == 0) xo[0] = xr;
+            else if (k == h) xo[n - 1] = xr;
+            else { xo[2 * k - 1] = xr; xo[2 * k] = xi; }
         }
+        memcpy(c, xo, n * sizeof(double));
     } else {
         /* X from halfcomplex; Z[k] = A + i exp(+2 pi i k/n) B,
            A = X[k] + conj(X[h-k]), B = X[k] - conj(X[h-k]); z = IFFT_h(Z) */
@@ -463,7 +634,6 @@ int io_rplan_exec(const io_rplan *p, double *c, int forward, double fct)
         io_cplan_exec(p->cp, (double *)z, 0, fct);
         for (size_t m = 0; m < h; ++m) { c[2 * m] = z[m].r; c[2 * m + 1] = z[m].i; }
     }
-    free(z);
     return 0;
 }
 
@@ -505,16 +675,63 @@ typedef struct {
     int rc;
 } io_batch_job;
 
+/* Two real lines a, b of odd length n in one complex transform: forward,
+   Z = FFT(a + i b), A[k] = (Z[k] + conj Z[n-k]) / 2, B[k] = (Z[k] - conj Z[n-k]) / 2i;
+   backward, Z[k] = A[k] + i B[k] over the full Hermitian spectra, a = Re IFFT(Z),
+   b = Im IFFT(Z).  Exact in the same way as one line per transform. */
+static int io_rplan_exec_pair(const io_rplan *p, double *ca, double *cb, int forward, double fct)
+{
+    const size_t n = p->n;
+    oc_t *z = io_scratch2(n);
+    if (!z) return -1;
+    if (forward) {
+        for (size_t m = 0; m < n; ++m) { z[m].r = ca[m]; z[m].i = cb[m]; }
+        int rc = io_cplan_exec(p->cp, (double *)z, 1, fct);
+        if (rc) return rc;
+        ca[0] = z[0].r;
+        cb[0] = z[0].i;
+        for (size_t k = 1; 2 * k < n + 1; ++k) {
+            const oc_t zk = z[k], zm = z[n - k];
+            ca[2 * k - 1] = 0.5 * (zk.r + zm.r);
+            ca[2 * k] = 0.5 * (zk.i - zm.i);
+            cb[2 * k - 1] = 0.5 * (zk.i + zm.i);
+            cb[2 * k] = 0.5 * (zm.r - zk.r);
+        }
+    } else {
+        z[0].r = ca[0];
+        z[0].i = cb[0];
+        for (size_t k = 1; 2 * k < n + 1; ++k) {
+            const double ar = ca[2 * k - 1], ai = ca[2 * k], br = cb[2 * k - 1], bi = cb[2 * k];
+            z[k].r = ar - bi;       /* A[k] + i B[k] */
+            z[k].i = ai + br;
+            z[n - k].r = ar + bi;   /* conj A[k] + i conj B[k] */
+            z[n - k].i = br - ai;
+        }
+        int rc = io_cplan_exec(p->cp, (double *)z, 0, fct);
+        if (rc) return rc;
+        for (size_t m = 0; m < n; ++m) { ca[m] = z[m].r; cb[m] = z[m].i; }
+    }
+    return 0;
+}
+
 static void *io_batch_worker(void *arg)
 {
     io_batch_job *j = (io_batch_job *)arg;
     size_t lo = j->batch * j->t / j->nt, hi = j->batch * (j->t + 1) / j->nt;
+    const int pair = j->real && ((const io_rplan *)j->plan)->n % 2 == 1 && ((const io_rplan *)j->plan)->n > 1;
     for (size_t b = lo; b < hi; ++b) {
         double *line = j->base + b * j->dist;
-        int rc = j->real ? io_rplan_exec((const io_rplan *)j->plan, line, j->forward, j->fct)
+        int rc;
+        if (pair && b + 1 < hi) {
+            rc = io_rplan_exec_pair((const io_rplan *)j->plan, line, line + j->dist, j->forward, j->fct);
+            ++b;
+        } else {
+            rc = j->real ? io_rplan_exec((const io_rplan *)j->plan, line, j->forward, j->fct)
                          : io_cplan_exec((const io_cplan *)j->plan, line, j->forward, j->fct);
+        }
         if (rc) j->rc = rc;
     }
+    if (j->t) io_scratch_release();  /* worker threads end here */
     return NULL;
 }
 
@@ -538,23 +755,89 @@ static int io_run_batch(const void *plan, int real, double *c, size_t batch, siz
     return rc;
 }
 
+/* Plan cache of the batch drivers, like the C++ backend's get_plan LRU
+   (pocketfft_hdronly.h:2655-2706): a few recent plans per kind, shared by
+   callers (plans are read-only while they execute), reference-counted so
+   that an evicted plan lives until its last user is done. */
+#define IO_CACHE 8
+typedef struct {
+    int real;
+    size_t n;
+    void *plan;
+    unsigned long long used;
+    int refs;
+    int dead;
+} io_cache_ent;
+static io_cache_ent io_cache[IO_CACHE];
+static unsigned long long io_cache_clock = 0;
+static pthread_mutex_t io_cache_mu = PTHREAD_MUTEX_INITIALIZER;
+
+static void io_plan_free(int real, void *plan)
+{
+    if (real) io_destroy_rplan((io_rplan *)plan);
+    else io_destroy_cplan((io_cplan *)plan);
+}
+
+static void *io_plan_get(int real, size_t n, int *slot)
+{
+    pthread_mutex_lock(&io_cache_mu);
+    for (int i = 0; i < IO_CACHE; ++i)
+        if (io_cache[i].plan && !io_cache[i].dead && io_cache[i].real == real && io_cache[i].n == n) {
+            io_cache[i].used = ++io_cache_clock;
+            io_cache[i].refs++;
+            *slot = i;
+            pthread_mutex_unlock(&io_cache_mu);
+            return io_cache[i].plan;
+        }
+    pthread_mutex_unlock(&io_cache_mu);
+    void *plan = real ? (void *)io_make_rplan(n) : (void *)io_make_cplan(n);
+    if (!plan) return NULL;
+    pthread_mutex_lock(&io_cache_mu);
+    int victim = -1;
+    for (int i = 0; i < IO_CACHE; ++i) {
+        if (!io_cache[i].plan) { victim = i; break; }
+        if (io_cache[i].refs == 0 && (victim < 0 || io_cache[i].used < io_cache[victim].used)) victim = i;
+    }
+    if (victim < 0) {  /* every entry in use: run uncached */
+        pthread_mutex_unlock(&io_cache_mu);
+        *slot = -1;
+        return plan;
+    }
+    if (io_cache[victim].plan) io_plan_free(io_cache[victim].real, io_cache[victim].plan);
+    io_cache_ent e = { real, n, plan, ++io_cache_clock, 1, 0 };
+    io_cache[victim] = e;
+    *slot = victim;
+    pthread_mutex_unlock(&io_cache_mu);
+    return plan;
+}
+
+static void io_plan_put(int real, void *plan, int slot)
+{
+    if (slot < 0) { io_plan_free(real, plan); return; }
+    pthread_mutex_lock(&io_cache_mu);
+    io_cache[slot].refs--;
+    pthread_mutex_unlock(&io_cache_mu);
+}
+
 /* batch lines of n complex numbers, line b at c + 2*b*dist doubles */
 int io_cfft_batch(size_t n, size_t batch, double *c, size_t dist, int forward, double fct, int nthreads)
 {
-    io_cplan *p = io_make_cplan(n);
+    int slot;
+    io_cplan *p = (io_cplan *)io_plan_get(0, n, &slot);
     if (!p) return -1;
     int rc = io_run_batch(p, 0, c, batch, 2 * dist, forward, fct, nthreads);
-    io_destroy_cplan(p);
+    io_plan_put(0, p, slot);
     return rc;
 }
 
 /* batch lines of n reals (halfcomplex in place), line b at c + b*dist doubles */
 int io_rfft_batch(size_t n, size_t batch, double *c, size_t dist, int forward, double fct, int nthreads)
 {
-    io_rplan *p = io_make_rplan(n);
+    int slot;
+    io_rplan *p = (io_rplan *)io_plan_get(1, n, &slot);
     if (!p) return -1;
     int rc = io_run_batch(p, 1, c, batch, dist, forward, fct, nthreads);
-    io_destroy_rplan(p);
+    io_plan_put(1, p, slot);
     return rc;
 }
 

@@ -23,6 +23,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libimpulse_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpocketfft_ref.so")
+REF_SCALAR_SO = os.path.join(HERE, "_ref", "libpocketfft_ref_scalar.so")
 
 _sz = C.c_size_t
 _pd = C.c_ssize_t
@@ -44,7 +45,7 @@ def build(ref: bool | None = None) -> None:
         if not present:
             raise RuntimeError("IMPULSE_REF must name an impulse checkout (with impulse/fft) to build the "
                                f"reference PocketFFT; got {refdir!r}")
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"IMPULSE_REF={refdir}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "ref-scalar", f"IMPULSE_REF={refdir}"], check=True)
 
 
 _lib = None
@@ -92,6 +93,22 @@ def lib():
 
 def ref_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+_ref_scalar = None
+
+
+def ref_scalar():
+    """The reference built without PocketFFT's SIMD (as on aarch64): r2r_fftpack
+    and the C backend's rfft_forward / rfft_backward line loop."""
+    global _ref_scalar
+    if _ref_scalar is None:
+        L = C.CDLL(REF_SCALAR_SO)
+        L.ref_rfft_batch.argtypes = [_sz, _sz, _dp, C.c_int, C.c_double]
+        L.ref_r2r_fftpack_f64.argtypes = [_sz, C.POINTER(_sz), C.POINTER(_pd), C.POINTER(_pd), _sz,
+                                          C.POINTER(_sz), C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double, _sz]
+        _ref_scalar = L
+    return _ref_scalar
 
 
 def ref():

@@ -17,6 +17,9 @@
 #include <stdexcept>
 #include <string>
 #include "pocketfft_hdronly.h"
+extern "C" {
+#include "pocketfft.h"  // the reference's C backend (impulse/fft/c_pocketfft/pocketfft.h)
+}
 
 static thread_local std::string g_err;
 
@@ -116,6 +119,20 @@ const char *ref_last_error(void) { return g_err.c_str(); }
                                             (const T *)in, (T *)out, (T)fct, nthreads);            \
     });                                                                                            \
   }
+
+// The C backend's per-line loop as impulse's fft(var openArray[float]) runs
+// it (pocketfft.nim:290-303 over rfft_forward / rfft_backward), for `batch`
+// contiguous lines of n reals, one plan for all of them.
+int ref_rfft_batch(size_t n, size_t batch, double *c, int forward, double fct)
+{
+  rfft_plan plan = make_rfft_plan(n);
+  if (!plan) return -1;
+  int rc = 0;
+  for (size_t b = 0; b < batch && rc == 0; ++b)
+    rc = forward ? rfft_forward(plan, c + b * n, fct) : rfft_backward(plan, c + b * n, fct);
+  destroy_rfft_plan(plan);
+  return rc;
+}
 
 REF_WRAP(double, f64)
 REF_WRAP(float, f32)
