@@ -2547,12 +2547,21 @@ int ig_fftconv_backward(ig_fftconv c, const void *x, const void *k, const void *
 // column passes; phase 1: row passes).  Lengths needing Bluestein over a
 // multi-pass core run on the general path.  The whole sequence can be
 // captured once into a CUDA graph.
-struct MultiPhase {
+// one persistent work-list launch: the groups of a phase that run the same
+// shared-memory kernel variant (elements per thread, buffering, radix class,
+// layout class)
+struct MultiPart {
+    int E = 16, db = 0, rs = RS_FULL, lay = LAY_GEN;
     std::vector<WorkGroup> groups;
     std::vector<long long> prefix;
     std::unique_ptr<DevBuf> d_groups, d_prefix;
     unsigned long long total = 0;
     size_t smem = 0;
+    int block = 0, grid = 0, slot = 0;  // slot: its counter
+};
+struct MultiPhase {
+    std::vector<WorkGroup> groups;  // before partitioning
+    std::vector<MultiPart> parts;
 };
 
 struct ig_multi_plan_i {
@@ -2570,6 +2579,7 @@ struct ig_multi_plan_i {
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> ev;  // ev[0] fork, ev[1 + i] join of side[i]
     std::unique_ptr<DevBuf> scratch, counter;
+    int nslots = 0;  // work-list counters, one per partition
     size_t n_wl = 0, n_4s = 0;
     cudaGraphExec_t gexec = nullptr;
     const void *g_in = nullptr;
@@ -2585,44 +2595,68 @@ struct ig_multi_plan_i {
 
 static const int kMultiSide = 8;
 
-static const int kWorklistThreads = 512;
-
-static void worklist_fit(Arith a, WorkGroup &g, size_t phase_smem)
+// Partition a phase's groups by kernel variant.  Each group keeps its core's
+// tuned configuration (elements per thread, buffering) and gets the lines per
+// CTA a stand-alone launch would; a partition's launch takes the largest
+// block and shared-memory size of its groups and as many CTAs as fit the GPU.
+static void finish_phase(Arith a, MultiPhase &ph, int &nslots)
 {
-    g.P.E = 16;
-    g.P.db = 0;  // the work-list kernel runs in-place stages
-    const long long tpl = (g.P.L + 15) / 16;
-    const long long line_bytes = (long long)g.P.LS * (long long)slot_bytes(a);
-    long long lpc = std::min<long long>(kMaxLinesPerCta, kWorklistThreads / tpl);
-    lpc = std::min<long long>(lpc, std::max<long long>(1, (long long)phase_smem / line_bytes));
-    lpc = std::max<long long>(1, std::min<long long>(lpc, g.io.nlines));
-    g.io.lpc = (int)lpc;
-    g.io.tpl = (int)tpl;
-    set_line_divs(g.io);
-}
-
-static void finish_phase(Arith a, MultiPhase &ph)
-{
-    if (ph.groups.empty()) return;
-    size_t smem = 0;
-    for (auto &g : ph.groups) smem = std::max(smem, (size_t)g.P.LS * slot_bytes(a));
-    smem = std::max<size_t>(smem, std::min<size_t>((size_t)max_smem(), 96 * 1024));
-    smem = std::min<size_t>(smem, (size_t)max_smem());
-    ph.smem = smem;
-    ph.prefix.clear();
-    unsigned long long tot = 0;
-    for (auto &g : ph.groups) {
-        worklist_fit(a, g, smem);
-        ph.prefix.push_back((long long)tot);
-        tot += (unsigned long long)((g.io.nlines + g.io.lpc - 1) / g.io.lpc);
+    std::map<std::tuple<int, int, int, int>, size_t> index;
+    int sms = 0;
+    ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_id()), "SM count");
+    for (WorkGroup g : ph.groups) {
+        long long line_bytes = 0;
+        const long long lpc = smem_lpc(a, g.P, g.io, line_bytes);
+        const long long tpl = (g.P.L + g.P.E - 1) / g.P.E;
+        g.io.lpc = (int)lpc;
+        g.io.tpl = (int)tpl;
+        set_line_divs(g.io);
+        g.io.lay = choose_layout(a, g.io);
+        int lay = g.io.lay == LAY_C2C || g.io.lay == LAY_TW ? g.io.lay : LAY_GEN;
+        if (a == A_F64) lay = LAY_GEN;
+        int rs = g.P.rs;
+        if (lay == LAY_GEN) rs = RS_FULL;
+        else if (g.P.E == 16 && rs == RS_P235) rs = RS_ALL;
+        const auto key = std::make_tuple(g.P.E, g.P.db, rs, lay);
+        auto it = index.find(key);
+        if (it == index.end()) {
+            it = index.emplace(key, ph.parts.size()).first;
+            ph.parts.emplace_back();
+            MultiPart &np = ph.parts.back();
+            np.E = g.P.E;
+            np.db = g.P.db;
+            np.rs = rs;
+            np.lay = lay;
+            np.slot = nslots++;
+        }
+        MultiPart &pt = ph.parts[it->second];
+        pt.smem = std::max(pt.smem, (size_t)(lpc * line_bytes));
+        pt.block = std::max(pt.block, (int)(lpc * tpl));
+        pt.groups.push_back(g);
     }
-    ph.total = tot;
-    ph.d_groups.reset(new DevBuf(ph.groups.size() * sizeof(WorkGroup)));
-    ph.d_prefix.reset(new DevBuf(ph.prefix.size() * sizeof(long long)));
-    ck(cudaMemcpy(ph.d_groups->p, ph.groups.data(), ph.groups.size() * sizeof(WorkGroup), cudaMemcpyHostToDevice),
-       "work list upload");
-    ck(cudaMemcpy(ph.d_prefix->p, ph.prefix.data(), ph.prefix.size() * sizeof(long long), cudaMemcpyHostToDevice),
-       "work list upload");
+    for (MultiPart &pt : ph.parts) {
+        pt.prefix.clear();
+        unsigned long long tot = 0;
+        for (auto &g : pt.groups) {
+            pt.prefix.push_back((long long)tot);
+            tot += (unsigned long long)((g.io.nlines + g.io.lpc - 1) / g.io.lpc);
+        }
+        pt.total = tot;
+        pt.d_groups.reset(new DevBuf(pt.groups.size() * sizeof(WorkGroup)));
+        pt.d_prefix.reset(new DevBuf(pt.prefix.size() * sizeof(long long)));
+        ck(cudaMemcpy(pt.d_groups->p, pt.groups.data(), pt.groups.size() * sizeof(WorkGroup), cudaMemcpyHostToDevice),
+           "work list upload");
+        ck(cudaMemcpy(pt.d_prefix->p, pt.prefix.data(), pt.prefix.size() * sizeof(long long), cudaMemcpyHostToDevice),
+           "work list upload");
+        int per_sm = 0;
+        cudaError_t e = a == A_F32 ? Launch<TagF32>::worklist_occupancy(pt.E, pt.db, pt.rs, pt.lay, pt.block, pt.smem, &per_sm)
+                      : a == A_DF  ? Launch<TagDF>::worklist_occupancy(pt.E, pt.db, pt.rs, pt.lay, pt.block, pt.smem, &per_sm)
+                                   : Launch<TagF64>::worklist_occupancy(pt.E, pt.db, pt.rs, pt.lay, pt.block, pt.smem, &per_sm);
+        ck(e, "work list occupancy");
+        pt.grid = (int)std::min<unsigned long long>((unsigned long long)sms * (unsigned long long)std::max(1, per_sm),
+                                                    std::max<unsigned long long>(1, pt.total));
+    }
+    ph.groups.clear();
 }
 
 // parts: 1 work-list phase 0 (single-CTA groups, four-step column passes),
@@ -2641,30 +2675,26 @@ static void multi_launch(ig_multi_plan_i &m, const void *in, void *out, cudaStre
             exec_op(m.a, OP_C2C, m.len[i], ln, m.fwd, m.fct, m.side[m.gstream[k]]);
         }
     }
-    const int smcount = [] {
-        int v = 0;
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device_id());
-        return v > 0 ? v : 1;
-    }();
-    ck(cudaMemsetAsync(m.counter->p, 0, 2 * sizeof(unsigned long long), st), "work list counter");
+    if (m.nslots) ck(cudaMemsetAsync(m.counter->p, 0, m.nslots * sizeof(unsigned long long), st), "work list counter");
     for (int k = 0; k < 2; ++k) {
-        MultiPhase &ph = m.ph[k];
-        if (!ph.total || !(parts & (1 << k))) continue;
-        int grid = (int)std::min<unsigned long long>((unsigned long long)smcount, ph.total);
-        unsigned long long *ctr = (unsigned long long *)m.counter->p + k;
-        void *scr = m.scratch ? m.scratch->p : nullptr;
-        cudaError_t e =
-            m.a == A_F32 ? Launch<TagF32>::fft_worklist((const WorkGroup *)ph.d_groups->p,
-                                                        (const long long *)ph.d_prefix->p, (int)ph.groups.size(),
-                                                        ph.total, ctr, in, out, scr, grid, ph.smem, st)
-          : m.a == A_DF  ? Launch<TagDF>::fft_worklist((const WorkGroup *)ph.d_groups->p,
-                                                       (const long long *)ph.d_prefix->p, (int)ph.groups.size(),
-                                                       ph.total, ctr, in, out, scr, grid, ph.smem, st)
-                         : Launch<TagF64>::fft_worklist((const WorkGroup *)ph.d_groups->p,
-                                                        (const long long *)ph.d_prefix->p, (int)ph.groups.size(),
-                                                        ph.total, ctr, in, out, scr, grid, ph.smem, st);
-        ck(e, "work list launch");
-        count_launch();
+        if (!(parts & (1 << k))) continue;
+        for (MultiPart &pt : m.ph[k].parts) {
+            if (!pt.total) continue;
+            unsigned long long *ctr = (unsigned long long *)m.counter->p + pt.slot;
+            void *scr = m.scratch ? m.scratch->p : nullptr;
+            const WorkGroup *gd = (const WorkGroup *)pt.d_groups->p;
+            const long long *pd = (const long long *)pt.d_prefix->p;
+            const int ng = (int)pt.groups.size();
+            cudaError_t e =
+                m.a == A_F32 ? Launch<TagF32>::fft_worklist(pt.E, pt.db, pt.rs, pt.lay, gd, pd, ng, pt.total, ctr, in, out,
+                                                            scr, pt.grid, pt.block, pt.smem, st)
+              : m.a == A_DF  ? Launch<TagDF>::fft_worklist(pt.E, pt.db, pt.rs, pt.lay, gd, pd, ng, pt.total, ctr, in, out,
+                                                           scr, pt.grid, pt.block, pt.smem, st)
+                             : Launch<TagF64>::fft_worklist(pt.E, pt.db, pt.rs, pt.lay, gd, pd, ng, pt.total, ctr, in,
+                                                            out, scr, pt.grid, pt.block, pt.smem, st);
+            ck(e, "work list launch");
+            count_launch();
+        }
     }
     if (gen) {
         for (size_t i = 0; i < m.side.size(); ++i) {
@@ -2768,8 +2798,16 @@ ig_multi_plan ig_make_multi_plan(int dtype, size_t count, const size_t *lengths,
             soff += c.M;
             ++m->n_4s;
         }
-        finish_phase(m->a, m->ph[0]);
-        finish_phase(m->a, m->ph[1]);
+        int optin0 = max_smem() + 1024;
+        static std::once_flag once0[3];
+        std::call_once(once0[m->a], [&] {
+            cudaError_t e = m->a == A_F32 ? Launch<TagF32>::set_max_smem(optin0)
+                          : m->a == A_DF  ? Launch<TagDF>::set_max_smem(optin0)
+                                          : Launch<TagF64>::set_max_smem(optin0);
+            ck(e, "cudaFuncSetAttribute");
+        });
+        finish_phase(m->a, m->ph[0], m->nslots);
+        finish_phase(m->a, m->ph[1], m->nslots);
         if (!m->general.empty()) {
             // longest first onto the least loaded side stream (cost ~ N log N)
             const int ns = (int)std::min<size_t>(kMultiSide, m->general.size());
@@ -2797,15 +2835,7 @@ ig_multi_plan ig_make_multi_plan(int dtype, size_t count, const size_t *lengths,
                 m->gstream[k] = best;
             }
         }
-        m->counter.reset(new DevBuf(2 * sizeof(unsigned long long)));
-        int optin = max_smem() + 1024;
-        static std::once_flag once[3];
-        std::call_once(once[m->a], [&] {
-            cudaError_t e = m->a == A_F32 ? Launch<TagF32>::set_max_smem(optin)
-                          : m->a == A_DF  ? Launch<TagDF>::set_max_smem(optin)
-                                          : Launch<TagF64>::set_max_smem(optin);
-            ck(e, "cudaFuncSetAttribute");
-        });
+        m->counter.reset(new DevBuf(std::max(1, m->nslots) * sizeof(unsigned long long)));
         plan = m.release();
     });
     return plan;

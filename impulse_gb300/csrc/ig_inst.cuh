@@ -17,6 +17,10 @@ template <class T, int E, bool DB>
 cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
 template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes);
 template <class T, int E, bool DB>
+cudaError_t launch_worklist_E(int rs, int lay, const WorkGroup *groups, const long long *prefix, int ngroups,
+                              unsigned long long total, unsigned long long *counter, const char *in, char *out,
+                              char *scr, int grid, int block, size_t smem, cudaStream_t st, int *per_sm);
+template <class T, int E, bool DB>
 cudaError_t launch_line_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
 template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes);
 
@@ -58,17 +62,25 @@ template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
         if ((e = set_smem_line_E<T, 16, false>(bytes)) != cudaSuccess) return e;
         if ((e = set_smem_line_E<T, 16, true>(bytes)) != cudaSuccess) return e;
     }
-    return set_smem_attr(k_fft_worklist<T, 16>, bytes);
+    return cudaSuccess;
 }
 template <class Tag>
-cudaError_t Launch<Tag>::fft_worklist(const WorkGroup *groups, const long long *prefix, int ngroups,
-                                      unsigned long long total, unsigned long long *counter, const void *in,
-                                      void *out, void *scr, int grid, size_t smem, cudaStream_t st)
+cudaError_t Launch<Tag>::fft_worklist(int E, int db, int rs, int lay, const WorkGroup *groups, const long long *prefix,
+                                      int ngroups, unsigned long long total, unsigned long long *counter,
+                                      const void *in, void *out, void *scr, int grid, int block, size_t smem,
+                                      cudaStream_t st)
 {
     using T = typename TagType<Tag>::T;
-    k_fft_worklist<T, 16><<<grid, 512, smem, st>>>(groups, prefix, ngroups, total, counter, (const char *)in,
-                                                   (char *)out, (char *)scr);
-    return cudaGetLastError();
+    auto f = E == 8 ? launch_worklist_E<T, 8, true> : db ? launch_worklist_E<T, 16, true> : launch_worklist_E<T, 16, false>;
+    return f(rs, lay, groups, prefix, ngroups, total, counter, (const char *)in, (char *)out, (char *)scr, grid, block,
+             smem, st, nullptr);
+}
+template <class Tag>
+cudaError_t Launch<Tag>::worklist_occupancy(int E, int db, int rs, int lay, int block, size_t smem, int *per_sm)
+{
+    using T = typename TagType<Tag>::T;
+    auto f = E == 8 ? launch_worklist_E<T, 8, true> : db ? launch_worklist_E<T, 16, true> : launch_worklist_E<T, 16, false>;
+    return f(rs, lay, nullptr, nullptr, 0, 0, nullptr, nullptr, nullptr, nullptr, 0, block, smem, 0, per_sm);
 }
 template <class Tag> cudaError_t Launch<Tag>::stage_tw(void *tw, int R, int ns)
 {

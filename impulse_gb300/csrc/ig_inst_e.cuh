@@ -41,6 +41,60 @@ cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaS
     return cudaGetLastError();
 }
 
+// work-list variants: the same (radix class, layout class) choice as
+// launch_fft_E; with per_sm set, report CTAs per SM instead of launching
+template <class T, int E, bool DB, int RS, int LAY>
+static cudaError_t worklist_one(const WorkGroup *groups, const long long *prefix, int ngroups, unsigned long long total,
+                                unsigned long long *counter, const char *in, char *out, char *scr, int grid, int block,
+                                size_t smem, cudaStream_t st, int *per_sm)
+{
+    auto k = k_fft_worklist<T, E, RS, LAY, DB>;
+    if (per_sm) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, block, smem);
+    k<<<grid, block, smem, st>>>(groups, prefix, ngroups, total, counter, in, out, scr);
+    return cudaGetLastError();
+}
+
+template <class T, int E, bool DB, int RS>
+static cudaError_t worklist_rs(int lay, const WorkGroup *groups, const long long *prefix, int ngroups,
+                               unsigned long long total, unsigned long long *counter, const char *in, char *out,
+                               char *scr, int grid, int block, size_t smem, cudaStream_t st, int *per_sm)
+{
+#define IG_W(LAY_) worklist_one<T, E, DB, RS, LAY_>(groups, prefix, ngroups, total, counter, in, out, scr, grid, block, smem, st, per_sm)
+    switch (lay) {
+    case LAY_C2C: return IG_W(LAY_C2C);
+    case LAY_TW: return IG_W(LAY_TW);
+    default: return worklist_one<T, E, DB, RS_FULL, LAY_GEN>(groups, prefix, ngroups, total, counter, in, out, scr,
+                                                            grid, block, smem, st, per_sm);
+    }
+#undef IG_W
+}
+
+template <class T, int E, bool DB>
+cudaError_t launch_worklist_E(int rs, int lay, const WorkGroup *groups, const long long *prefix, int ngroups,
+                              unsigned long long total, unsigned long long *counter, const char *in, char *out,
+                              char *scr, int grid, int block, size_t smem, cudaStream_t st, int *per_sm)
+{
+    if constexpr (!Variants<T, E>::kSpecialised) {
+        return worklist_one<T, E, DB, RS_FULL, LAY_GEN>(groups, prefix, ngroups, total, counter, in, out, scr, grid,
+                                                       block, smem, st, per_sm);
+    } else {
+        if (lay != LAY_C2C && lay != LAY_TW)
+            return worklist_one<T, E, DB, RS_FULL, LAY_GEN>(groups, prefix, ngroups, total, counter, in, out, scr,
+                                                           grid, block, smem, st, per_sm);
+        if (rs == RS_P2)
+            return worklist_rs<T, E, DB, RS_P2>(lay, groups, prefix, ngroups, total, counter, in, out, scr, grid, block,
+                                                smem, st, per_sm);
+        if (E == 8 && rs == RS_P235)
+            return worklist_rs<T, E, DB, (E == 8 ? RS_P235 : RS_ALL)>(lay, groups, prefix, ngroups, total, counter, in,
+                                                                    out, scr, grid, block, smem, st, per_sm);
+        if (rs == RS_ALL || rs == RS_P235)
+            return worklist_rs<T, E, DB, RS_ALL>(lay, groups, prefix, ngroups, total, counter, in, out, scr, grid,
+                                                 block, smem, st, per_sm);
+        return worklist_rs<T, E, DB, RS_FULL>(lay, groups, prefix, ngroups, total, counter, in, out, scr, grid, block,
+                                              smem, st, per_sm);
+    }
+}
+
 template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes)
 {
     cudaError_t e = set_smem_attr(k_fft_smem<T, E, RS_FULL, LAY_GEN, DB>, bytes);
@@ -57,7 +111,16 @@ template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes)
         IG_S(RS_FULL)
         if constexpr (E == 8) { IG_S(RS_P235) }
 #undef IG_S
+#define IG_SW(RS_)                                                                                        \
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_, LAY_C2C, DB>, bytes);                 \
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_, LAY_TW, DB>, bytes);
+        IG_SW(RS_P2)
+        IG_SW(RS_ALL)
+        IG_SW(RS_FULL)
+        if constexpr (E == 8) { IG_SW(RS_P235) }
+#undef IG_SW
     }
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_FULL, LAY_GEN, DB>, bytes);
     return e;
 }
 

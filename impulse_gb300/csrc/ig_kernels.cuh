@@ -99,27 +99,31 @@ __device__ __forceinline__ int line_i0(const IODesc &io, long long l)
 
 __device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
 
-// Line-scale keys: the biased exponent of |x| as if x were normal (double
-// subnormals get their true exponent below the normal range, down to -51;
-// float subnormals down to -22), plus kKeyOff, so that 0 stays "no value"
-// (zeros, infinities and NaN).  A line's exact power-of-two scale is
-// (bias + kKeyOff) - (largest key of the line).
+// Line-scale keys.  A line's elements are reduced to the largest magnitude
+// word (dmag: the high 32 bits of |x| for doubles, fmag: |x| for floats,
+// whose unsigned order is the order of |x|; two integer operations per
+// element), and that maximum to a key once: the biased exponent as if the
+// value were normal (double subnormals get their true exponent below the
+// normal range, down to -19 from the high word -- values under 2^-1042 count
+// as zero; float subnormals down to -22), plus kKeyOff, so that 0 stays "no
+// value" (zeros; infinities and NaN dominate the maximum and also give 0, no
+// rescaling).  A line's exact power-of-two scale is (bias + kKeyOff) - key.
 constexpr int kKeyOff = 64;
-__device__ __forceinline__ int dkey(double x)
+__device__ __forceinline__ unsigned dmag(double x) { return (unsigned)(__double_as_longlong(x) >> 32) & 0x7fffffffu; }
+__device__ __forceinline__ unsigned fmag(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+__device__ __forceinline__ int dkey_mag(unsigned m)
 {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
-    const int e = (int)(u >> 52);
-    if (e != 0 && e != 0x7ff) return e + kKeyOff;
-    if (e == 0x7ff || u == 0) return 0;
-    return (63 - __clzll((long long)u)) - 51 + kKeyOff;
+    const int e = (int)(m >> 20);
+    if (e == 0x7ff || m == 0) return 0;
+    if (e) return e + kKeyOff;
+    return (31 - __clz((int)m)) - 19 + kKeyOff;
 }
-__device__ __forceinline__ int fkey(float x)
+__device__ __forceinline__ int fkey_mag(unsigned m)
 {
-    const unsigned u = __float_as_uint(x) & 0x7fffffffu;
-    const int e = (int)(u >> 23);
-    if (e != 0 && e != 0xff) return e + kKeyOff;
-    if (e == 0xff || u == 0) return 0;
-    return (31 - __clz((int)u)) - 22 + kKeyOff;
+    const int e = (int)(m >> 23);
+    if (e == 0xff || m == 0) return 0;
+    if (e) return e + kKeyOff;
+    return (31 - __clz((int)m)) - 22 + kKeyOff;
 }
 
 // slot read with optional raw-double conversion
@@ -528,7 +532,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         for (int attempt = 0; attempt < (scaled ? 2 : 1); ++attempt) {
             const int esc = (scaled && act) ? s_esc[2 * gi] : 0;
             const int escb = (scaled && act) ? s_esc[2 * gi + 1] : 0;
-            int emax = 0, emaxb = 0;
+            unsigned emax = 0, emaxb = 0;  // largest magnitude words (dmag / fmag)
             if (act && (LAY == LAY_C2C || LAY == LAY_R2HC || LAY == LAY_TW)) {
                 // complex units, no conjugation / Hermitian steps / pairs
                 constexpr int CH = 4;
@@ -546,7 +550,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                         const int u = u0 + c * tpl;
                         if (u >= cnt) break;
                         if constexpr (RAW) {
-                            emax = max(emax, max(dkey(v[c].x), dkey(v[c].y)));
+                            emax = max(emax, max(dmag(v[c].x), dmag(v[c].y)));
                         }
                         cx<T> z{Store<T>::in(v[c].x, esc), Store<T>::in(v[c].y, esc)};
                         sput(line + sp(u, pad), cc ? conjx(z) : z);
@@ -573,11 +577,11 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                         const int u = u0 + c * tpl;
                         if (u >= cnt) break;
                         if constexpr (RAW) {
-                            emax = max(emax, dkey(va[c]));
-                            emaxb = max(emaxb, dkey(vb[c]));
+                            emax = max(emax, dmag(va[c]));
+                            emaxb = max(emaxb, dmag(vb[c]));
                         } else {
-                            emax = max(emax, fkey(va[c]));
-                            emaxb = max(emaxb, fkey(vb[c]));
+                            emax = max(emax, fmag(va[c]));
+                            emaxb = max(emaxb, fmag(vb[c]));
                         }
                         sput(line + sp(u, pad), cx<T>{Store<T>::in(va[c], esc), Store<T>::in(vb[c], escb)});
                     }
@@ -606,11 +610,11 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     if (io.pre != PRE_NONE && (u == 0 || (io.pre == PRE_HERM_EVEN && u == M))) { im = S(0); ib = S(0); }
                     if (scaled) {
                         if constexpr (RAW) {
-                            emax = max(emax, max(dkey(re), dkey(im)));
-                            emaxb = max(emaxb, max(dkey(rb), dkey(ib)));
+                            emax = max(emax, max(dmag(re), dmag(im)));
+                            emaxb = max(emaxb, max(dmag(rb), dmag(ib)));
                         } else {
-                            emax = max(emax, max(fkey((float)re), fkey((float)im)));
-                            emaxb = max(emaxb, max(fkey((float)rb), fkey((float)ib)));
+                            emax = max(emax, max(fmag((float)re), fmag((float)im)));
+                            emaxb = max(emaxb, max(fmag((float)rb), fmag((float)ib)));
                         }
                     }
                     if (!paired) {
@@ -634,8 +638,11 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 }
             }
             if (!scaled || attempt == 1) break;
-            if (act && emax > 0) atomicMax(&s_emax[2 * gi], emax);
-            if (act && emaxb > 0) atomicMax(&s_emax[2 * gi + 1], emaxb);
+            {
+                const int ka = RAW ? dkey_mag(emax) : fkey_mag(emax), kb = RAW ? dkey_mag(emaxb) : fkey_mag(emaxb);
+                if (act && ka > 0) atomicMax(&s_emax[2 * gi], ka);
+                if (act && kb > 0) atomicMax(&s_emax[2 * gi + 1], kb);
+            }
             __syncthreads();
             for (int l = threadIdx.x; l < nl; l += blockDim.x) {
                 const int ea = s_emax[2 * l], eb = s_emax[2 * l + 1];  // line-scale keys
@@ -1040,12 +1047,15 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_smem_regs<T, E, RS, DB>(
 // of group g (binary search on prefix).  Groups hold their own core and line
 // descriptors; their in/out pointers are byte offsets from one of three
 // bases (0: input, 1: output, 2: scratch).  Items are claimed with one
-// atomic per block; the counter is reset before every launch.
-template <class T, int E>
-__global__ void __launch_bounds__(512, 1) k_fft_worklist(const WorkGroup *__restrict__ groups,
-                                                         const long long *__restrict__ prefix, int ngroups,
-                                                         unsigned long long total, unsigned long long *counter,
-                                                         const char *in, char *out, char *scr)
+// atomic per block; the counter is reset before every launch.  One
+// instantiation per shared-memory kernel variant (elements per thread,
+// buffering, radix class, layout class): the host partitions the groups by
+// the variant their core and layout ask for and launches each partition with
+// as many CTAs as the occupancy calculator allows.
+template <class T, int E, int RS, int LAY, bool DB>
+__global__ void __launch_bounds__(512) __maxnreg__((fft_smem_regs<T, E, RS, DB>()))
+    k_fft_worklist(const WorkGroup *__restrict__ groups, const long long *__restrict__ prefix, int ngroups,
+                   unsigned long long total, unsigned long long *counter, const char *in, char *out, char *scr)
 {
     __shared__ unsigned long long s_item;
     for (;;) {
@@ -1063,8 +1073,8 @@ __global__ void __launch_bounds__(512, 1) k_fft_worklist(const WorkGroup *__rest
         const WorkGroup &G = groups[lo];
         const char *ib = G.in_base == 0 ? in : G.in_base == 1 ? (const char *)out : (const char *)scr;
         char *ob = G.out_base == 1 ? out : G.out_base == 2 ? scr : (char *)in;
-        fft_block<T, E, RS_FULL, LAY_GEN>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]), ib + (size_t)G.io.in,
-                        ob + (size_t)G.io.out);
+        fft_block<T, E, RS, LAY, DB>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]),
+                                     ib + (size_t)G.io.in, ob + (size_t)G.io.out);
         __syncthreads();
     }
 }
@@ -1086,7 +1096,7 @@ template <> struct Loc<df> {
     int esc = 0;
     __device__ void fit(double a, double b, double c = 0.0, double d = 0.0)
     {
-        const int e = max(max(dkey(a), dkey(b)), max(dkey(c), dkey(d)));
+        const int e = dkey_mag(max(max(dmag(a), dmag(b)), max(dmag(c), dmag(d))));
         esc = e > 0 ? 1023 + kKeyOff - e : 0;
     }
     __device__ cx<df> in(double re, double im) const { return cx<df>{df_from_double(re, esc), df_from_double(im, esc)}; }
@@ -1292,19 +1302,20 @@ __global__ void k_line_exp(const __grid_constant__ IODesc io, int *__restrict__ 
     const long long l = blockIdx.x;
     const char *base = io.in + line_off(io, l, false);
     const bool has_b = 2LL * line_i0(io, l) + 1 < io.pair_n0;
-    int ea = 0, eb = 0;
+    unsigned ma = 0, mb = 0;
     for (int u = threadIdx.x; u < io.cnt_in; u += blockDim.x) {
         S re, im, rb = S(0), ib = S(0);
         load_unit<S, S2>(io, base, u, re, im);
         if (has_b) load_unit<S, S2>(io, base + io.pair_in, u, rb, ib);
         if constexpr (sizeof(S) == 8) {
-            ea = max(ea, max(dkey((double)re), dkey((double)im)));
-            eb = max(eb, max(dkey((double)rb), dkey((double)ib)));
+            ma = max(ma, max(dmag((double)re), dmag((double)im)));
+            mb = max(mb, max(dmag((double)rb), dmag((double)ib)));
         } else {
-            ea = max(ea, max(fkey((float)re), fkey((float)im)));
-            eb = max(eb, max(fkey((float)rb), fkey((float)ib)));
+            ma = max(ma, max(fmag((float)re), fmag((float)im)));
+            mb = max(mb, max(fmag((float)rb), fmag((float)ib)));
         }
     }
+    const int ea = sizeof(S) == 8 ? dkey_mag(ma) : fkey_mag(ma), eb = sizeof(S) == 8 ? dkey_mag(mb) : fkey_mag(mb);
     if (ea) atomicMax(&s_e[0], ea);
     if (eb) atomicMax(&s_e[1], eb);
     __syncthreads();

@@ -20,9 +20,12 @@ template <class Tag> struct Launch {
     // same descriptors, for complex lines and even real lines to halfcomplex
     static cudaError_t fft_line(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
     static cudaError_t set_max_smem(int bytes);
-    static cudaError_t fft_worklist(const WorkGroup *groups, const long long *prefix, int ngroups,
-                                    unsigned long long total, unsigned long long *counter, const void *in, void *out,
-                                    void *scr, int grid, size_t smem, cudaStream_t st);
+    // persistent work-list launch of the k_fft_smem variant (E, db, rs, lay):
+    // `grid` CTAs of `block` threads; `occupancy` reports CTAs per SM for it
+    static cudaError_t fft_worklist(int E, int db, int rs, int lay, const WorkGroup *groups, const long long *prefix,
+                                    int ngroups, unsigned long long total, unsigned long long *counter, const void *in,
+                                    void *out, void *scr, int grid, int block, size_t smem, cudaStream_t st);
+    static cudaError_t worklist_occupancy(int E, int db, int rs, int lay, int block, size_t smem, int *per_sm);
     static cudaError_t stage_tw(void *tw, int R, int ns);
     static cudaError_t roots(void *out, long long count, unsigned long long mult, unsigned long long D);
     static cudaError_t convert64(const void *in, void *out, long long n);

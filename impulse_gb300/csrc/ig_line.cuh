@@ -58,15 +58,16 @@ __device__ __forceinline__ int line_first(cx<T> *line, const char *base, long lo
     }
     int esc = 0;
     if constexpr (RAW) {
-        int emax = 0;  // largest line-scale key (dkey) of the thread's values
+        unsigned mm = 0;  // largest magnitude word (dmag) of the thread's values
 #pragma unroll
         for (int i = 0; i < NB; ++i) {
             const int j = t + i * tpl;
             if (act && j < nr) {
 #pragma unroll
-                for (int m = 0; m < R; ++m) emax = max(emax, max(dkey(raw[i][m].x), dkey(raw[i][m].y)));
+                for (int m = 0; m < R; ++m) mm = max(mm, max(dmag(raw[i][m].x), dmag(raw[i][m].y)));
             }
         }
+        const int emax = dkey_mag(mm);
         // common case: every thread's largest value inside the safe window
         // 2^+-40 (all-zero threads are safe); otherwise the CTA takes the
         // exact per-line maximum
@@ -288,11 +289,13 @@ __device__ __forceinline__ void line_last_r2hc(const cx<T> *src, char *obase, lo
     }
 
 // register caps: 512-thread CTAs (lines of 4096 / 8192 units) must fit the
-// 64 K register file; FP32 8-element complex lines run two such CTAs per SM
+// 64 K register file; FP32 8-element lines run two such CTAs per SM (four of
+// 256 threads: the halfcomplex variant spills a few bytes at this cap, and
+// measured faster with the extra CTA than without the spill)
 template <class T, int E, int RS, int K, bool DB> constexpr int fft_line_regs()
 {
     if constexpr (std::is_same<T, df>::value) return 128;
-    return E == 8 ? (K == LK_C2C ? 64 : 72) : 128;
+    return E == 8 ? 64 : 128;
 }
 
 // One CTA: `lpc` lines of `tpl` threads; shared memory lpc * LSt complex slots

@@ -105,7 +105,7 @@ def test_halfcomplex_range_scaling(engine, oracle_lib, n):
         assert oracle_lib.rel_l2(back[r], x[r]) < 2 * F64_TOL, (n, r)
 
 
-@pytest.mark.parametrize("n", [65521, 8191, 29403])
+@pytest.mark.parametrize("n", [65521, 8191, 29403, 4096, 2205, 18144])
 def test_halfcomplex_range_scaling_rader_and_odd_multipass(engine, oracle_lib, n):
     """Rader lines (65521 over a multi-pass core, 8191) and an odd four-step
     length, with rows at 1e300, 1e-300 and double-subnormal 1e-310 paired in
@@ -136,3 +136,19 @@ def test_halfcomplex_range_scaling_rader_and_odd_multipass(engine, oracle_lib, n
     want_b = scaled_oracle(spec, False, 1.0 / n)
     for r in range(7):
         assert oracle_lib.rel_l2(back[r], want_b[r]) < F64_TOL, (n, r, "backward")
+
+
+@pytest.mark.parametrize("n", [4096, 1000, 2048, 65536])
+def test_complex_range_scaling_subnormal_rows(engine, oracle_lib, n):
+    """Complex lines of double subnormals (and huge ones) next to unit lines:
+    every line keeps FP64 accuracy (single-CTA line kernel and four-step)."""
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(n + 5)
+    scales = np.array([1e-310, 1.0, 1e300, 1e-309, 3e-308])[:, None]
+    z = (rng.standard_normal((5, n)) + 1j * rng.standard_normal((5, n))) * scales
+    for fwd in (True, False):
+        got = F.cfft_batch(z, fwd, 1.0)
+        for r in range(5):
+            e = -int(np.floor(np.log2(np.max(np.abs(z[r])))))
+            want = oracle_lib.cfft(z[r] * 2.0 ** e, fwd, 1.0) * 2.0 ** -e
+            assert oracle_lib.rel_l2(got[r], want) < F64_TOL, (n, r, fwd)
