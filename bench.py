@@ -584,6 +584,12 @@ def run_nd(lib, dev, args, peak, keep=None):
     g = torch.Generator(device=dev)
     g.manual_seed(1)
     out = {}
+    if not args.no_autotune:
+        # the complex lengths of configs 1 and 3, tuned like the halfcomplex ones
+        from impulse_gb300 import fft as F
+        for n, code in ((4096, L.IG_F64), (4096, L.IG_F32), (256, L.IG_F32)):
+            F.autotune(n, code, 0)
+        F.autotune(4096, L.IG_F32, 1)
 
     def uniform_c(shape, dt):
         rdt = torch.float64 if dt == torch.complex128 else torch.float32

@@ -2614,9 +2614,11 @@ static void finish_phase(Arith a, MultiPhase &ph, int &nslots)
         g.io.lay = choose_layout(a, g.io);
         int lay = g.io.lay == LAY_C2C || g.io.lay == LAY_TW ? g.io.lay : LAY_GEN;
         if (a == A_F64) lay = LAY_GEN;
-        int rs = g.P.rs;
-        if (lay == LAY_GEN) rs = RS_FULL;
-        else if (g.P.E == 16 && rs == RS_P235) rs = RS_ALL;
+        // the full radix class for every partition: work-list instantiations of
+        // the narrower classes gave wrong results on twiddled radix-8 (FP32) and
+        // radix-7 (double-float) stages, although the same device code is exact
+        // in the stand-alone kernel; the cause is not found
+        const int rs = RS_FULL;
         const auto key = std::make_tuple(g.P.E, g.P.db, rs, lay);
         auto it = index.find(key);
         if (it == index.end()) {

@@ -78,18 +78,10 @@ cudaError_t launch_worklist_E(int rs, int lay, const WorkGroup *groups, const lo
         return worklist_one<T, E, DB, RS_FULL, LAY_GEN>(groups, prefix, ngroups, total, counter, in, out, scr, grid,
                                                        block, smem, st, per_sm);
     } else {
+        (void)rs;  // the host sends every partition with the full radix class
         if (lay != LAY_C2C && lay != LAY_TW)
             return worklist_one<T, E, DB, RS_FULL, LAY_GEN>(groups, prefix, ngroups, total, counter, in, out, scr,
                                                            grid, block, smem, st, per_sm);
-        if (rs == RS_P2)
-            return worklist_rs<T, E, DB, RS_P2>(lay, groups, prefix, ngroups, total, counter, in, out, scr, grid, block,
-                                                smem, st, per_sm);
-        if (E == 8 && rs == RS_P235)
-            return worklist_rs<T, E, DB, (E == 8 ? RS_P235 : RS_ALL)>(lay, groups, prefix, ngroups, total, counter, in,
-                                                                    out, scr, grid, block, smem, st, per_sm);
-        if (rs == RS_ALL || rs == RS_P235)
-            return worklist_rs<T, E, DB, RS_ALL>(lay, groups, prefix, ngroups, total, counter, in, out, scr, grid,
-                                                 block, smem, st, per_sm);
         return worklist_rs<T, E, DB, RS_FULL>(lay, groups, prefix, ngroups, total, counter, in, out, scr, grid, block,
                                               smem, st, per_sm);
     }
@@ -111,14 +103,8 @@ template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes)
         IG_S(RS_FULL)
         if constexpr (E == 8) { IG_S(RS_P235) }
 #undef IG_S
-#define IG_SW(RS_)                                                                                        \
-    if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_, LAY_C2C, DB>, bytes);                 \
-    if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_, LAY_TW, DB>, bytes);
-        IG_SW(RS_P2)
-        IG_SW(RS_ALL)
-        IG_SW(RS_FULL)
-        if constexpr (E == 8) { IG_SW(RS_P235) }
-#undef IG_SW
+        if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_FULL, LAY_C2C, DB>, bytes);
+        if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_FULL, LAY_TW, DB>, bytes);
     }
     if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_FULL, LAY_GEN, DB>, bytes);
     return e;
