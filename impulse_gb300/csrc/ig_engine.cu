@@ -2573,7 +2573,7 @@ struct ig_multi_plan_i {
     MultiPhase ph[2];
     std::vector<std::unique_ptr<DevBuf>> tables;
     std::vector<long long> general;
-    // general transforms run on side streams (fork / join around the work
+    // general transforms run on up to 16 side streams (fork / join around the work
     // list): their launches are small, so several run at once
     std::vector<int> gstream;  // side stream of general[k]
     std::vector<cudaStream_t> side;
@@ -2593,7 +2593,7 @@ struct ig_multi_plan_i {
     }
 };
 
-static const int kMultiSide = 8;
+static const int kMultiSide = 16;
 
 // Partition a phase's groups by kernel variant.  Each group keeps its core's
 // tuned configuration (elements per thread, buffering) and gets the lines per

@@ -1058,18 +1058,36 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_smem_regs<T, E, RS, DB>(
                    unsigned long long total, unsigned long long *counter, const char *in, char *out, char *scr)
 {
     __shared__ unsigned long long s_item;
+    __shared__ int s_group;
+    if (threadIdx.x == 0) s_group = 0;
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1ull);
+        if (threadIdx.x == 0) {
+            const unsigned long long w = atomicAdd(counter, 1ull);
+            s_item = w;
+            // a CTA's claims increase, so its group index only moves forward:
+            // gallop from the previous group, then bisect (no full search of
+            // dependent loads per item)
+            if (w < total) {
+                int lo = s_group, step = 1, hi = lo;
+                while (hi + 1 < ngroups && (unsigned long long)prefix[hi + 1] <= w) {
+                    lo = hi + 1;
+                    hi = min(ngroups - 1, hi + step);
+                    step <<= 1;
+                }
+                if ((unsigned long long)prefix[hi] > w) --hi;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if ((unsigned long long)prefix[mid] <= w) lo = mid;
+                    else hi = mid - 1;
+                }
+                s_group = lo;
+            }
+        }
         __syncthreads();
         const unsigned long long w = s_item;
+        const int lo = s_group;
         __syncthreads();
         if (w >= total) break;
-        int lo = 0, hi = ngroups - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if ((unsigned long long)prefix[mid] <= w) lo = mid;
-            else hi = mid - 1;
-        }
         const WorkGroup &G = groups[lo];
         const char *ib = G.in_base == 0 ? in : G.in_base == 1 ? (const char *)out : (const char *)scr;
         char *ob = G.out_base == 1 ? out : G.out_base == 2 ? scr : (char *)in;

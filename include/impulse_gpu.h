@@ -160,7 +160,7 @@ int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff
  * fit one CTA and runs them, with the column passes of longer four-step
  * lengths, through one persistent work-list launch; a second launch runs the
  * row passes; lengths needing Bluestein or Rader over a multi-pass core use
- * the general path, on up to eight side streams forked from and joined back
+ * the general path, on up to sixteen side streams forked from and joined back
  * into the caller's stream.  ig_multi_exec_graph captures that sequence into a CUDA graph
  * on its first call for given pointers and replays it afterwards;
  * ig_multi_exec_loop_device is the one-call-per-transform pattern, for
