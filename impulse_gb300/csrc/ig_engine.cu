@@ -1946,12 +1946,14 @@ static void nd_c2r_device(Arith a, size_t ndim, const size_t *shape_out, const p
     std::vector<ptrdiff_t> sinter(ndim);
     sinter[ndim - 1] = (ptrdiff_t)ce;
     for (size_t d = ndim - 1; d-- > 0;) sinter[d] = sinter[d + 1] * (ptrdiff_t)shape_in[d + 1];
-    DevBuf tmp(prod(ndim, shape_in.data()) * ce);
-    nd_c2c_device(a, ndim, shape_in.data(), sin, sinter.data(), naxes - 1, axes, forward, in, tmp.p, 1.0, st);
-    for_lines(ndim, shape_out, sinter.data(), sout, last, (const char *)tmp.p, (char *)out, [&](const Lines &ln) {
+    // the temporary (pocketfft_hdronly.h:3384 allocates it per call) is a grow-only
+    // workspace of the stream, kept between calls (slot 7: the multi-pass paths
+    // of the line transforms use slots 0-6)
+    void *tmp = scratch_for(st).get(7, prod(ndim, shape_in.data()) * ce);
+    nd_c2c_device(a, ndim, shape_in.data(), sin, sinter.data(), naxes - 1, axes, forward, in, tmp, 1.0, st);
+    for_lines(ndim, shape_out, sinter.data(), sout, last, (const char *)tmp, (char *)out, [&](const Lines &ln) {
         exec_op(a, OP_C2R, (long long)shape_out[last], ln, forward, fct, st);
     });
-    ck(cudaStreamSynchronize(st), "c2r temporary");
 }
 
 int ig_c2r_device(int dtype, size_t ndim, const size_t *shape_out, const ptrdiff_t *sin, const ptrdiff_t *sout,

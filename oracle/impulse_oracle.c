@@ -454,7 +454,7 @@ static int io_stockham_exec(const io_cplan *p, oc_t *x, oc_t *scratch, int forwa
 }
 
 /* per-thread scratch of at least `count` complex values, kept between calls
-   (freed at thread exit by io_scratch_release in the batch workers) */
+   (the batch workers are persistent pool threads) */
 static __thread oc_t *io_tls_buf = NULL;
 static __thread size_t io_tls_len = 0;
 static oc_t *io_scratch(size_t count)
@@ -481,18 +481,6 @@ static oc_t *io_scratch2(size_t count)
 }
 static __thread oc_t *io_tls_blue = NULL;
 static __thread size_t io_tls_blue_len = 0;
-static void io_scratch_release(void)
-{
-    free(io_tls_buf);
-    io_tls_buf = NULL;
-    io_tls_len = 0;
-    free(io_tls_buf2);
-    io_tls_buf2 = NULL;
-    io_tls_len2 = 0;
-    free(io_tls_blue);
-    io_tls_blue = NULL;
-    io_tls_blue_len = 0;
-}
 
 /* Bluestein (pocketfft.c:1945-2008): premultiply by the chirp, convolve with
    the chirp through two length-n2 FFTs, postmultiply by the chirp. */
@@ -731,7 +719,38 @@ static void *io_batch_worker(void *arg)
         }
         if (rc) j->rc = rc;
     }
-    if (j->t) io_scratch_release();  /* worker threads end here */
+    return NULL;
+}
+
+/* A persistent worker pool for the batch drivers (the C++ backend keeps one
+   too, pocketfft_hdronly.h:651-667): workers sleep on a condition variable;
+   a batch call hands out its job slices and waits for them.  One batch call
+   at a time uses the pool (others run their slices on their own thread). */
+#define IO_POOL_MAX 256
+static pthread_mutex_t io_pool_mu = PTHREAD_MUTEX_INITIALIZER;
+static pthread_cond_t io_pool_cv = PTHREAD_COND_INITIALIZER, io_pool_done = PTHREAD_COND_INITIALIZER;
+static pthread_mutex_t io_pool_busy = PTHREAD_MUTEX_INITIALIZER;
+static int io_pool_size = 0;              /* workers started */
+static unsigned long long io_pool_gen = 0; /* bumped per batch call */
+static io_batch_job *io_pool_jobs = NULL;
+static int io_pool_njobs = 0, io_pool_pending = 0;
+
+static void *io_pool_main(void *arg)
+{
+    const int me = (int)(size_t)arg; /* serves job slot me (slot 0 is the caller's) */
+    unsigned long long seen = 0;
+    pthread_mutex_lock(&io_pool_mu);
+    for (;;) {
+        while (io_pool_gen == seen) pthread_cond_wait(&io_pool_cv, &io_pool_mu);
+        seen = io_pool_gen;
+        if (me < io_pool_njobs) {
+            io_batch_job *j = &io_pool_jobs[me];
+            pthread_mutex_unlock(&io_pool_mu);
+            io_batch_worker(j);
+            pthread_mutex_lock(&io_pool_mu);
+            if (--io_pool_pending == 0) pthread_cond_signal(&io_pool_done);
+        }
+    }
     return NULL;
 }
 
@@ -739,19 +758,47 @@ static int io_run_batch(const void *plan, int real, double *c, size_t batch, siz
 {
     if (nthreads < 1) nthreads = 1;
     if ((size_t)nthreads > batch) nthreads = (int)(batch ? batch : 1);
+    if (nthreads > IO_POOL_MAX) nthreads = IO_POOL_MAX;
     io_batch_job *jobs = (io_batch_job *)calloc((size_t)nthreads, sizeof(io_batch_job));
-    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
-    if (!jobs || !th) { free(jobs); free(th); return -1; }
+    if (!jobs) return -1;
     for (int t = 0; t < nthreads; ++t) {
         io_batch_job v = { plan, real, c, batch, dist, forward, fct, (size_t)t, (size_t)nthreads, 0 };
         jobs[t] = v;
     }
-    for (int t = 1; t < nthreads; ++t) pthread_create(&th[t], NULL, io_batch_worker, &jobs[t]);
-    io_batch_worker(&jobs[0]);
-    int rc = jobs[0].rc;
-    for (int t = 1; t < nthreads; ++t) { pthread_join(th[t], NULL); if (jobs[t].rc) rc = jobs[t].rc; }
+    int rc = 0;
+    if (nthreads > 1 && pthread_mutex_trylock(&io_pool_busy) == 0) {
+        pthread_mutex_lock(&io_pool_mu);
+        while (io_pool_size < nthreads - 1) {
+            pthread_t th;
+            if (pthread_create(&th, NULL, io_pool_main, (void *)(size_t)(io_pool_size + 1)) != 0) break;
+            pthread_detach(th);
+            ++io_pool_size;
+        }
+        const int njobs = io_pool_size + 1 < nthreads ? io_pool_size + 1 : nthreads;
+        /* slices are re-cut for the workers available */
+        for (int t = 0; t < njobs; ++t) { jobs[t].t = (size_t)t; jobs[t].nt = (size_t)njobs; }
+        io_pool_jobs = jobs;
+        io_pool_njobs = njobs;
+        io_pool_pending = njobs - 1;
+        ++io_pool_gen;
+        pthread_cond_broadcast(&io_pool_cv);
+        pthread_mutex_unlock(&io_pool_mu);
+        io_batch_worker(&jobs[0]);
+        pthread_mutex_lock(&io_pool_mu);
+        while (io_pool_pending > 0) pthread_cond_wait(&io_pool_done, &io_pool_mu);
+        io_pool_jobs = NULL;
+        io_pool_njobs = 0;
+        pthread_mutex_unlock(&io_pool_mu);
+        pthread_mutex_unlock(&io_pool_busy);
+        for (int t = 0; t < njobs; ++t) if (jobs[t].rc) rc = jobs[t].rc;
+    } else {
+        /* single-threaded, or the pool is serving another call */
+        jobs[0].t = 0;
+        jobs[0].nt = 1;
+        io_batch_worker(&jobs[0]);
+        rc = jobs[0].rc;
+    }
     free(jobs);
-    free(th);
     return rc;
 }
 
