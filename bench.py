@@ -368,6 +368,22 @@ def run_ours(args, rank, world):
         for ln in open(prof):
             if ln.startswith("dram_bytes_per_algorithmic_byte:"):
                 traffic = round(float(ln.split(":")[1]) * sb / len(single))
+    # compute (issue) roofline of the same kernel: thread instructions per complex point from the
+    # ncu capture in profiles/ x complex points per second, against the SM issue peak (4
+    # schedulers x 32 lanes per SM per clock) at the sampled SM clock
+    compute = None
+    ipp = os.path.join(ROOT, "profiles", "instr_per_point.txt")
+    if os.path.exists(ipp) and single and clocks.get("sm_mhz"):
+        for ln in open(ipp):
+            if ln.startswith("df_halfcomplex_4096:"):
+                inst = float(ln.split(":")[1])
+                sms = torch.cuda.get_device_properties(dev).multi_processor_count
+                peak_ti = sms * 4 * 32 * clocks["sm_mhz"] * 1e6 / 1e12
+                ach_ti = inst * (achieved * 1e9 / 32.0) / 1e12  # 32 bytes (16 in, 16 out) per complex point
+                compute = {"bound": "instruction issue (double-float arithmetic on the FP32 pipes)",
+                           "instr_per_complex_point": inst, "achieved": round(ach_ti, 2),
+                           "peak": round(peak_ti, 2), "unit": "T thread-instructions/s",
+                           "frac": round(ach_ti / peak_ti, 3)}
     slow = [(n, round(2 * 8 * n * b / (t / 1e3) / 1e9, 1)) for (n, b, *_), t in zip(items64, per_ms)]
     result = {
         "metric": "FFT GB/s (halfcomplex real FFT, algorithmic bytes) vs HBM peak",
@@ -398,6 +414,7 @@ def run_ours(args, rank, world):
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s",
                      "workload_achieved": round(workload_achieved, 1),
+                     "compute_roofline": compute,
                      "note": "achieved = algorithmic bytes of the single-launch lengths / their event-timed "
                              "launch durations; traffic = ncu DRAM bytes per algorithmic byte x bytes per launch; "
                              "workload_achieved covers every length, multi-pass ones included"},

@@ -535,7 +535,9 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             unsigned emax = 0, emaxb = 0;  // largest magnitude words (dmag / fmag)
             if (act && (LAY == LAY_C2C || LAY == LAY_R2HC || LAY == LAY_TW)) {
                 // complex units, no conjugation / Hermitian steps / pairs
-                constexpr int CH = 4;
+                // loads in flight per thread before the first is used: the prologue is
+                // latency-bound on global loads; FP32 units are small enough for eight
+                constexpr int CH = RAW ? 4 : 8;
                 const int cnt = io.cnt_in;
                 const long long is = io.is;
                 for (int u0 = ti; u0 < cnt; u0 += CH * tpl) {
@@ -558,7 +560,9 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 }
             } else if (act && LAY == LAY_PR2HC) {
                 // two real lines -> (a, b)
-                constexpr int CH = 4;
+                // loads in flight per thread before the first is used: the prologue is
+                // latency-bound on global loads; FP32 units are small enough for eight
+                constexpr int CH = RAW ? 4 : 8;
                 const int cnt = io.cnt_in;
                 const long long is = io.is;
                 for (int u0 = ti; u0 < cnt; u0 += CH * tpl) {
