@@ -719,23 +719,63 @@ PROFILE_CASES = {
     "rfft4096_f64": ("r", "f64", 4096, 16384),
     "rfft4096_f32": ("r", "f32", 4096, 32768),
     "c2c4096_f64": ("c", "f64", 4096, 8192),
+    "c2c4096_f32": ("c", "f32", 4096, 16384),
     "rfft2205_f64": ("r", "f64", 2205, 7609),
     "rfft52272_f64": ("r", "f64", 52272, 321),
     "rfft52272_f32": ("r", "f32", 52272, 642),
     "c2c4096x4096_f32_axes01": ("n", "f32", 4096, 4096),
     "rfft1009_f64": ("r", "f64", 1009, 16628),
     "rfft65521_f64": ("r", "f64", 65521, 256),
+    "rfft8191_f64": ("r", "f64", 8191, 2048),
+    # every 10th transform of the uneven-length workload (FP32, work-list graph)
+    "uneven_tenth_f32": ("u", "f32", 0, 10),
+    # FFT convolution forward, 4 images 2048^2 f32, 31x31 filters, padded to 4096^2
+    "conv4_f32": ("v", "f32", 2048, 4),
 }
 
 
 def run_case(name):
-    """One launch sequence of a small named case, for profiler captures."""
+    """One launch sequence of a small named case, for profiler captures.  Plans
+    and inputs are made first; only the transform runs between
+    cudaProfilerStart and cudaProfilerStop (ncu --profile-from-start off
+    captures just that)."""
     import torch
     from impulse_gb300 import _lib as L
     kind, dt, n, b = PROFILE_CASES[name]
     lib = L.load()
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     code = L.IG_F64 if dt == "f64" else L.IG_F32
+    prof = torch.cuda.cudart()
+    if kind == "u":
+        from impulse_gb300.batch import MultiFFT, uneven_lengths
+        lengths = uneven_lengths()[::b]
+        tot = sum(lengths)
+        x = torch.complex(torch.randn(tot, device="cuda"), torch.randn(tot, device="cuda"))
+        y = torch.empty_like(x)
+        plan = MultiFFT(lengths, code)
+        cs = torch.cuda.Stream()  # graph capture needs a created stream
+        plan.run(x.data_ptr(), y.data_ptr(), cs.cuda_stream, "graph")  # graph captured and instantiated here
+        torch.cuda.synchronize()
+        prof.cudaProfilerStart()
+        plan.run(x.data_ptr(), y.data_ptr(), cs.cuda_stream, "graph")
+        torch.cuda.synchronize()
+        prof.cudaProfilerStop()
+        print(json.dumps({"case": name, "ok": True, "transforms": len(lengths), "elements": tot}))
+        return
+    if kind == "v":
+        from impulse_gb300.fftconv import FFTConv2d
+        K = 31
+        x = torch.rand((b, n, n), device="cuda")
+        k = torch.randn((b, K, K), device="cuda")
+        op = FFTConv2d(b, n, n, K, b, torch.float32, recompute=True, pad=(2 * n, 2 * n))
+        op.forward(x, k)
+        torch.cuda.synchronize()
+        prof.cudaProfilerStart()
+        op.forward(x, k)
+        torch.cuda.synchronize()
+        prof.cudaProfilerStop()
+        print(json.dumps({"case": name, "ok": True}))
+        return
     if kind == "n":
         # multi-axis c2c of an n x b array over axes [0, 1]
         x = torch.randn((n, b), device="cuda", dtype=torch.complex128 if dt == "f64" else torch.complex64)
@@ -743,6 +783,10 @@ def run_case(name):
         torch.cuda.synchronize()
         _nd_call(lib, "c2c", code, x, y, [0, 1], True, 1.0, s)
         torch.cuda.synchronize()
+        prof.cudaProfilerStart()
+        _nd_call(lib, "c2c", code, x, y, [0, 1], True, 1.0, s)
+        torch.cuda.synchronize()
+        prof.cudaProfilerStop()
         print(json.dumps({"case": name, "ok": True}))
         return
     if kind == "r":
@@ -757,6 +801,10 @@ def run_case(name):
     torch.cuda.synchronize()
     L.check(fn(plan, x.data_ptr(), y.data_ptr(), b, n, n, 1, 1.0, s))
     torch.cuda.synchronize()
+    prof.cudaProfilerStart()
+    L.check(fn(plan, x.data_ptr(), y.data_ptr(), b, n, n, 1, 1.0, s))
+    torch.cuda.synchronize()
+    prof.cudaProfilerStop()
     print(json.dumps({"case": name, "ok": True}))
 
 

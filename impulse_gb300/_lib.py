@@ -101,6 +101,7 @@ SIGNATURES = {
     "ig_set_f64_arith": (C.c_int, [C.c_int]),
     "ig_release_caches": (None, []),
     "ig_launch_count": (C.c_ulonglong, [C.c_int]),
+    "ig_device_faults": (C.c_int, [C.POINTER(C.c_uint)]),
 }
 
 _lib = None

@@ -64,13 +64,13 @@ template <bool FWD, class R> IGD void dft4(cx<R> &x0, cx<R> &x1, cx<R> &x2, cx<R
 // multiply by exp(-+2 pi i e/8) for e = 1, 3 (e = 2 is rot)
 template <bool FWD, class R> IGD cx<R> w8_1(cx<R> a)
 {
-    constexpr R h = RealOps<R>::k(kSqrtHalf);
+    const R h = RealOps<R>::k(kSqrtHalf);
     if (FWD) return cx<R>{(a.r + a.i) * h, (a.i - a.r) * h};
     return cx<R>{(a.r - a.i) * h, (a.i + a.r) * h};
 }
 template <bool FWD, class R> IGD cx<R> w8_3(cx<R> a)
 {
-    constexpr R h = RealOps<R>::k(kSqrtHalf);
+    const R h = RealOps<R>::k(kSqrtHalf);
     if (FWD) return cx<R>{(a.i - a.r) * h, (-(a.r + a.i)) * h};
     return cx<R>{(-(a.r + a.i)) * h, (a.r - a.i) * h};
 }
@@ -104,11 +104,11 @@ template <bool FWD, class R> IGD void dft16(cx<R> *v)
     // now v[m1 + 4 q1] = Y[m1][q1]
     // w16^1 = (c, -+s), w16^2 = w8^1, w16^3 = (s, -+c), w16^4 = -+i, w16^6 = w8^3,
     // w16^9 = (-c, +-s), with c = cos(pi/8), s = sin(pi/8)
-    constexpr R c = RealOps<R>::k(kCos8), s = RealOps<R>::k(kSin8);
-    constexpr R w1i = RealOps<R>::k(FWD ? -kSin8 : kSin8);
-    constexpr R w3i = RealOps<R>::k(FWD ? -kCos8 : kCos8);
-    constexpr R w9r = RealOps<R>::k(-kCos8);
-    constexpr R w9i = RealOps<R>::k(FWD ? kSin8 : -kSin8);
+    const R c = RealOps<R>::k(kCos8), s = RealOps<R>::k(kSin8);
+    const R w1i = RealOps<R>::k(FWD ? -kSin8 : kSin8);
+    const R w3i = RealOps<R>::k(FWD ? -kCos8 : kCos8);
+    const R w9r = RealOps<R>::k(-kCos8);
+    const R w9i = RealOps<R>::k(FWD ? kSin8 : -kSin8);
     v[1 + 4 * 1] = cmulk(v[1 + 4 * 1], c, w1i);
     v[1 + 4 * 2] = w8_1<FWD>(v[1 + 4 * 2]);
     v[1 + 4 * 3] = cmulk(v[1 + 4 * 3], s, w3i);

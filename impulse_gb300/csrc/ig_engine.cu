@@ -86,6 +86,18 @@ static int device_id()
     return d;
 }
 
+// shared memory of one SM (all resident CTAs together)
+static long long smem_per_sm()
+{
+    static long long v = 0;
+    if (!v) {
+        int x = 0;
+        ck(cudaDeviceGetAttribute(&x, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device_id()), "smem attr");
+        v = x;
+    }
+    return v;
+}
+
 static int g_max_smem = 0;
 static int max_smem()
 {
@@ -417,6 +429,22 @@ static void build_stockham(Core &c, long long L, const std::vector<int> &rad)
         void *p = (char *)tw + (size_t)c.d.st[s].tw * twb;
         launch_stage_tw(c.a, p, rad[s], c.d.st[s].ns);
     }
+    // FP32 cores with an even first radix: the same twiddles laid out for
+    // butterfly pairs (k_fft_pair), stages after the first
+    c.d.twp = nullptr;
+    if (c.a == A_F32 && !rad.empty() && rad[0] % 2 == 0) {
+        long long offp = 0;
+        for (size_t s = 1; s < rad.size(); ++s) {
+            c.d.st[s].twp = (int)offp;
+            offp += (c.d.st[s].ns / 2) * (long long)(rad[s] - 1);
+        }
+        void *twp = c.alloc(std::max<long long>(offp, 1) * 16);
+        c.d.twp = twp;
+        for (size_t s = 1; s < rad.size(); ++s) {
+            ck(launch_stage_twp((char *)twp + (size_t)c.d.st[s].twp * 16, rad[s], c.d.st[s].ns), "pair twiddle table");
+            count_launch();
+        }
+    }
 }
 
 // Bluestein tables for a logical length M over a Stockham/four-step length L:
@@ -488,6 +516,7 @@ static bool rader_single(Arith a, long long M, const TuneCfg &cfg)
     std::vector<int> rad;
     if (!gpu_factor(M - 1, rad, cfg.E, cfg.order, cfg.no9) || !fits_smem(a, M - 1, M)) return false;
     if (elems_per_thread(M - 1, cfg.E) == 8) return true;
+    if (getenv("IG_RADER_SB")) return true;  // single-buffered 16-element Rader core (measurement)
     const long long slots = (M + 1) + ((M + 1) >> 3);
     return 2 * slots * (long long)slot_bytes(a) <= (long long)max_smem() - 4096;
 }
@@ -677,6 +706,67 @@ static bool line_kernel_ok(Arith a, const CoreDesc &d, const IODesc &io)
     return false;
 }
 
+// k_fft_line_pipe: FP32 lines whose input units are contiguous and whose
+// starts and sizes allow 16-byte bulk copies.  Off by default (IG_PIPE=1
+// turns it on, IG_PIPE_SLOTS=1|2 fixes the staging depth): its staging slots
+// cost CTAs per SM, and k_fft_line measured faster on every length tried
+// (rfft 4096: 2601 vs 1850 GB/s, c2c 4096: 3217 vs 2603, rfft 256: 3162 vs
+// 1960).
+static bool pipe_env()
+{
+    const char *v = getenv("IG_PIPE");
+    return v && atoi(v) != 0;
+}
+static const bool g_pipe_kernel = pipe_env();
+static int pipe_slots_env()
+{
+    const char *v = getenv("IG_PIPE_SLOTS");
+    return v ? std::max(1, std::min(2, atoi(v))) : 0;
+}
+static const int g_pipe_slots = pipe_slots_env();
+static bool pipe_ok(Arith a, const CoreDesc &d, const IODesc &io)
+{
+    if (!g_pipe_kernel || a != A_F32 || io.is != 8) return false;
+    const long long line_bytes = (long long)d.L * 8;
+    if (line_bytes % 16 || ((uintptr_t)io.in & 15)) return false;
+    for (int k = 0; k < 3; ++k)
+        if (io.bn[k] > 1 && (io.bsi[k] & 15)) return false;
+    return true;
+}
+static int sm_count()
+{
+    static int n = 0;
+    if (!n) ck(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device_id()), "SM count");
+    return n;
+}
+
+// k_fft_pair: FP32 complex lines and even real lines to halfcomplex whose
+// core has an even first radix, radices up to 8 or odd (the 7/11 class at
+// most), L / R even in every later stage, contiguous units in and out and
+// output line starts aligned for the 16-byte (complex) or 8-byte
+// (halfcomplex) stores (IG_NO_PAIR=1 turns it off)
+static const bool g_pair_kernel = getenv("IG_NO_PAIR") == nullptr;
+static bool pair_ok(Arith a, const CoreDesc &d, const IODesc &io)
+{
+    // below 512 points k_fft_line measured faster (a line's 16-element
+    // threads are too few: N = 96 real 1966 vs 1679 GB/s, 256 3070 vs 2675);
+    // from 512 on the pairs win (1200 real 1927 -> 2178, 1280 2145 -> 2421,
+    // 1680 1867 -> 2070, complex 4096 3263 -> 3529) or tie (4096 real)
+    if (!g_pair_kernel || a != A_F32 || !d.twp || d.L < 512 || d.rs > RS_ALL || io.is != 8) return false;
+    const int R0 = d.st[0].R;
+    if (R0 != 2 && R0 != 4 && R0 != 8) return false;
+    for (int s = 1; s < d.nst; ++s) {
+        const int R = d.st[s].R;
+        if (R == 16 || R == 13 || (d.L / R) % 2) return false;
+    }
+    const long long oal = io.lay == LAY_R2HC ? 8 : 16;
+    if (io.lay == LAY_R2HC ? io.os != 4 || !d.rtw : io.os != 8) return false;
+    if ((uintptr_t)io.out % oal) return false;
+    for (int k = 0; k < 3; ++k)
+        if (io.bn[k] > 1 && io.bso[k] % oal) return false;
+    return true;
+}
+
 // lines per CTA of a shared-memory launch of core d
 static long long smem_lpc(Arith a, const CoreDesc &d, const IODesc &io, long long &line_bytes)
 {
@@ -689,8 +779,13 @@ static long long smem_lpc(Arith a, const CoreDesc &d, const IODesc &io, long lon
     if (d.lpc_pref > 0) lpc = d.lpc_pref;
     lpc = std::min<long long>(lpc, kMaxLinesPerCta);
     lpc = std::min<long long>(lpc, std::max<long long>(1, kMaxThreads / tpl));
-    // keep three (or two) CTAs per SM when a line is small enough
-    long long budget = line_bytes * 3 <= smax ? smax / 3 : line_bytes * 2 <= smax ? smax / 2 : smax;
+    // keep three (or two) CTAs per SM when a line is small enough: a third
+    // (half) of the SM's shared memory less what each CTA holds besides its
+    // line buffers (the reserved 1 KB and the kernels' static arrays, at most
+    // 4 KB); a third of the per-block limit let only two CTAs in
+    const long long per_cta = 1024 + 4096, sm_total = smem_per_sm();
+    const long long b3 = sm_total / 3 - per_cta, b2 = sm_total / 2 - per_cta;
+    long long budget = line_bytes <= b3 ? b3 : line_bytes <= b2 ? b2 : smax;
     lpc = std::min<long long>(lpc, std::max<long long>(1, budget / line_bytes));
     return std::min<long long>(lpc, std::max<long long>(1, io.nlines));
 }
@@ -741,7 +836,40 @@ static void launch_smem(Arith a, const CoreDesc &d_in, IODesc io, cudaStream_t s
     long long grid = (io.nlines + lpc - 1) / lpc;
     if (grid > 0x7fffffffLL) raise(IG_ETOOLARGE, "too many lines for one launch");
     cudaError_t e;
-    if (line_kernel_ok(a, d, io))
+    // staging slots of the pipelined line kernel: two while the CTAs per SM
+    // that the line buffers allow stay the same with them (at most three are
+    // counted), else one; none when even one slot does not fit
+    int nslot = 0;
+    if (line_kernel_ok(a, d, io) && pipe_ok(a, d, io) && grid < (1LL << 30)) {
+        const size_t stage = (size_t)lpc * d.L * 8;
+        const size_t w = (smem + 127) / 128 * 128;
+        const size_t cap = (size_t)smax, per_sm = cap + 1024;
+        if (w + stage <= cap) {
+            nslot = g_pipe_slots ? g_pipe_slots : 1;
+            if (!g_pipe_slots && w + 2 * stage <= cap &&
+                per_sm / (w + 2 * stage + 1024) >= std::min<size_t>(3, per_sm / (w + stage + 1024)))
+                nslot = 2;
+            if (w + nslot * stage > cap) nslot = 1;
+        }
+    }
+    if (nslot) {
+        e = Launch<TagF32>::fft_line_pipe(d, io, smem, nslot, sm_count(), st);
+    } else if (line_kernel_ok(a, d, io) && pair_ok(a, d, io)) {
+        // 16 elements a thread; line buffers of GS padded 16-byte groups, two a line
+        const int GS = (d.L / 2 - 1) + ((d.L / 2 - 1) >> 3) + 1;
+        const long long tplp = (d.L + 15) / 16, lb = 2LL * GS * 16;
+        const long long per_cta = 1024 + 1024, b3 = smem_per_sm() / 3 - per_cta;
+        long long lp = d.lpc_pref > 0 ? d.lpc_pref : std::max<long long>(1, 256 / tplp);
+        lp = std::min<long long>(lp, std::max<long long>(1, kMaxThreads / tplp));
+        lp = std::min<long long>(lp, std::max<long long>(1, (lb <= b3 ? b3 : (long long)smax) / lb));
+        lp = std::min<long long>(std::min<long long>(lp, kMaxLinesPerCta), std::max<long long>(1, io.nlines));
+        IODesc iop = io;
+        iop.lpc = (int)lp;
+        iop.tpl = (int)tplp;
+        static std::once_flag once_pair;
+        std::call_once(once_pair, [&] { ck(set_smem_pair(smax + 1024), "cudaFuncSetAttribute"); });
+        e = launch_pair(d, iop, GS, (size_t)(lp * lb), st);
+    } else if (line_kernel_ok(a, d, io))
         e = a == A_F32 ? Launch<TagF32>::fft_line(d, io, smem, st) : Launch<TagDF>::fft_line(d, io, smem, st);
     else
         e = a == A_F32 ? Launch<TagF32>::fft_smem(d, io, smem, st)
@@ -1611,6 +1739,16 @@ void ig_release_caches(void)
 unsigned long long ig_launch_count(int reset)
 {
     return reset ? g_launches.exchange(0) : g_launches.load();
+}
+
+int ig_device_faults(unsigned *count)
+{
+    return guarded([&] {
+        if (!count) raise(IG_EINVAL, "null count");
+        *count = 0;
+        ck(cudaDeviceSynchronize(), "device synchronize");
+        ck(Launch<TagF32>::pipe_faults(count), "fault counters");
+    });
 }
 
 // ---- 1-D plans ----
@@ -2621,7 +2759,12 @@ static void finish_phase(Arith a, MultiPhase &ph, int &nslots)
         // radix-7 (double-float) stages, although the same device code is exact
         // in the stand-alone kernel; the cause is not found
         const int rs = RS_FULL;
-        const auto key = std::make_tuple(g.P.E, g.P.db, rs, lay);
+        // groups of 512-thread blocks (lines of 4096 points at 8 elements a
+        // thread) get their own partition: a partition launches with its
+        // largest block, and one 512-thread block per SM left the 256-thread
+        // groups at a third of the warps they could have
+        const int big = lpc * tpl > 256 ? 1 : 0;
+        const auto key = std::make_tuple(g.P.E, g.P.db, rs, lay * 2 + big);
         auto it = index.find(key);
         if (it == index.end()) {
             it = index.emplace(key, ph.parts.size()).first;

@@ -23,6 +23,10 @@ cudaError_t launch_worklist_E(int rs, int lay, const WorkGroup *groups, const lo
 template <class T, int E, bool DB>
 cudaError_t launch_line_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
 template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes);
+template <class T, int E, bool DB>
+cudaError_t launch_line_pipe_E(const CoreDesc &d, const IODesc &io, size_t work_bytes, int nslot, int sms,
+                               cudaStream_t st);
+template <class T, int E, bool DB> cudaError_t line_pipe_faults_E(unsigned *count);
 
 template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
@@ -40,6 +44,31 @@ template <class Tag> cudaError_t Launch<Tag>::fft_line(const CoreDesc &d, const 
         return d.E == 8 ? launch_line_E<T, 8, true>(d, io, smem, st)
              : d.db     ? launch_line_E<T, 16, true>(d, io, smem, st)
                         : launch_line_E<T, 16, false>(d, io, smem, st);
+    }
+}
+template <class Tag>
+cudaError_t Launch<Tag>::fft_line_pipe(const CoreDesc &d, const IODesc &io, size_t work_bytes, int nslot, int sms,
+                                       cudaStream_t st)
+{
+    using T = typename TagType<Tag>::T;
+    if constexpr (!std::is_same<T, float>::value) {
+        return cudaErrorNotSupported;  // FP32 only: double-float lines need the per-line range check
+    } else {
+        return d.E == 8 ? launch_line_pipe_E<T, 8, true>(d, io, work_bytes, nslot, sms, st)
+             : d.db     ? launch_line_pipe_E<T, 16, true>(d, io, work_bytes, nslot, sms, st)
+                        : launch_line_pipe_E<T, 16, false>(d, io, work_bytes, nslot, sms, st);
+    }
+}
+template <class Tag> cudaError_t Launch<Tag>::pipe_faults(unsigned *count)
+{
+    using T = typename TagType<Tag>::T;
+    if constexpr (!std::is_same<T, float>::value) {
+        return cudaSuccess;
+    } else {
+        cudaError_t e = line_pipe_faults_E<T, 8, true>(count);
+        if (e == cudaSuccess) e = line_pipe_faults_E<T, 16, true>(count);
+        if (e == cudaSuccess) e = line_pipe_faults_E<T, 16, false>(count);
+        return e;
     }
 }
 template <class K> static cudaError_t set_smem_attr(K kernel, int bytes)

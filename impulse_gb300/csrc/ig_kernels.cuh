@@ -1035,7 +1035,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
 // registers, which lets three 256-thread CTAs share an SM
 template <class T, int E, int RS, bool DB> constexpr int fft_smem_regs()
 {
-    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS >= RS_ALL ? 96 : 80;
+    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS >= RS_FULL ? 96 : 80;
     if constexpr (DB && E == 8 && std::is_same<T, float>::value) return 80;
     return 128;
 }

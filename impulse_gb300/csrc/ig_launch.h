@@ -19,6 +19,13 @@ template <class Tag> struct Launch {
     // k_fft_line (first / last stages fused with the HBM reads / writes): the
     // same descriptors, for complex lines and even real lines to halfcomplex
     static cudaError_t fft_line(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
+    // k_fft_line_pipe (FP32, contiguous lines): bulk-copy (TMA) staging of
+    // `nslot` tiles ahead, persistent CTAs on `sms` SMs; `work_bytes` = the
+    // line buffers of one CTA
+    static cudaError_t fft_line_pipe(const CoreDesc &d, const IODesc &io, size_t work_bytes, int nslot, int sms,
+                                     cudaStream_t st);
+    // adds the pipelined kernels' bounded-wait give-ups since the last call
+    static cudaError_t pipe_faults(unsigned *count);
     static cudaError_t set_max_smem(int bytes);
     // persistent work-list launch of the k_fft_smem variant (E, db, rs, lay):
     // `grid` CTAs of `block` threads; `occupancy` reports CTAs per SM for it
@@ -57,6 +64,13 @@ template <class Tag> struct Launch {
     static cudaError_t decimate(const void *C, long long P, int down, void *y, long long dy, long long ny, long long B,
                                 cudaStream_t st);
 };
+
+// k_fft_pair (ig_pair_f32.cu): FP32 lines with two butterflies per thread in
+// paired FP32 lanes; GS = padded 16-byte groups of one line buffer
+cudaError_t launch_pair(const CoreDesc &d, const IODesc &io, int GS, size_t smem, cudaStream_t st);
+cudaError_t set_smem_pair(int bytes);
+// pair twiddle table of one stage (ns even)
+cudaError_t launch_stage_twp(void *tw, int R, int ns);
 
 // FP64 helpers for Bluestein tables (built in ig_inst_df.cu)
 cudaError_t launch_chirp64(void *bk, long long n);

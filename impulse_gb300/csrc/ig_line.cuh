@@ -26,6 +26,7 @@
 // exact power-of-two scale, as in k_fft_smem.
 #pragma once
 #include "ig_kernels.cuh"
+#include "ig_tma.cuh"
 
 namespace ig {
 
@@ -398,6 +399,235 @@ cudaError_t launch_line_E(const CoreDesc &d, const IODesc &io, size_t smem, cuda
     return cudaGetLastError();
 }
 
+// --------------------------------------------------------------------------
+// k_fft_line_pipe: the same transform as k_fft_line on contiguous FP32 lines,
+// with the input lines brought into shared memory by bulk copies (TMA) one or
+// two tiles ahead.  A CTA is persistent: it walks tiles of `lpc` lines
+// (blockIdx.x, + gridDim.x, ...).  Thread 0 issues one cp.async.bulk per
+// line of a tile into a staging slot, completing on the slot's mbarrier;
+// after the first stage has read slot s, the slot is refilled with the tile
+// `nslot` steps ahead, so the copy of later lines overlaps the middle and
+// last stages of this one.  k_fft_line keeps each thread's eight global
+// loads in registers and waits on their latency with ~20 warps per SM; here
+// the copy engine holds the bytes in flight.
+// --------------------------------------------------------------------------
+
+// number of bounded-wait give-ups seen by this translation unit's pipelined
+// kernels (read and cleared by the host, ig_device_faults)
+static __device__ unsigned g_pipe_wait_fault;
+
+// polls of one mbarrier wait before a CTA gives up (each poll may suspend the
+// thread for a while; a tile lands in microseconds)
+constexpr unsigned kPipeWaitPolls = 1u << 22;
+
+// first stage from a staged line: unit u of the line is src[u]
+template <class T, int E, int R>
+__device__ __forceinline__ void line_first_sm(cx<T> *line, const typename Traits<T>::S2 *src, const CoreDesc &P,
+                                              int tpl, int t, bool act, bool cc)
+{
+    using S2 = typename Traits<T>::S2;
+    using B = Bfly<T>;
+    using V = typename B::V;
+    constexpr int NB = (E + R - 1) / R;
+    const int nr = P.L / R, pad = P.pad;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        const int j = t + i * tpl;
+        if (act && j < nr) {
+            V v[R];
+#pragma unroll
+            for (int m = 0; m < R; ++m) {
+                const S2 r = src[j + m * nr];
+                const cx<T> z{r.x, r.y};
+                v[m] = cc ? conjx(z) : z;
+            }
+            B::template dft<R>(v);
+            const int base_i = j * R;
+#pragma unroll
+            for (int m = 0; m < R; ++m) B::st(line + sp(base_i + m, pad), v[m]);
+        }
+        asm volatile("" ::: "memory");
+    }
+}
+
+// Shared memory: [lpc line buffers of LSt slots][nslot staging slots of lpc
+// lines x L units], the staging area starting at byte `stage_off` (a
+// multiple of 128).  Requires FP32 (no per-line range scaling), input units
+// contiguous along the line (io.is = 8 bytes), every line start and the
+// line size 16-byte aligned.
+// register cap of the pipelined variant: its staging slots already hold an
+// 8-element line's CTAs at three per SM, which leaves 85 registers a thread
+template <class T, int E, int RS, int K, bool DB> constexpr int fft_line_pipe_regs()
+{
+    return E == 8 ? 80 : 128;
+}
+
+template <class T, int E, int RS, int K, bool DB>
+__global__ void __launch_bounds__(512) __maxnreg__((fft_line_pipe_regs<T, E, RS, K, DB>()))
+    k_fft_line_pipe(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io, int nslot, int stage_off)
+{
+    static_assert(!Traits<T>::kRaw, "pipelined lines carry no range scaling");
+    using S2 = typename Traits<T>::S2;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ __align__(8) unsigned long long s_bar[2];
+    cx<T> *sm = reinterpret_cast<cx<T> *>(smraw);
+    S2 *stg = reinterpret_cast<S2 *>(smraw + stage_off);
+    const int LS = P.LS, LSt = DB ? 2 * LS : LS;
+    const int lpc = io.lpc, tpl = io.tpl;
+    const int units = P.L;
+    const unsigned line_bytes = (unsigned)units * (unsigned)sizeof(S2);
+    const int ntiles = (int)((io.nlines + lpc - 1) / lpc);
+    // tile `tile` into slot `s`: one bulk copy per line, one arrival
+    auto issue = [&](int tile, int s) {
+        const unsigned long long policy = l2_evict_first_policy();
+        const long long l0 = (long long)tile * lpc;
+        const int n = (int)min((long long)lpc, io.nlines - l0);
+        mbar_arrive_expect_tx(&s_bar[s], (unsigned)n * line_bytes);
+        S2 *dst = stg + (size_t)s * lpc * units;
+        for (int i = 0; i < n; ++i)
+            bulk_g2s(dst + (size_t)i * units, io.in + line_off(io, l0 + i, false), line_bytes, &s_bar[s], policy);
+    };
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < nslot; ++s) mbar_init(&s_bar[s], 1);
+        mbar_init_fence();
+        for (int s = 0; s < nslot; ++s) {
+            const long long tile = blockIdx.x + (long long)s * gridDim.x;
+            if (tile < ntiles) issue((int)tile, s);
+        }
+    }
+    __syncthreads();
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        // per-thread line and position, recomputed per tile rather than kept
+        // live across the stages
+        const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
+        const bool cc = K == LK_C2C && !io.fwd;
+        cx<T> *const line = sm + (size_t)g * LSt;
+        // the stage count is laundered per tile so that nothing derived from
+        // the last stage's descriptor is hoisted out of the loop and kept live
+        // across the stages
+        int nst = P.nst;
+        asm volatile("" : "+r"(nst));
+        const int s = it % nslot;
+        const unsigned par = (unsigned)(it / nslot) & 1u;
+        // every thread waits for the slot (bounded); the vote is also the
+        // barrier that keeps this tile's first stage behind the previous
+        // tile's last-stage reads of the line buffers
+        const bool ok = mbar_wait_bounded(&s_bar[s], par, kPipeWaitPolls);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicAdd(&g_pipe_wait_fault, 1u);
+            break;
+        }
+        const long long line0 = (long long)tile * lpc;
+        const int nl = (int)min((long long)lpc, io.nlines - line0);
+        const bool act = g < nl;
+        const S2 *src0 = stg + ((size_t)s * lpc + (act ? g : 0)) * units;
+        IG_LINE_EDGE_SWITCH(P.st[0].R, (line_first_sm<T, E, R_>(line, src0, P, tpl, t, act, cc)))
+        __syncthreads();
+        // slot s is consumed: refill it with the tile nslot steps ahead
+        if (threadIdx.x == 0) {
+            const long long nxt = tile + (long long)nslot * gridDim.x;
+            if (nxt < ntiles) {
+                fence_proxy_async_smem();
+                issue((int)nxt, s);
+            }
+        }
+        int cur = 0;
+        for (int si = 1; si < nst - 1; ++si) {
+            if constexpr (DB) {
+                const cx<T> *a = sm + cur;
+                cx<T> *b = sm + (LS - cur);
+                IG_LINE_RADIX_SWITCH(P.st[si].R, (stage_db<T, E, R_>(a, b, 2 * LS, P, si, nl, tpl, g, t)))
+                cur = LS - cur;
+                __syncthreads();
+            } else {
+                IG_LINE_RADIX_SWITCH(P.st[si].R, (stage<T, E, R_>(sm, P, si, nl, tpl, g, t)))
+            }
+        }
+        OutScale<T> sc;
+        sc.init(io);
+        if constexpr (K == LK_R2HC) sc.f *= 0.5f;  // the split's 1/2 joins the output scale
+        char *obase = io.out + (act ? line_off(io, line0 + g, true) : 0);
+        const cx<T> *src = line + cur;
+        if constexpr (K == LK_C2C) {
+            IG_LINE_EDGE_SWITCH(P.st[nst - 1].R,
+                                (line_last_c2c<T, E, R_>(src, obase, io.os, P, nst - 1, tpl, t, act, cc, sc, 0)))
+        } else {
+            switch (P.st[nst - 1].R) {
+            case 2: line_last_r2hc<T, E, 2>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, 0); break;
+            case 4: line_last_r2hc<T, E, 4>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, 0); break;
+            case 8: line_last_r2hc<T, E, 8>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, 0); break;
+            case 3:
+                if constexpr (rs_has<E, RS>(3)) line_last_r2hc<T, E, 3>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, 0);
+                break;
+            case 5:
+                if constexpr (rs_has<E, RS>(5)) line_last_r2hc<T, E, 5>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, 0);
+                break;
+            default: break;
+            }
+        }
+    }
+    // a CTA that gave up still has copies in flight into its staging slots:
+    // wait for them (bounded) before the shared memory is released
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < nslot; ++k) {
+            const int s = (it + k) % nslot;
+            const long long tile = blockIdx.x + (long long)(it + k) * gridDim.x;
+            if (tile < ntiles) mbar_wait_bounded(&s_bar[s], (unsigned)((it + k) / nslot) & 1u, kPipeWaitPolls);
+        }
+    }
+}
+
+template <class T, int E, bool DB, int RS, int K> static auto line_pipe_kernel()
+{
+    return k_fft_line_pipe<T, E, RS, K, DB>;
+}
+
+// Pipelined launch of one (arithmetic, elements per thread, buffering)
+// family.  `work_bytes` = lpc line buffers; nslot staging slots of lpc lines
+// follow at a 128-byte boundary; grid = SMs x resident CTAs (no more than
+// the tiles).  Returns cudaErrorNotSupported for a core outside the family.
+template <class T, int E, bool DB>
+cudaError_t launch_line_pipe_E(const CoreDesc &d, const IODesc &io, size_t work_bytes, int nslot, int sms,
+                               cudaStream_t st)
+{
+    if constexpr (Traits<T>::kRaw) {
+        return cudaErrorNotSupported;
+    } else {
+        using S2 = typename Traits<T>::S2;
+        const unsigned blk = (unsigned)(io.lpc * io.tpl);
+        const int stage_off = (int)((work_bytes + 127) / 128 * 128);
+        const size_t smem = (size_t)stage_off + (size_t)nslot * io.lpc * d.L * sizeof(S2);
+        const long long ntiles = (io.nlines + io.lpc - 1) / io.lpc;
+        const bool hc = io.lay == LAY_R2HC;
+        void (*kern)(CoreDesc, IODesc, int, int) = nullptr;
+        if (d.rs == RS_P2) kern = hc ? line_pipe_kernel<T, E, DB, RS_P2, LK_R2HC>() : line_pipe_kernel<T, E, DB, RS_P2, LK_C2C>();
+        else if (E == 8 && d.rs == RS_P235)
+            kern = hc ? line_pipe_kernel<T, E, DB, (E == 8 ? RS_P235 : RS_ALL), LK_R2HC>()
+                      : line_pipe_kernel<T, E, DB, (E == 8 ? RS_P235 : RS_ALL), LK_C2C>();
+        else if (d.rs == RS_ALL || d.rs == RS_P235)
+            kern = hc ? line_pipe_kernel<T, E, DB, RS_ALL, LK_R2HC>() : line_pipe_kernel<T, E, DB, RS_ALL, LK_C2C>();
+        else return cudaErrorNotSupported;
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)blk, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorNotSupported;
+        const long long grid = std::min<long long>(ntiles, (long long)per_sm * sms);
+        kern<<<(unsigned)grid, blk, smem, st>>>(d, io, nslot, stage_off);
+        return cudaGetLastError();
+    }
+}
+
+// give-ups of this unit's pipelined waits since the last call (cleared)
+template <class T, int E, bool DB> cudaError_t line_pipe_faults_E(unsigned *count)
+{
+    unsigned v = 0, z = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_pipe_wait_fault, sizeof v);
+    if (e == cudaSuccess && v) e = cudaMemcpyToSymbol(g_pipe_wait_fault, &z, sizeof z);
+    *count += v;
+    return e;
+}
+
 template <class K> static cudaError_t line_smem_attr(K kernel, int bytes)
 {
     cudaFuncAttributes fa;
@@ -410,8 +640,11 @@ template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes)
     cudaError_t e = cudaSuccess;
 #define IG_SL(RS_)                                                                                        \
     if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_C2C, DB>, bytes);                     \
-    if constexpr (!std::is_same<T, df>::value)                                                            \
-        if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC, DB>, bytes);
+    if constexpr (!std::is_same<T, df>::value) {                                                          \
+        if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC, DB>, bytes);                \
+        if (e == cudaSuccess) e = line_smem_attr(k_fft_line_pipe<T, E, RS_, LK_C2C, DB>, bytes);            \
+        if (e == cudaSuccess) e = line_smem_attr(k_fft_line_pipe<T, E, RS_, LK_R2HC, DB>, bytes);           \
+    }
     IG_SL(RS_P2)
     IG_SL(RS_ALL)
     if constexpr (E == 8) { IG_SL(RS_P235) }

@@ -5,4 +5,7 @@
 namespace ig {
 template cudaError_t launch_line_E<float, 8, true>(const CoreDesc &, const IODesc &, size_t, cudaStream_t);
 template cudaError_t set_smem_line_E<float, 8, true>(int);
+template cudaError_t launch_line_pipe_E<float, 8, true>(const CoreDesc &, const IODesc &, size_t, int, int,
+                                                         cudaStream_t);
+template cudaError_t line_pipe_faults_E<float, 8, true>(unsigned *);
 }  // namespace ig

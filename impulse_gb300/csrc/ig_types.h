@@ -16,6 +16,7 @@ constexpr int kEMax = 16;  // largest complex-elements-per-thread variant of the
 
 struct StageDesc {
     int R, ns, tw;  // radix, product of previous radices, twiddle offset (cx units)
+    int twp;        // offset into the FP32 pair twiddle table (16-byte entries; ns even)
     FastDiv fns;    // division by ns
 };
 
@@ -64,6 +65,7 @@ struct CoreDesc {
     int nst;
     StageDesc st[kMaxStages];
     const void *tw;     // cx<T> stage twiddles, forward sign
+    const void *twp;    // FP32: the same twiddles for butterfly pairs (k_fft_pair), stages with ns even
     const void *chirp;  // cx<T> exp(+i pi m^2 / M), m < M  (Bluestein)
     const void *chirpf; // cx<T> FFT_L of the padded chirp / L  (Bluestein)
     const void *rtw;    // cx<T> exp(-2 pi i k / (2M)), k <= M  (real split)

@@ -296,6 +296,12 @@ int ig_set_f64_arith(int mode);
 void ig_release_caches(void);
 /* Number of kernel launches the engine issued since the last reset. */
 unsigned long long ig_launch_count(int reset);
+/* Synchronise the current device and report in *count how many waits of the
+ * engine's pipelined kernels gave up since the last call (each wait on a bulk
+ * copy is bounded; a CTA that gives up abandons its remaining lines).  0 in
+ * normal operation; the counters are cleared.  No counterpart in the
+ * reference (CPU code has no device waits). */
+int ig_device_faults(unsigned *count);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -1,0 +1,62 @@
+"""GPU parity of the FP32 paired-lane line kernel (k_fft_pair: two butterflies
+per thread in the lanes of the f32x2 instructions), the default FP32 path for
+complex lines and even real lines (halfcomplex out) of 512 points and more
+whose plan starts with an even radix.  Cases cover both last-stage kinds, the
+real split's pair edges (M divisible by 4 and M = 2 mod 4), the 7/11 radix
+class, line distances longer than the line, output starts that are not
+16-byte aligned (the engine then takes k_fft_line) and a backward complex
+transform; every result is checked against the FP64 oracle at 1e-6 log2 N."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def tol(n):
+    return 1e-6 * max(1.0, np.log2(n))
+
+
+@pytest.mark.parametrize("n", [1024, 1100, 1200, 1232, 1280, 1680, 4096, 6144, 8192, 10000, 16384])
+@pytest.mark.parametrize("dist_pad", [0, 6])
+def test_pair_halfcomplex(engine, oracle_lib, n, dist_pad):
+    import ctypes as C
+    import torch
+    from impulse_gb300 import _lib as L
+    b = 23
+    dist = n + dist_pad
+    rng = np.random.default_rng(n + dist_pad)
+    host = rng.standard_normal((b, dist)).astype(np.float32)
+    x = torch.from_numpy(host).cuda()
+    y = torch.zeros_like(x)
+    plan = engine.ig_make_rfft_plan(n, L.IG_F32)
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    L.check(engine.ig_rfft_exec_device(plan, x.data_ptr(), y.data_ptr(), b, dist, dist, 1, 0.25, s))
+    torch.cuda.synchronize()
+    engine.ig_destroy_rfft_plan(plan)
+    got = y.cpu().numpy()[:, :n].astype(np.float64)
+    want = oracle_lib.rfft_hc(host[:, :n].astype(np.float64), forward=True, fct=0.25)
+    assert oracle_lib.rel_l2(got, want) < tol(n), n
+
+
+@pytest.mark.parametrize("n", [512, 1000, 1024, 2048, 4096, 5040, 8192])
+@pytest.mark.parametrize("fwd", [1, 0])
+@pytest.mark.parametrize("out_off", [0, 1])
+def test_pair_complex(engine, oracle_lib, n, fwd, out_off):
+    import ctypes as C
+    import torch
+    from impulse_gb300 import _lib as L
+    b = 9
+    rng = np.random.default_rng(7 * n + fwd)
+    host = (rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))).astype(np.complex64)
+    x = torch.from_numpy(host).cuda()
+    # out_off = 1: output lines start 8 bytes past a 16-byte boundary
+    ybuf = torch.zeros(b * n + 1, dtype=torch.complex64, device="cuda")
+    y = ybuf[out_off:out_off + b * n]
+    plan = engine.ig_make_cfft_plan(n, L.IG_F32)
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    L.check(engine.ig_cfft_exec_device(plan, x.data_ptr(), y.data_ptr(), b, n, n, fwd, 0.5, s))
+    torch.cuda.synchronize()
+    engine.ig_destroy_cfft_plan(plan)
+    got = y.cpu().numpy().reshape(b, n)
+    want = oracle_lib.cfft(host.astype(np.complex128), bool(fwd), 0.5)
+    assert oracle_lib.rel_l2(got, want) < tol(n), n
