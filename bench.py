@@ -410,7 +410,7 @@ def run_ours(args, rank, world):
         "clocks": clocks,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": f"k_fft_smem, one launch per length ({len(single)} of {len(items64)} lengths)",
+                     "kernel": f"double-float line kernels (k_fft_line halfcomplex, else k_fft_smem), one launch per length ({len(single)} of {len(items64)} lengths)",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s",
                      "workload_achieved": round(workload_achieved, 1),

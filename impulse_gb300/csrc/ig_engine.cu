@@ -693,16 +693,22 @@ static std::shared_ptr<Core> get_core(Arith a, long long M, bool real_tw)
 // by the batch dimensions (rows: consecutive threads walk a line's units)
 // with the plain complex layout or the even real -> halfcomplex one
 static const bool g_line_kernel = getenv("IG_NO_LINE_KERNEL") == nullptr;
+static const bool g_df_line_hc = getenv("IG_NO_DF_LINE_HC") == nullptr;
 static bool line_kernel_ok(Arith a, const CoreDesc &d, const IODesc &io)
 {
     if (!g_line_kernel || (a != A_F32 && a != A_DF) || d.blue != 0 || d.nst < 2 || d.L != d.M) return false;
     if (d.rs == RS_FULL || !line_edge_ok(d.st[0].R) || !line_edge_ok(d.st[d.nst - 1].R)) return false;
     if (io.cols_in || io.cols_out || io.loff_in || io.loff_out || io.pair || io.split_N1) return false;
     if (io.lay == LAY_C2C) return io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C;
-    // halfcomplex lines: FP32 only (double-float ones measured faster on k_fft_smem)
-    if (io.lay == LAY_R2HC)
-        return a == A_F32 && io.post == POST_SPLIT && io.in_kind == IN_C && io.out_kind == OUT_HC &&
-               io.nreal == 2LL * d.M && line_r2hc_last_ok(d.st[d.nst - 1].R);
+    // halfcomplex lines: FP32 with the split fused into the last stage's
+    // mirror butterflies (last radix with line_r2hc_last_ok), double-float
+    // with a split pass after the last stage (IG_NO_DF_LINE_HC=1: k_fft_smem)
+    if (io.lay == LAY_R2HC) {
+        if (io.post != POST_SPLIT || io.in_kind != IN_C || io.out_kind != OUT_HC || io.nreal != 2LL * d.M) return false;
+        // (double-float: double-buffered cores only; the single-buffered
+        // 16-element line variants spill kilobytes a thread)
+        return a == A_F32 ? line_r2hc_last_ok(d.st[d.nst - 1].R) : g_df_line_hc && d.db;
+    }
     return false;
 }
 

@@ -32,6 +32,11 @@ namespace ig {
 
 constexpr int LK_C2C = 0;   // complex units in, complex units out
 constexpr int LK_R2HC = 1;  // real pairs in (as complex units), halfcomplex out
+// the same for double-float: the last stage writes the spectrum Z to the
+// other line buffer and a split pass reads Z[k], Z[M - k] from it (the mirror
+// butterflies of LK_R2HC keep two butterflies live, which cost double-float
+// lines a CTA per SM)
+constexpr int LK_R2HC_S = 2;
 
 // First stage: load, (double-float: range check), convert, radix-R DFT, write
 // the Stockham positions j R + m of buffer `line`.  Returns the line's
@@ -295,7 +300,9 @@ __device__ __forceinline__ void line_last_r2hc(const cx<T> *src, char *obase, lo
 // measured faster with the extra CTA than without the spill)
 template <class T, int E, int RS, int K, bool DB> constexpr int fft_line_regs()
 {
-    if constexpr (std::is_same<T, df>::value) return 128;
+    // double-float 8-element halfcomplex lines: 80 registers, three 256-thread
+    // CTAs per SM like k_fft_smem's
+    if constexpr (std::is_same<T, df>::value) return (K == LK_R2HC_S && E == 8) ? 80 : 128;
     return E == 8 ? 64 : 128;
 }
 
@@ -352,6 +359,32 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, D
     if constexpr (K == LK_C2C) {
         IG_LINE_EDGE_SWITCH(P.st[nst - 1].R,
                             (line_last_c2c<T, E, R_>(src, obase, io.os, P, nst - 1, tpl, t, act, cc, sc, esc)))
+    } else if constexpr (K == LK_R2HC_S) {
+        // last stage into the other buffer (in place when the line has a
+        // single buffer), then the real split from it
+        if constexpr (std::is_same<T, df>::value) sc.e -= 1;
+        else sc.f *= 0.5f;
+        {
+            const int s = nst - 1;
+            if constexpr (DB) {
+                const cx<T> *a = sm + cur;
+                cx<T> *b = sm + (LS - cur);
+                IG_LINE_RADIX_SWITCH(P.st[s].R, (stage_db<T, E, R_>(a, b, 2 * LS, P, s, nl, tpl, g, t)))
+                cur = LS - cur;
+                __syncthreads();
+            } else {
+                IG_LINE_RADIX_SWITCH(P.st[s].R, (stage<T, E, R_>(sm, P, s, nl, tpl, g, t)))
+            }
+        }
+        if (act) {
+            const cx<T> *z = line + cur;
+            const int M = P.L, pad = P.pad;
+            const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
+            for (int k = t; 2 * k <= M; k += tpl) {
+                const cx<T> a = sget(z + sp(k, pad)), b = sget(z + sp(k == 0 ? 0 : M - k, pad));
+                line_split_store<T>(a, b, k, M, rtw, obase, io.os, sc, esc, P);
+            }
+        }
     } else {
         // the split's 1/2 joins the output scale
         if constexpr (std::is_same<T, df>::value) sc.e -= 1;
@@ -377,13 +410,12 @@ template <class T, int E, bool DB, int RS>
 static void launch_line_rs(const CoreDesc &d, const IODesc &io, unsigned grid, unsigned blk, size_t smem,
                            cudaStream_t st)
 {
-    // double-float halfcomplex lines stay on k_fft_smem: the fused split's two
-    // live butterflies cost a CTA per SM (line_kernel_ok)
-    if constexpr (!std::is_same<T, df>::value) {
-        if (io.lay == LAY_R2HC) {
-            k_fft_line<T, E, RS, LK_R2HC, DB><<<grid, blk, smem, st>>>(d, io);
-            return;
-        }
+    // double-float halfcomplex lines split after the last stage (LK_R2HC_S):
+    // the fused mirror butterflies' two live butterflies cost a CTA per SM
+    if (io.lay == LAY_R2HC) {
+        if constexpr (std::is_same<T, df>::value) k_fft_line<T, E, RS, LK_R2HC_S, DB><<<grid, blk, smem, st>>>(d, io);
+        else k_fft_line<T, E, RS, LK_R2HC, DB><<<grid, blk, smem, st>>>(d, io);
+        return;
     }
     k_fft_line<T, E, RS, LK_C2C, DB><<<grid, blk, smem, st>>>(d, io);
 }
@@ -640,6 +672,8 @@ template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes)
     cudaError_t e = cudaSuccess;
 #define IG_SL(RS_)                                                                                        \
     if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_C2C, DB>, bytes);                     \
+    if constexpr (std::is_same<T, df>::value)                                                             \
+        if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC_S, DB>, bytes);              \
     if constexpr (!std::is_same<T, df>::value) {                                                          \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC, DB>, bytes);                \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line_pipe<T, E, RS_, LK_C2C, DB>, bytes);            \
