@@ -1065,6 +1065,129 @@ static void fourstep_passes(const Core &c, const IODesc &io, char *B, IODesc &p1
     p2.keep0_rows = (int)N1;
 }
 
+// Strided-axis FP32 transforms (lines = adjacent columns, elements a row
+// apart) of 2048 points and more as a four-step split M = N1 N2 with the
+// columns as the fastest line index of both passes.  A single-CTA launch of
+// such columns holds only a few whole columns per CTA (four 4096-point FP32
+// columns fill 128 KB: one CTA per SM) and is latency-bound; here each CTA
+// transforms 32 adjacent columns of N1 (then N2) elements, every row segment
+// read or written is a run of adjacent columns, and the scratch B holds
+// element e of column c at e C + c (C = columns of a batch row).  Pass 1:
+// columns of length N1 with the inter-pass twiddle (row index n2 = batch dim
+// 1), into B; pass 2: length N2, written transposed to the output.
+static const bool g_col4 = getenv("IG_NO_COL_FOURSTEP") == nullptr;
+static std::mutex g_colcore_mu;
+static std::map<std::tuple<int, int, long long>, std::shared_ptr<Core>> g_colcores;
+
+static bool col_fourstep_ok(Arith a, const Core &c, const IODesc &io)
+{
+    return g_col4 && a == A_F32 && c.kind == 0 && c.d.blue == 0 && c.M >= 2048 && io.cols_in && io.cols_out &&
+           io.in_kind == IN_C && io.out_kind == OUT_C && io.pre == PRE_NONE && io.post == POST_NONE && !io.pair &&
+           !io.loff_in && !io.loff_out && !io.tw4 && !io.mul && !io.keep0 && !io.split_N1 && !io.real_out &&
+           io.bn[0] >= 32;
+}
+
+// the four-step core of a column transform: N1 the divisor of M nearest its
+// square root with both factors on single-CTA cores (nullptr if none)
+static std::shared_ptr<Core> col_core(Arith a, long long M)
+{
+    const auto key = std::make_tuple(device_id(), (int)a, M);
+    {
+        std::lock_guard<std::mutex> lk(g_colcore_mu);
+        auto it = g_colcores.find(key);
+        if (it != g_colcores.end()) return it->second;
+    }
+    long long best = 0;
+    for (long long d = 2; d * d <= M; ++d) {
+        if (M % d) continue;
+        std::vector<int> r1, r2;
+        if (gpu_factor(d, r1) && gpu_factor(M / d, r2) && fits_smem(a, d, d) && fits_smem(a, M / d, M / d)) best = d;
+    }
+    std::shared_ptr<Core> c;
+    if (best) {
+        TuneCfg cfg;
+        cfg.N1 = best;
+        g_cfg_override = &cfg;
+        g_cfg_override_len = M;
+        g_cfg_override_arith = a;
+        try {
+            c = make_core(a, M, false);
+        } catch (...) {
+            g_cfg_override = nullptr;
+            throw;
+        }
+        g_cfg_override = nullptr;
+        if (c->kind != 1) c.reset();
+    }
+    std::lock_guard<std::mutex> lk(g_colcore_mu);
+    auto it = g_colcores.find(key);
+    if (it != g_colcores.end()) return it->second;
+    g_colcores[key] = c;
+    return c;
+}
+
+static void run_fourstep_cols(const Core &c, const IODesc &io, char *B, cudaStream_t st)
+{
+    const long long N1 = c.N1, N2 = c.N2, M = c.M;
+    const long long ES = 2 * (long long)store_real_bytes(c.a);
+    const long long C = io.bn[0], NB1 = io.bn[1];
+    IODesc p1 = io;
+    p1.nlines = C * N2 * NB1;
+    p1.bn[0] = C;
+    p1.bsi[0] = io.bsi[0];
+    p1.bn[1] = N2;
+    p1.bsi[1] = io.is;
+    p1.bn[2] = NB1;
+    p1.bsi[2] = io.bsi[1];
+    p1.is = N2 * io.is;
+    p1.cnt_in = p1.cnt_out = (int)N1;
+    p1.out = B;
+    p1.out_kind = OUT_C;
+    p1.os = N2 * C * ES;
+    p1.bso[0] = ES;
+    p1.bso[1] = C * ES;
+    p1.bso[2] = M * C * ES;
+    p1.pre = PRE_NONE;
+    p1.post = POST_NONE;
+    p1.conj_out = 0;
+    p1.real_out = 0;
+    p1.mul = nullptr;
+    p1.keep0 = nullptr;
+    p1.fct = 1.0;
+    p1.tw4 = 1;
+    p1.tw4_dim1 = 1;
+    p1.tw4N = M;
+    p1.tw4S = N2;
+    p1.fdS = make_fdiv((unsigned)N2);
+    p1.tw4hi = c.whi;
+    p1.tw4lo = c.wlo;
+    p1.tw4tab = c.tw4tab;
+    p1.cols_in = p1.cols_out = 1;
+    IODesc p2 = io;
+    p2.in = B;
+    p2.in_kind = IN_C;
+    p2.conj_in = 0;
+    p2.pre = PRE_NONE;
+    p2.is = C * ES;
+    p2.nlines = C * N1 * NB1;
+    p2.bn[0] = C;
+    p2.bsi[0] = ES;
+    p2.bn[1] = N1;
+    p2.bsi[1] = N2 * C * ES;
+    p2.bn[2] = NB1;
+    p2.bsi[2] = M * C * ES;
+    p2.os = N1 * io.os;
+    p2.bso[0] = io.bso[0];
+    p2.bso[1] = io.os;
+    p2.bso[2] = io.bso[1];
+    p2.cnt_in = p2.cnt_out = (int)N2;
+    p2.tw4 = 0;
+    p2.tw4_dim1 = 0;
+    p2.cols_in = p2.cols_out = 1;
+    launch_smem(c.a, c.c1->d, p1, st);
+    launch_smem(c.a, c.c2->d, p2, st);
+}
+
 // Forward real halfcomplex transform over a four-step core of length M = N1 N2
 // (N = 2M reals): column pass into scratch B, then a row pass whose CTAs hold
 // each row r next to its mirror N1 - r and write X[k], X[M - k] directly.
@@ -1514,6 +1637,23 @@ static void exec_op(Arith a, Op op, long long N, const Lines &ln, int forward, d
     long long ue_out = (io.out_kind == OUT_C || io.out_kind == OUT_P) ? 2 * sr : sr;
     io.cols_in = (ln.bn[0] > 1 && std::llabs(ln.bsi[0]) <= ue_in && std::llabs(io.is) > ue_in) ? 1 : 0;
     io.cols_out = (ln.bn[0] > 1 && std::llabs(ln.bso[0]) <= ue_out && std::llabs(io.os) > ue_out) ? 1 : 0;
+    if (!forced && col_fourstep_ok(a, *core, io)) {
+        auto c4 = col_core(a, core->M);
+        if (c4) {
+            const long long ES = 2 * (long long)store_real_bytes(a);
+            for (long long i2 = 0; i2 < io.bn[2]; ++i2) {
+                IODesc q = io;
+                q.in += i2 * io.bsi[2];
+                q.out += i2 * io.bso[2];
+                q.bn[2] = 1;
+                q.bsi[2] = q.bso[2] = 0;
+                q.nlines = q.bn[0] * q.bn[1];
+                char *B = (char *)scratch_for(st).get(1, (size_t)(q.nlines * c4->M * ES));
+                run_fourstep_cols(*c4, q, B, st);
+            }
+            return;
+        }
+    }
     run_complex(*core, io, st);
 }
 

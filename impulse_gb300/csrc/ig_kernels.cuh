@@ -96,6 +96,12 @@ __device__ __forceinline__ int line_i0(const IODesc &io, long long l)
     const unsigned lu = (unsigned)l;
     return (int)(lu - fdiv(lu, io.fb0) * (unsigned)io.bn[0]);
 }
+// index of line l along batch dim 1
+__device__ __forceinline__ int line_i1(const IODesc &io, long long l)
+{
+    const unsigned q0 = fdiv((unsigned)l, io.fb0);
+    return (int)(q0 - fdiv(q0, io.fb1) * (unsigned)io.bn[1]);
+}
 
 __device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
 
@@ -925,7 +931,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const cx<T> *line = sm + (size_t)g2 * LSt + cur;
             const int i0l = (io.tw4 || io.mul || io.keep0 || paired) ? line_i0(io, l) : 0;
             const bool has_b = paired && (2LL * i0l + 1 < io.pair_n0);
-            const int n2 = io.tw4 ? i0l : 0;
+            const int n2 = io.tw4 ? (io.tw4_dim1 ? line_i1(io, l) : i0l) : 0;
             const int ml = io.mul ? (int)(i0l * io.mul_a) : 0;
             const cx<T> *whi = reinterpret_cast<const cx<T> *>(io.tw4hi);
             const cx<T> *wlo = reinterpret_cast<const cx<T> *>(io.tw4lo);

@@ -105,6 +105,7 @@ struct IODesc {
     // four-step inter-pass twiddle on output unit u of line l:
     // t = ((l % bn0) * u) mod tw4N, value w_hi[t / tw4S] * w_lo[t % tw4S]
     int tw4;
+    int tw4_dim1;           // the twiddle's row index is batch dim 1 ((l / bn0) % bn1), not dim 0
     long long tw4N, tw4S;
     FastDiv fdS;            // division by tw4S
     const void *tw4hi, *tw4lo;
