@@ -1043,6 +1043,9 @@ template <class T, int E, int RS, bool DB> constexpr int fft_smem_regs()
 {
     if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS >= RS_FULL ? 96 : 80;
     if constexpr (DB && E == 8 && std::is_same<T, float>::value) return 80;
+    // FP32 16-element double-buffered lines (4097-8192 points) fit 64 registers
+    // without spills below the full class: two 512-thread CTAs per SM
+    if constexpr (DB && E == 16 && std::is_same<T, float>::value) return RS >= RS_FULL ? 128 : 64;
     return 128;
 }
 

@@ -303,7 +303,7 @@ template <class T, int E, int RS, int K, bool DB> constexpr int fft_line_regs()
     // double-float 8-element halfcomplex lines: 80 registers, three 256-thread
     // CTAs per SM like k_fft_smem's
     if constexpr (std::is_same<T, df>::value) return (K == LK_R2HC_S && E == 8) ? 80 : 128;
-    return E == 8 ? 64 : 128;
+    return (E == 8 || DB) ? 64 : 128;
 }
 
 // One CTA: `lpc` lines of `tpl` threads; shared memory lpc * LSt complex slots
