@@ -242,7 +242,7 @@ static bool fits_smem(Arith a, long long L, long long M)
     long long tpl = (L + kEMax - 1) / kEMax;
     if (tpl > kMaxThreads) return false;
     long long slots = smem_slots(L, M);
-    slots += slots >> 3;  // worst-case padding
+    slots += (slots >> 3) + 1;  // worst-case padding, and the odd per-line stride
     return slots * (long long)slot_bytes(a) <= (long long)max_smem();
 }
 
@@ -778,7 +778,8 @@ static long long smem_lpc(Arith a, const CoreDesc &d, const IODesc &io, long lon
 {
     const long long tpl = (d.L + d.E - 1) / d.E;
     // double-buffered stages: two line buffers
-    line_bytes = (long long)d.LS * (long long)slot_bytes(a) * (d.db ? 2 : 1);
+    // (k_fft_smem's per-line stride is odd in slots: 2 LS + 1, or LS rounded up to odd)
+    line_bytes = (long long)(d.db ? 2LL * d.LS + 1 : (long long)(d.LS | 1)) * (long long)slot_bytes(a);
     const int smax = max_smem();
     long long lpc = std::max<long long>(1, 256 / tpl);
     if (io.cols_in || io.cols_out) lpc = std::max<long long>(lpc, 8);

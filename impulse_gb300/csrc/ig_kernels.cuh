@@ -196,7 +196,7 @@ __device__ __forceinline__ cx<T> tw_apply(cx<T> z, const typename Bfly<T>::W *w,
 // DFT and writes y[(j / ns) ns R + k + m ns].  All reads of a stage precede
 // the barrier and all writes follow it.
 template <class T, int E, int R>
-__device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int nl, int tpl, int g, int t)
+__device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int nl, int tpl, int g, int t, int LSl)
 {
     using B = Bfly<T>;
     using V = typename B::V;
@@ -204,7 +204,7 @@ __device__ __forceinline__ void stage(cx<T> *sm, const CoreDesc &P, int si, int 
     const int nr = P.L / R, ns = P.st[si].ns, pad = P.pad;
     const FastDiv fns = P.st[si].fns;
     const typename B::W *tw = reinterpret_cast<const typename B::W *>(P.tw) + P.st[si].tw;
-    cx<T> *line = sm + (size_t)g * P.LS;
+    cx<T> *line = sm + (size_t)g * LSl;
     V v[NB][R];
     int jj[NB];
 #pragma unroll
@@ -311,20 +311,20 @@ template <int E, int RS> __host__ __device__ constexpr bool rs_has(int R)
 // (IFFT(x) = conj(FFT(conj(x)))), with the conjugations folded into the
 // prologue, the epilogue and the Bluestein steps.
 template <class T, int E, int RS>
-__device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl, int tpl, int g, int t)
+__device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl, int tpl, int g, int t, int LSl)
 {
     for (int s = 0; s < P.nst; ++s) {
         switch (P.st[s].R) {
-        case 2: stage<T, E, 2>(sm, P, s, nl, tpl, g, t); break;
-        case 4: stage<T, E, 4>(sm, P, s, nl, tpl, g, t); break;
-        case 8: stage<T, E, 8>(sm, P, s, nl, tpl, g, t); break;
-        case 16: if constexpr (rs_has<E, RS>(16)) stage<T, E, 16>(sm, P, s, nl, tpl, g, t); break;
-        case 3: if constexpr (rs_has<E, RS>(3)) stage<T, E, 3>(sm, P, s, nl, tpl, g, t); break;
-        case 5: if constexpr (rs_has<E, RS>(5)) stage<T, E, 5>(sm, P, s, nl, tpl, g, t); break;
-        case 9: if constexpr (rs_has<E, RS>(9)) stage<T, E, 9>(sm, P, s, nl, tpl, g, t); break;
-        case 7: if constexpr (rs_has<E, RS>(7)) stage<T, E, 7>(sm, P, s, nl, tpl, g, t); break;
-        case 11: if constexpr (rs_has<E, RS>(11)) stage<T, E, 11>(sm, P, s, nl, tpl, g, t); break;
-        case 13: if constexpr (rs_has<E, RS>(13)) stage<T, E, 13>(sm, P, s, nl, tpl, g, t); break;
+        case 2: stage<T, E, 2>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 4: stage<T, E, 4>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 8: stage<T, E, 8>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 16: if constexpr (rs_has<E, RS>(16)) stage<T, E, 16>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 3: if constexpr (rs_has<E, RS>(3)) stage<T, E, 3>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 5: if constexpr (rs_has<E, RS>(5)) stage<T, E, 5>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 9: if constexpr (rs_has<E, RS>(9)) stage<T, E, 9>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 7: if constexpr (rs_has<E, RS>(7)) stage<T, E, 7>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 11: if constexpr (rs_has<E, RS>(11)) stage<T, E, 11>(sm, P, s, nl, tpl, g, t, LSl); break;
+        case 13: if constexpr (rs_has<E, RS>(13)) stage<T, E, 13>(sm, P, s, nl, tpl, g, t, LSl); break;
         default: break;
         }
     }
@@ -333,9 +333,10 @@ __device__ __forceinline__ void run_stages(cx<T> *sm, const CoreDesc &P, int nl,
 // double-buffered core: buffers A = sm, B = sm + LS (line stride LS2 = 2 LS);
 // returns the offset (0 or LS) of the buffer that holds the result
 template <class T, int E, int RS>
-__device__ __forceinline__ int run_stages_db(cx<T> *sm, int cur, const CoreDesc &P, int nl, int tpl, int g, int t)
+__device__ __forceinline__ int run_stages_db(cx<T> *sm, int cur, const CoreDesc &P, int nl, int tpl, int g, int t,
+                                             int LS2)
 {
-    const int LS = P.LS, LS2 = 2 * P.LS;
+    const int LS = P.LS;
     for (int s = 0; s < P.nst; ++s) {
         const cx<T> *src = sm + cur;
         cx<T> *dst = sm + (LS - cur);
@@ -498,7 +499,10 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     __shared__ int s_rescale;
 
     // DB: double-buffered stages (2 LS slots per line)
-    const int LSt = DB ? 2 * P.LS : P.LS;
+    // per-line stride of the CTA's line buffers: odd (in slots), so that the
+    // column-mapped prologue and epilogue (consecutive threads on consecutive
+    // lines) hit distinct banks
+    const int LSt = DB ? 2 * P.LS + 1 : (P.LS | 1);
     const int lpc = io.lpc, tpl = io.tpl, pad = P.pad;
     const long long line0 = blk * lpc;
     const int nl = (int)min((long long)lpc, io.nlines - line0);
@@ -761,10 +765,10 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             }
             if (P.blue) __syncthreads();
             if constexpr (DB) {
-                cur = run_stages_db<T, E, RS>(sm, cur, P, nl, tpl, g, t);
+                cur = run_stages_db<T, E, RS>(sm, cur, P, nl, tpl, g, t, LSt);
                 myline = line_a + cur;
             } else {
-                run_stages<T, E, RS>(sm, P, nl, tpl, g, t);
+                run_stages<T, E, RS>(sm, P, nl, tpl, g, t, LSt);
             }
         }
         if (blue) {

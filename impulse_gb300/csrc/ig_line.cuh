@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, D
             cur = LS - cur;
             __syncthreads();
         } else {
-            IG_LINE_RADIX_SWITCH(P.st[s].R, (stage<T, E, R_>(sm, P, s, nl, tpl, g, t)))
+            IG_LINE_RADIX_SWITCH(P.st[s].R, (stage<T, E, R_>(sm, P, s, nl, tpl, g, t, LS)))
         }
     }
     OutScale<T> sc;
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, D
                 cur = LS - cur;
                 __syncthreads();
             } else {
-                IG_LINE_RADIX_SWITCH(P.st[s].R, (stage<T, E, R_>(sm, P, s, nl, tpl, g, t)))
+                IG_LINE_RADIX_SWITCH(P.st[s].R, (stage<T, E, R_>(sm, P, s, nl, tpl, g, t, LS)))
             }
         }
         if (act) {
@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_line_pipe_regs<T, E, RS,
                 cur = LS - cur;
                 __syncthreads();
             } else {
-                IG_LINE_RADIX_SWITCH(P.st[si].R, (stage<T, E, R_>(sm, P, si, nl, tpl, g, t)))
+                IG_LINE_RADIX_SWITCH(P.st[si].R, (stage<T, E, R_>(sm, P, si, nl, tpl, g, t, LS)))
             }
         }
         OutScale<T> sc;
