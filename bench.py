@@ -726,6 +726,7 @@ PROFILE_CASES = {
     "c2c4096x4096_f32_axes01": ("n", "f32", 4096, 4096),
     "rfft1009_f64": ("r", "f64", 1009, 16628),
     "rfft65521_f64": ("r", "f64", 65521, 256),
+    "rfft65521_f32": ("r", "f32", 65521, 512),
     "rfft8191_f64": ("r", "f64", 8191, 2048),
     # every 10th transform of the uneven-length workload (FP32, work-list graph)
     "uneven_tenth_f32": ("u", "f32", 0, 10),
