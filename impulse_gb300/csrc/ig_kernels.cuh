@@ -970,6 +970,47 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 }
                 return;
             }
+            if constexpr (LAY == LAY_TW) {
+                // complex units out (the layout class guarantees it), with the
+                // four-step twiddle and / or the pointwise table product; the
+                // output pointer and the table rows advance by one add per unit
+                const int cnt = io.cnt_out;
+                const long long os = io.os, pstep = (long long)tpl * os;
+                const auto *wrow = io.tw4 && io.tw4tab
+                                       ? reinterpret_cast<const typename Bfly<T>::W *>(io.tw4tab) + (size_t)n2 * cnt
+                                       : nullptr;
+                const cx<T> *mrow = io.mul ? mt + ml : nullptr;
+                const long long mb = io.mul_b;
+                char *p = base + (long long)t2 * os;
+                for (int u = t2; u < cnt; u += tpl, p += pstep) {
+                    cx<T> z = sget(line + sp(u, pad));
+                    if (cc) z.i = -z.i;
+                    if (wrow) {
+                        z = tw_apply<T>(z, wrow + u, io.fwd, P);
+                    } else if (io.tw4) {
+                        const unsigned tt = (unsigned)n2 * (unsigned)u;
+                        const unsigned hi = fdiv(tt, io.fdS), lo = tt - hi * (unsigned)io.tw4S;
+                        const cx<T> w = cmul(whi[hi], wlo[lo]);
+                        z = io.fwd ? cmul(z, w) : cmulc(z, w);
+                    }
+                    if (io.keep0 && u == 0 && (io.keep0_rows == 1 || i0l == 0)) {
+                        S2 o;
+                        o.x = sc.apply(z.r, esc);
+                        o.y = sc.apply(z.i, esc);
+                        reinterpret_cast<S2 *>(io.keep0)[io.keep0_rows == 1 ? l : (long long)fdiv((unsigned)l, io.fb0)] =
+                            o;
+                    }
+                    if (mrow) {
+                        const cx<T> w = mrow[(long long)u * mb];
+                        z = io.mul_conj ? cmulc(z, w) : cmul(z, w);
+                    }
+                    S2 o;
+                    o.x = sc.apply(z.r, esc);
+                    o.y = sc.apply(z.i, esc);
+                    stg_s<S2>(p, o);
+                }
+                return;
+            }
             if constexpr (LAY == LAY_PR2HC) {
                 const int cnt = io.cnt_out;
                 const long long os = io.os, nreal = io.nreal, po = io.pair_out;
