@@ -291,6 +291,11 @@ static int choose_layout(Arith a, const IODesc &io)
     if (io.tw4 || io.mul)
         return (plain && !io.pair && io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C) ? LAY_TW
                                                                                                           : LAY_GEN;
+    // r2c's last axis: contiguous reals, real split, half spectrum with real DC
+    // and Nyquist bins (conjugated for a backward r2c)
+    if (a != A_F64 && !io.pair && io.in_kind == IN_C && io.out_kind == OUT_C && io.post == POST_SPLIT && io.real_out &&
+        !io.conj_in && io.pre == PRE_NONE && !io.keep0 && !io.mul && !io.tw4)
+        return LAY_R2C;
     if (!plain) return LAY_GEN;
     if (!io.pair && io.in_kind == IN_C && io.out_kind == OUT_C && io.post == POST_NONE) return LAY_C2C;
     // the fused four-step split reads complex rows and has its own epilogue
@@ -700,6 +705,9 @@ static bool line_kernel_ok(Arith a, const CoreDesc &d, const IODesc &io)
     if (d.rs == RS_FULL || !line_edge_ok(d.st[0].R) || !line_edge_ok(d.st[d.nst - 1].R)) return false;
     if (io.cols_in || io.cols_out || io.loff_in || io.loff_out || io.pair || io.split_N1) return false;
     if (io.lay == LAY_C2C) return io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C;
+    // r2c half spectra (FP32): the halfcomplex butterflies storing complex units
+    if (io.lay == LAY_R2C)
+        return a == A_F32 && io.nreal == 2LL * d.M && line_r2hc_last_ok(d.st[d.nst - 1].R);
     // halfcomplex lines: FP32 with the split fused into the last stage's
     // mirror butterflies (last radix with line_r2hc_last_ok), double-float
     // with a split pass after the last stage (IG_NO_DF_LINE_HC=1: k_fft_smem)
@@ -732,7 +740,7 @@ static int pipe_slots_env()
 static const int g_pipe_slots = pipe_slots_env();
 static bool pipe_ok(Arith a, const CoreDesc &d, const IODesc &io)
 {
-    if (!g_pipe_kernel || a != A_F32 || io.is != 8) return false;
+    if (!g_pipe_kernel || a != A_F32 || io.is != 8 || (io.lay != LAY_C2C && io.lay != LAY_R2HC)) return false;
     const long long line_bytes = (long long)d.L * 8;
     if (line_bytes % 16 || ((uintptr_t)io.in & 15)) return false;
     for (int k = 0; k < 3; ++k)
@@ -754,6 +762,7 @@ static int sm_count()
 static const bool g_pair_kernel = getenv("IG_NO_PAIR") == nullptr;
 static bool pair_ok(Arith a, const CoreDesc &d, const IODesc &io)
 {
+    if (io.lay != LAY_C2C && io.lay != LAY_R2HC) return false;
     // below 512 points k_fft_line measured faster (a line's 16-element
     // threads are too few: N = 96 real 1966 vs 1679 GB/s, 256 3070 vs 2675);
     // from 512 on the pairs win (1200 real 1927 -> 2178, 1280 2145 -> 2421,

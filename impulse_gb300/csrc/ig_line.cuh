@@ -37,6 +37,11 @@ constexpr int LK_R2HC = 1;  // real pairs in (as complex units), halfcomplex out
 // butterflies of LK_R2HC keep two butterflies live, which cost double-float
 // lines a CTA per SM)
 constexpr int LK_R2HC_S = 2;
+// real pairs in, half spectrum out as complex units (pocketfft::r2c's last
+// axis, general_r2c, pocketfft_hdronly.h:3125): the LK_R2HC butterflies with
+// X[k] stored as unit k (DC and Nyquist imaginary parts 0, conjugated for
+// a backward r2c)
+constexpr int LK_R2C = 3;
 
 // First stage: load, (double-float: range check), convert, radix-R DFT, write
 // the Stockham positions j R + m of buffer `line`.  Returns the line's
@@ -161,10 +166,12 @@ __device__ __forceinline__ void line_last_c2c(const cx<T> *src, char *obase, lon
 }
 
 // real split of the partner bins a = Z[k], b = Z[M - k] and the halfcomplex
-// stores of X[k] and X[M - k]; sc carries fct / 2
-template <class T>
+// stores of X[k] and X[M - k] (HS: as complex units k and M - k of a half
+// spectrum, imaginary parts negated when cjo); sc carries fct / 2
+template <class T, bool HS = false>
 __device__ __forceinline__ void line_split_store(cx<T> a, cx<T> b, int k, int M, const cx<T> *rtw, char *obase,
-                                                 long long os, const OutScale<T> &sc, int esc, const CoreDesc &P)
+                                                 long long os, const OutScale<T> &sc, int esc, const CoreDesc &P,
+                                                 bool cjo = false)
 {
     using S = typename Traits<T>::S;
     cx<T> X, Y;  // X[k], X[M - k]
@@ -184,6 +191,20 @@ __device__ __forceinline__ void line_split_store(cx<T> a, cx<T> b, int k, int M,
         Y = cx<T>{Z.r, -Z.i};
     }
     const int k2 = M - k;
+    if constexpr (HS) {
+        using S2 = typename Traits<T>::S2;
+        const S zero = S(0);
+        S2 o;
+        o.x = sc.apply(X.r, esc);
+        o.y = k == 0 ? zero : sc.apply(cjo ? -X.i : X.i, esc);
+        stg_s<S2>(obase + (long long)k * os, o);
+        if (k2 != k) {
+            o.x = sc.apply(Y.r, esc);
+            o.y = k2 == M ? zero : sc.apply(cjo ? -Y.i : Y.i, esc);
+            stg_s<S2>(obase + (long long)k2 * os, o);
+        }
+        return;
+    }
     if (k == 0) {
         stg_s<S>(obase, sc.apply(X.r, esc));
     } else {
@@ -207,9 +228,10 @@ __device__ __forceinline__ void line_split_store(cx<T> a, cx<T> b, int k, int M,
 // Z[p + m nr], whose partner Z[M - p - m nr] is output R - 1 - m of butterfly
 // nr - p (for p = 0: output R - m of butterfly 0; for 2p = nr: output
 // R - 1 - m of butterfly p itself).
-template <class T, int E, int R>
+template <class T, int E, int R, bool HS = false>
 __device__ __forceinline__ void line_last_r2hc(const cx<T> *src, char *obase, long long os, const CoreDesc &P,
-                                               int si, int tpl, int t, bool act, const OutScale<T> &sc, int esc)
+                                               int si, int tpl, int t, bool act, const OutScale<T> &sc, int esc,
+                                               bool cjo = false)
 {
     using B = Bfly<T>;
     using V = typename B::V;
@@ -242,15 +264,15 @@ __device__ __forceinline__ void line_last_r2hc(const cx<T> *src, char *obase, lo
             B::template dft<R>(vb);
 #pragma unroll
             for (int m = 0; m < R; ++m)
-                line_split_store<T>(line_val<T>(va[m]), line_val<T>(vb[R - 1 - m]), p + m * nr, M, rtw, obase, os, sc,
-                                    esc, P);
+                line_split_store<T, HS>(line_val<T>(va[m]), line_val<T>(vb[R - 1 - m]), p + m * nr, M, rtw, obase, os, sc,
+                                    esc, P, cjo);
         } else if (p == 0) {
             // k = m nr, partner (R - m) nr (m = 0: k = 0 with itself)
 #pragma unroll
             for (int m = 0; m < R; ++m) {
                 const int mp = m == 0 ? 0 : R - m;
                 if (m <= mp)
-                    line_split_store<T>(line_val<T>(va[m]), line_val<T>(va[mp]), m * nr, M, rtw, obase, os, sc, esc, P);
+                    line_split_store<T, HS>(line_val<T>(va[m]), line_val<T>(va[mp]), m * nr, M, rtw, obase, os, sc, esc, P, cjo);
             }
         } else {
             // 2 p = nr: k = p + m nr, partner p + (R - 1 - m) nr
@@ -258,8 +280,8 @@ __device__ __forceinline__ void line_last_r2hc(const cx<T> *src, char *obase, lo
             for (int m = 0; m < R; ++m) {
                 const int mp = R - 1 - m;
                 if (m <= mp)
-                    line_split_store<T>(line_val<T>(va[m]), line_val<T>(va[mp]), p + m * nr, M, rtw, obase, os, sc,
-                                        esc, P);
+                    line_split_store<T, HS>(line_val<T>(va[m]), line_val<T>(va[mp]), p + m * nr, M, rtw, obase, os, sc,
+                                        esc, P, cjo);
             }
         }
         asm volatile("" ::: "memory");
@@ -389,15 +411,19 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, D
         // the split's 1/2 joins the output scale
         if constexpr (std::is_same<T, df>::value) sc.e -= 1;
         else sc.f *= 0.5f;
+        constexpr bool HS = K == LK_R2C;
+        const bool cjo = HS && io.conj_out;
         switch (P.st[nst - 1].R) {
-        case 2: line_last_r2hc<T, E, 2>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc); break;
-        case 4: line_last_r2hc<T, E, 4>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc); break;
-        case 8: line_last_r2hc<T, E, 8>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc); break;
+        case 2: line_last_r2hc<T, E, 2, HS>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc, cjo); break;
+        case 4: line_last_r2hc<T, E, 4, HS>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc, cjo); break;
+        case 8: line_last_r2hc<T, E, 8, HS>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc, cjo); break;
         case 3:
-            if constexpr (rs_has<E, RS>(3)) line_last_r2hc<T, E, 3>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc);
+            if constexpr (rs_has<E, RS>(3))
+                line_last_r2hc<T, E, 3, HS>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc, cjo);
             break;
         case 5:
-            if constexpr (rs_has<E, RS>(5)) line_last_r2hc<T, E, 5>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc);
+            if constexpr (rs_has<E, RS>(5))
+                line_last_r2hc<T, E, 5, HS>(src, obase, io.os, P, nst - 1, tpl, t, act, sc, esc, cjo);
             break;
         default: break;  // other last radices are not sent here (line_r2hc_last_ok)
         }
@@ -416,6 +442,12 @@ static void launch_line_rs(const CoreDesc &d, const IODesc &io, unsigned grid, u
         if constexpr (std::is_same<T, df>::value) k_fft_line<T, E, RS, LK_R2HC_S, DB><<<grid, blk, smem, st>>>(d, io);
         else k_fft_line<T, E, RS, LK_R2HC, DB><<<grid, blk, smem, st>>>(d, io);
         return;
+    }
+    if constexpr (!std::is_same<T, df>::value) {
+        if (io.lay == LAY_R2C) {
+            k_fft_line<T, E, RS, LK_R2C, DB><<<grid, blk, smem, st>>>(d, io);
+            return;
+        }
     }
     k_fft_line<T, E, RS, LK_C2C, DB><<<grid, blk, smem, st>>>(d, io);
 }
@@ -676,6 +708,7 @@ template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes)
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC_S, DB>, bytes);              \
     if constexpr (!std::is_same<T, df>::value) {                                                          \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC, DB>, bytes);                \
+        if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2C, DB>, bytes);                 \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line_pipe<T, E, RS_, LK_C2C, DB>, bytes);            \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line_pipe<T, E, RS_, LK_R2HC, DB>, bytes);           \
     }

@@ -60,3 +60,21 @@ def test_pair_complex(engine, oracle_lib, n, fwd, out_off):
     got = y.cpu().numpy().reshape(b, n)
     want = oracle_lib.cfft(host.astype(np.complex128), bool(fwd), 0.5)
     assert oracle_lib.rel_l2(got, want) < tol(n), n
+
+
+@pytest.mark.parametrize("shape,axes", [((33, 4096), [1]), ((7, 1000), [1]), ((5, 96), [1]), ((3, 6144), [1]),
+                                        ((4, 5, 2048), [2]), ((64, 512), [0, 1]), ((2, 40, 256), [1, 2])])
+@pytest.mark.parametrize("fwd", [True, False])
+def test_r2c_half_spectrum_f32(engine, oracle_lib, shape, axes, fwd):
+    """pocketfft::r2c FP32 with an even contiguous last axis: the line kernel's
+    half-spectrum split (DC and Nyquist imaginary parts 0, conjugated for a
+    backward transform)."""
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(sum(shape) + fwd)
+    x = rng.standard_normal(shape).astype(np.float32)
+    got = F.r2c(x, axes, forward=fwd, fct=0.5)
+    want = oracle_lib.r2c(x.astype(np.float64), axes, forward=fwd, fct=0.5)
+    assert oracle_lib.rel_l2(got, want) < tol(max(shape)) * 2, (shape, axes, fwd)
+    last = got.reshape(-1, got.shape[-1]) if axes[-1] == len(shape) - 1 else None
+    if last is not None and len(axes) == 1:
+        assert np.all(last[:, 0].imag == 0) and np.all(last[:, -1].imag == 0)
