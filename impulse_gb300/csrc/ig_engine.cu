@@ -296,6 +296,10 @@ static int choose_layout(Arith a, const IODesc &io)
     if (a != A_F64 && !io.pair && io.in_kind == IN_C && io.out_kind == OUT_C && io.post == POST_SPLIT && io.real_out &&
         !io.conj_in && io.pre == PRE_NONE && !io.keep0 && !io.mul && !io.tw4)
         return LAY_R2C;
+    // c2r's last axis: half spectrum in (Hermitian pre-step), real pairs out
+    if (a != A_F64 && !io.pair && io.in_kind == IN_C && io.out_kind == OUT_C && io.pre == PRE_HERM_EVEN &&
+        io.post == POST_NONE && !io.conj_out && !io.real_out && !io.keep0 && !io.mul && !io.tw4)
+        return LAY_C2R;
     if (!plain) return LAY_GEN;
     if (!io.pair && io.in_kind == IN_C && io.out_kind == OUT_C && io.post == POST_NONE) return LAY_C2C;
     // the fused four-step split reads complex rows and has its own epilogue
@@ -708,6 +712,8 @@ static bool line_kernel_ok(Arith a, const CoreDesc &d, const IODesc &io)
     // r2c half spectra (FP32): the halfcomplex butterflies storing complex units
     if (io.lay == LAY_R2C)
         return a == A_F32 && io.nreal == 2LL * d.M && line_r2hc_last_ok(d.st[d.nst - 1].R);
+    // c2r half spectra (FP32): the pre-step from HBM, every stage from shared memory
+    if (io.lay == LAY_C2R) return a == A_F32 && d.rtw && io.cnt_in == d.M + 1 && io.cnt_out == d.M;
     // halfcomplex lines: FP32 with the split fused into the last stage's
     // mirror butterflies (last radix with line_r2hc_last_ok), double-float
     // with a split pass after the last stage (IG_NO_DF_LINE_HC=1: k_fft_smem)
@@ -791,8 +797,10 @@ static long long smem_lpc(Arith a, const CoreDesc &d, const IODesc &io, long lon
     line_bytes = (long long)(d.db ? 2LL * d.LS + 1 : (long long)(d.LS | 1)) * (long long)slot_bytes(a);
     const int smax = max_smem();
     long long lpc = std::max<long long>(1, 256 / tpl);
-    if (io.cols_in || io.cols_out) lpc = std::max<long long>(lpc, 8);
     if (d.lpc_pref > 0) lpc = d.lpc_pref;
+    // column-mapped launches need several lines per CTA for coalescing, whatever
+    // the tuner chose for the core's contiguous lines
+    if (io.cols_in || io.cols_out) lpc = std::max<long long>(lpc, 8);
     lpc = std::min<long long>(lpc, kMaxLinesPerCta);
     lpc = std::min<long long>(lpc, std::max<long long>(1, kMaxThreads / tpl));
     // keep three (or two) CTAs per SM when a line is small enough: a third

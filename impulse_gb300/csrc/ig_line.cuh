@@ -42,6 +42,47 @@ constexpr int LK_R2HC_S = 2;
 // X[k] stored as unit k (DC and Nyquist imaginary parts 0, conjugated for
 // a backward r2c)
 constexpr int LK_R2C = 3;
+// half spectrum in (complex units X[0..M]), real pairs out (pocketfft::c2r's
+// last axis, general_c2r, pocketfft_hdronly.h:3180): the Hermitian pre-step
+// reads X[k] and X[M - k] straight from HBM and writes Z[k], Z[M - k] to the
+// line buffer, every stage then runs from shared memory and the last one
+// writes the real pairs to HBM
+constexpr int LK_C2R = 4;
+
+// c2r pre-step from HBM into `line`: Z[k] = (X[k] + conj X[M-k]) + i w^-k
+// (X[k] - conj X[M-k]) for the slot pairs (k, M - k) a thread owns (the DC
+// and Nyquist bins' imaginary parts read as 0, the input conjugated when
+// cin, the backward core's conjugation folded in when cc)
+template <class T>
+__device__ __forceinline__ void line_herm_pre(cx<T> *line, const char *base, long long is, const CoreDesc &P, int tpl,
+                                              int t, bool act, bool cin, bool cc)
+{
+    using S2 = typename Traits<T>::S2;
+    const int M = P.L, pad = P.pad;
+    const cx<T> *rtw = reinterpret_cast<const cx<T> *>(P.rtw);
+    if (!act) return;
+    for (int k = t; 2 * k <= M; k += tpl) {
+        const int k2 = M - k;
+        const S2 ra = ldg_s<S2>(base + (long long)k * is), rb = ldg_s<S2>(base + (long long)k2 * is);
+        cx<T> a{ra.x, cin ? -ra.y : ra.y}, b{rb.x, cin ? -rb.y : rb.y};
+        if (k == 0) {
+            a.i = T(0);
+            b.i = T(0);
+        }
+        {
+            const cx<T> xb = conjx(b), A = a + xb, Bv = a - xb;
+            const cx<T> tB = cmulc(Bv, rtw[k]);
+            const cx<T> z{A.r - tB.i, A.i + tB.r};
+            sput(line + sp(k, pad), cc ? conjx(z) : z);
+        }
+        if (k > 0 && k2 != k) {
+            const cx<T> xb = conjx(a), A = b + xb, Bv = b - xb;
+            const cx<T> tB = cmulc(Bv, rtw[k2]);
+            const cx<T> z{A.r - tB.i, A.i + tB.r};
+            sput(line + sp(k2, pad), cc ? conjx(z) : z);
+        }
+    }
+}
 
 // First stage: load, (double-float: range check), convert, radix-R DFT, write
 // the Stockham positions j R + m of buffer `line`.  Returns the line's
@@ -349,7 +390,8 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, D
     const int nl = (int)min((long long)lpc, io.nlines - line0);
     const int g = threadIdx.x / tpl, t = threadIdx.x - g * tpl;
     const bool act = g < nl;
-    const bool cc = K == LK_C2C && !io.fwd;  // backward: forward stages on conjugated data
+    // backward: forward stages on conjugated data
+    const bool cc = (K == LK_C2C || K == LK_C2R) && !io.fwd;
     cx<T> *const line = sm + (size_t)(act ? g : 0) * LSt;
     const char *ibase = io.in + (act ? line_off(io, line0 + g, false) : 0);
     if constexpr (RAW) {
@@ -358,12 +400,18 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, D
         __syncthreads();
     }
     int esc = 0;
-    IG_LINE_EDGE_SWITCH(P.st[0].R,
-                        (esc = line_first<T, E, R_>(line, ibase, io.is, P, tpl, t, act, cc, g, s_emax, &s_flag)))
+    int s_first = 1;
+    if constexpr (K == LK_C2R) {
+        line_herm_pre<T>(line, ibase, io.is, P, tpl, t, act, io.conj_in != 0, cc);
+        s_first = 0;
+    } else {
+        IG_LINE_EDGE_SWITCH(P.st[0].R,
+                            (esc = line_first<T, E, R_>(line, ibase, io.is, P, tpl, t, act, cc, g, s_emax, &s_flag)))
+    }
     __syncthreads();
     int cur = 0;
     const int nst = P.nst;
-    for (int s = 1; s < nst - 1; ++s) {
+    for (int s = s_first; s < nst - 1; ++s) {
         if constexpr (DB) {
             const cx<T> *src = sm + cur;
             cx<T> *dst = sm + (LS - cur);
@@ -378,7 +426,7 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, D
     sc.init(io);
     char *obase = io.out + (act ? line_off(io, line0 + g, true) : 0);
     const cx<T> *src = line + cur;
-    if constexpr (K == LK_C2C) {
+    if constexpr (K == LK_C2C || K == LK_C2R) {
         IG_LINE_EDGE_SWITCH(P.st[nst - 1].R,
                             (line_last_c2c<T, E, R_>(src, obase, io.os, P, nst - 1, tpl, t, act, cc, sc, esc)))
     } else if constexpr (K == LK_R2HC_S) {
@@ -446,6 +494,10 @@ static void launch_line_rs(const CoreDesc &d, const IODesc &io, unsigned grid, u
     if constexpr (!std::is_same<T, df>::value) {
         if (io.lay == LAY_R2C) {
             k_fft_line<T, E, RS, LK_R2C, DB><<<grid, blk, smem, st>>>(d, io);
+            return;
+        }
+        if (io.lay == LAY_C2R) {
+            k_fft_line<T, E, RS, LK_C2R, DB><<<grid, blk, smem, st>>>(d, io);
             return;
         }
     }
@@ -709,6 +761,7 @@ template <class T, int E, bool DB> cudaError_t set_smem_line_E(int bytes)
     if constexpr (!std::is_same<T, df>::value) {                                                          \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2HC, DB>, bytes);                \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_R2C, DB>, bytes);                 \
+        if (e == cudaSuccess) e = line_smem_attr(k_fft_line<T, E, RS_, LK_C2R, DB>, bytes);                 \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line_pipe<T, E, RS_, LK_C2C, DB>, bytes);            \
         if (e == cudaSuccess) e = line_smem_attr(k_fft_line_pipe<T, E, RS_, LK_R2HC, DB>, bytes);           \
     }

@@ -78,3 +78,20 @@ def test_r2c_half_spectrum_f32(engine, oracle_lib, shape, axes, fwd):
     last = got.reshape(-1, got.shape[-1]) if axes[-1] == len(shape) - 1 else None
     if last is not None and len(axes) == 1:
         assert np.all(last[:, 0].imag == 0) and np.all(last[:, -1].imag == 0)
+
+
+@pytest.mark.parametrize("shape,axes", [((33, 4096), [1]), ((7, 1000), [1]), ((5, 96), [1]), ((3, 6144), [1]),
+                                        ((4, 5, 2048), [2]), ((64, 512), [0, 1]), ((2, 40, 256), [1, 2])])
+@pytest.mark.parametrize("fwd", [True, False])
+def test_c2r_half_spectrum_f32(engine, oracle_lib, shape, axes, fwd):
+    """pocketfft::c2r FP32 with an even contiguous last axis: the line kernel
+    with the Hermitian pre-step read straight from HBM (DC and Nyquist
+    imaginary parts ignored, input conjugated for a forward c2r)."""
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(sum(shape) + 3 * fwd)
+    hs = list(shape)
+    hs[axes[-1]] = shape[axes[-1]] // 2 + 1
+    x = (rng.standard_normal(hs) + 1j * rng.standard_normal(hs)).astype(np.complex64)
+    got = F.c2r(x, shape, axes, forward=fwd, fct=0.25)
+    want = oracle_lib.c2r(x.astype(np.complex128), shape, axes, forward=fwd, fct=0.25)
+    assert oracle_lib.rel_l2(got, want) < tol(max(shape)) * 2, (shape, axes, fwd)
