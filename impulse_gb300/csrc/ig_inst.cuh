@@ -1,5 +1,7 @@
 // ig_inst.cuh -- launcher definitions, instantiated once per arithmetic.
 #pragma once
+#include <algorithm>
+
 #include "ig_kernels.cuh"
 #include "ig_launch.h"
 
@@ -178,7 +180,9 @@ cudaError_t Launch<Tag>::pad2d(const void *in, void *out, long long B, long long
                                long long P1, long long r0, long long c0, cudaStream_t st)
 {
     using S = typename Traits<typename TagType<Tag>::T>::S;
-    k_pad2d<S><<<map_grid(B * P0 * P1), 256, 0, st>>>((const S *)in, (S *)out, B, H, W, P0, P1, r0, c0);
+    const long long rows = B * P0;
+    k_pad2d<S><<<(unsigned)std::min<long long>(std::max<long long>(rows, 1), 152LL * 16), 256, 0, st>>>(
+        (const S *)in, (S *)out, B, H, W, P0, P1, r0, c0);
     return cudaGetLastError();
 }
 template <class Tag>
@@ -186,7 +190,9 @@ cudaError_t Launch<Tag>::crop2d(const void *in, void *out, long long B, long lon
                                 long long P1, long long r0, long long c0, cudaStream_t st)
 {
     using S = typename Traits<typename TagType<Tag>::T>::S;
-    k_crop2d<S><<<map_grid(B * H * W), 256, 0, st>>>((const S *)in, (S *)out, B, H, W, P0, P1, r0, c0);
+    const long long rows = B * H;
+    k_crop2d<S><<<(unsigned)std::min<long long>(std::max<long long>(rows, 1), 152LL * 16), 256, 0, st>>>(
+        (const S *)in, (S *)out, B, H, W, P0, P1, r0, c0);
     return cudaGetLastError();
 }
 template <class Tag>

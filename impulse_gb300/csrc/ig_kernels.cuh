@@ -1743,12 +1743,21 @@ template <class S>
 __global__ void k_pad2d(const S *__restrict__ in, S *__restrict__ out, long long B, long long H, long long W,
                         long long P0, long long P1, long long r0, long long c0)
 {
-    const long long total = B * P0 * P1;
-    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (long long)gridDim.x * blockDim.x) {
-        long long j = idx % P1, r = idx / P1, i = r % P0, b = r / P0;
-        long long si = i - r0, sj = j - c0;
-        out[idx] = (si >= 0 && si < H && sj >= 0 && sj < W) ? in[(b * H + si) * W + sj] : S(0);
+    // one output row per block iteration (the row's source decided once), the
+    // threads over its columns: no 64-bit division per element
+    const long long rows = B * P0;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const long long b = r / P0, si = r - b * P0 - r0;
+        S *orow = out + r * P1;
+        if (si >= 0 && si < H) {
+            const S *irow = in + (b * H + si) * W;
+            for (long long j = threadIdx.x; j < P1; j += blockDim.x) {
+                const long long sj = j - c0;
+                orow[j] = (sj >= 0 && sj < W) ? irow[sj] : S(0);
+            }
+        } else {
+            for (long long j = threadIdx.x; j < P1; j += blockDim.x) orow[j] = S(0);
+        }
     }
 }
 
@@ -1757,11 +1766,12 @@ template <class S>
 __global__ void k_crop2d(const S *__restrict__ in, S *__restrict__ out, long long B, long long H, long long W,
                          long long P0, long long P1, long long r0, long long c0)
 {
-    const long long total = B * H * W;
-    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (long long)gridDim.x * blockDim.x) {
-        long long j = idx % W, r = idx / W, i = r % H, b = r / H;
-        out[idx] = in[(b * P0 + i + r0) * P1 + j + c0];
+    const long long rows = B * H;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const long long b = r / H, i = r - b * H;
+        const S *irow = in + (b * P0 + i + r0) * P1 + c0;
+        S *orow = out + r * W;
+        for (long long j = threadIdx.x; j < W; j += blockDim.x) orow[j] = irow[j];
     }
 }
 
