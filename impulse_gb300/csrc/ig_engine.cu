@@ -702,6 +702,12 @@ static std::shared_ptr<Core> get_core(Arith a, long long M, bool real_tw)
 // by the batch dimensions (rows: consecutive threads walk a line's units)
 // with the plain complex layout or the even real -> halfcomplex one
 static const bool g_line_kernel = getenv("IG_NO_LINE_KERNEL") == nullptr;
+static int line_pf_env()
+{
+    const char *v = getenv("IG_LINE_PF");
+    return v ? std::max(0, std::min(8, atoi(v))) : 1;
+}
+static const int g_line_pf = line_pf_env();
 static const bool g_df_line_hc = getenv("IG_NO_DF_LINE_HC") == nullptr;
 static bool line_kernel_ok(Arith a, const CoreDesc &d, const IODesc &io)
 {
@@ -814,6 +820,19 @@ static long long smem_lpc(Arith a, const CoreDesc &d, const IODesc &io, long lon
     return std::min<long long>(lpc, std::max<long long>(1, io.nlines));
 }
 
+// Prefetch distance of the paired-lane kernel, in lines: SMs x resident CTAs
+// (shared memory, threads and registers at `regs` a thread) x lines a CTA,
+// times the IG_LINE_PF waves to prefetch ahead (default 1; 0 turns it off)
+static int line_pf_lines(size_t smem, long long threads, int regs, long long lpc)
+{
+    if (g_line_pf <= 0) return 0;
+    const long long by_smem = (smem_per_sm() - 1024) / (long long)(smem + 1024);
+    const long long by_thr = 2048 / std::max<long long>(1, threads);
+    const long long by_reg = 65536 / std::max<long long>(1, (long long)regs * threads);
+    const long long res = std::max<long long>(1, std::min(by_smem, std::min(by_thr, by_reg)));
+    return (int)std::min<long long>(0x3fffffff, g_line_pf * sm_count() * res * lpc);
+}
+
 static void launch_smem(Arith a, const CoreDesc &d_in, IODesc io, cudaStream_t st)
 {
     if (io.nlines <= 0) return;
@@ -890,11 +909,13 @@ static void launch_smem(Arith a, const CoreDesc &d_in, IODesc io, cudaStream_t s
         IODesc iop = io;
         iop.lpc = (int)lp;
         iop.tpl = (int)tplp;
+        iop.pf_lines = line_pf_lines((size_t)(lp * lb), lp * tplp, 64, lp);
         static std::once_flag once_pair;
         std::call_once(once_pair, [&] { ck(set_smem_pair(smax + 1024), "cudaFuncSetAttribute"); });
         e = launch_pair(d, iop, GS, (size_t)(lp * lb), st);
-    } else if (line_kernel_ok(a, d, io))
+    } else if (line_kernel_ok(a, d, io)) {
         e = a == A_F32 ? Launch<TagF32>::fft_line(d, io, smem, st) : Launch<TagDF>::fft_line(d, io, smem, st);
+    }
     else
         e = a == A_F32 ? Launch<TagF32>::fft_smem(d, io, smem, st)
           : a == A_DF  ? Launch<TagDF>::fft_smem(d, io, smem, st)

@@ -86,7 +86,8 @@ __device__ __forceinline__ float4 pv_interleave(PV v)
 // First stage, butterflies j = t + i tpl (one per slot): units j + m nr from
 // HBM, DFT, outputs j R + m (R even) as groups (j R + m) / 2.
 template <int E, int R>
-__device__ __forceinline__ void pair_first(float4 *dst, const char *base, int nr, int tpl, int t, bool cc)
+__device__ __forceinline__ void pair_first(float4 *dst, const char *base, int nr, int tpl, int t, bool cc,
+                                           const char *pf)
 {
     constexpr int NB = (E + R - 1) / R;
     float2 raw[NB][R];
@@ -97,6 +98,18 @@ __device__ __forceinline__ void pair_first(float4 *dst, const char *base, int nr
             const float2 *p = reinterpret_cast<const float2 *>(base) + j;
 #pragma unroll
             for (int m = 0; m < R; ++m) raw[i][m] = __ldcs(p + m * nr);
+        }
+    }
+    // the same points of a line a wave of CTAs ahead, into L2
+    if (pf) {
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+            const int j = t + i * tpl;
+            if (j < nr) {
+                const float2 *p = reinterpret_cast<const float2 *>(pf) + j;
+#pragma unroll
+                for (int m = 0; m < R; ++m) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + m * nr));
+            }
         }
     }
 #pragma unroll
@@ -272,12 +285,15 @@ __global__ void __maxnreg__(kPairRegs)
     const bool cc = K == PK_C2C && !io.fwd;
     float4 *bufA = sm + (size_t)(act ? g : 0) * 2 * GS, *bufB = bufA + GS;
     const char *ibase = io.in + (act ? line_off(io, line0 + g, false) : 0);
+    const char *pf = io.pf_lines && act && line0 + g + io.pf_lines < io.nlines
+                         ? io.in + line_off(io, line0 + g + io.pf_lines, false)
+                         : nullptr;
     if (act) {
         const int nr0 = L / P.st[0].R;
         switch (P.st[0].R) {
-        case 2: pair_first<E, 2>(bufA, ibase, nr0, tpl, t, cc); break;
-        case 4: pair_first<E, 4>(bufA, ibase, nr0, tpl, t, cc); break;
-        case 8: pair_first<E, 8>(bufA, ibase, nr0, tpl, t, cc); break;
+        case 2: pair_first<E, 2>(bufA, ibase, nr0, tpl, t, cc, pf); break;
+        case 4: pair_first<E, 4>(bufA, ibase, nr0, tpl, t, cc, pf); break;
+        case 8: pair_first<E, 8>(bufA, ibase, nr0, tpl, t, cc, pf); break;
         default: break;
         }
     }

@@ -105,6 +105,7 @@ struct IODesc {
     float fct_f, fct_h, fct_l;
     int fct_e;
     int lay;                // layout class of the kernel variant (set by the host)
+    int pf_lines;           // paired-lane kernel: prefetch into L2 the points of line l + pf_lines (0: none)
     // four-step inter-pass twiddle on output unit u of line l:
     // t = ((l % bn0) * u) mod tw4N, value w_hi[t / tw4S] * w_lo[t % tw4S]
     int tw4;
