@@ -2109,6 +2109,27 @@ int ig_rfft_exec_device(ig_rfft_plan plan, const void *in, void *out, size_t bat
     });
 }
 
+// Pageable host memory that the device reaches through the host's page tables
+// (address translation services): the pipeline's copies then run as SM copy
+// kernels, since a copy engine moving pageable memory waits for the host and
+// the two directions would not overlap.  IG_PAGEABLE_CE=1 keeps the copy
+// engines.
+static bool pageable_by_sms(const void *c)
+{
+    static const bool off = getenv("IG_PAGEABLE_CE") != nullptr;
+    if (off) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, c) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (at.type != cudaMemoryTypeUnregistered) return false;
+    int dev = device_id(), pageable = 0, host_pt = 0;
+    ck(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev), "device attribute");
+    ck(cudaDeviceGetAttribute(&host_pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev), "device attribute");
+    return pageable && host_pt;
+}
+
 // Host-memory batches.  Batches longer than one chunk run as a pipeline of
 // line chunks over three streams, so that the host-to-device copy of one
 // chunk, the transform of the next and the device-to-host copy of a third
@@ -2135,6 +2156,8 @@ static int host_batch(bool real, size_t n, Arith a, void *c, size_t batch, size_
             return;
         }
         Pipe &pp = pipe_for_device();
+        const bool by_sms = pageable_by_sms(c);
+        const int sms = sm_count() / 2;  // copy grids of 4 CTAs per SM
         const size_t cbytes = ((chunk_lines - 1) * dist + n) * (size_t)es;
         void *dbuf[kPipe];
         for (int i = 0; i < kPipe; ++i) dbuf[i] = pp.ws[i].get(cbytes);
@@ -2146,10 +2169,20 @@ static int host_batch(bool real, size_t n, Arith a, void *c, size_t batch, size_
                 char *h = (char *)c + l0 * line_bytes;
                 cudaStream_t st = pp.st[i % kPipe];
                 void *d = dbuf[i % kPipe];
-                ck(cudaMemcpyAsync(d, h, nb, cudaMemcpyHostToDevice, st), "H2D copy");
+                if (by_sms) {
+                    ck(launch_copy(h, d, nb, sms, st), "H2D copy kernel");
+                    count_launch();
+                } else {
+                    ck(cudaMemcpyAsync(d, h, nb, cudaMemcpyHostToDevice, st), "H2D copy");
+                }
                 Lines ln = contiguous_lines(d, d, (long long)nl, (long long)dist, (long long)dist, es, es);
                 exec_op(a, op, (long long)n, ln, forward, fct, st);
-                ck(cudaMemcpyAsync(h, d, nb, cudaMemcpyDeviceToHost, st), "D2H copy");
+                if (by_sms) {
+                    ck(launch_copy(d, h, nb, sms, st), "D2H copy kernel");
+                    count_launch();
+                } else {
+                    ck(cudaMemcpyAsync(h, d, nb, cudaMemcpyDeviceToHost, st), "D2H copy");
+                }
             }
             for (int k = 0; k < kPipe; ++k) ck(cudaStreamSynchronize(pp.st[k]), "pipeline");
         } catch (...) {

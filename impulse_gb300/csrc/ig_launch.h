@@ -71,6 +71,9 @@ cudaError_t launch_pair(const CoreDesc &d, const IODesc &io, int GS, size_t smem
 cudaError_t set_smem_pair(int bytes);
 // pair twiddle table of one stage (ns even)
 cudaError_t launch_stage_twp(void *tw, int R, int ns);
+// copy of `bytes` bytes by the SMs (grid of at most 8 CTAs per SM on `sms`
+// SMs), for host memory the device addresses through the host page tables
+cudaError_t launch_copy(const void *src, void *dst, size_t bytes, int sms, cudaStream_t st);
 
 // FP64 helpers for Bluestein tables (built in ig_inst_df.cu)
 cudaError_t launch_chirp64(void *bk, long long n);

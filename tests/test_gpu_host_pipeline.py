@@ -1,5 +1,8 @@
 """GPU parity of host-memory batches larger than one pipeline chunk (16 MiB):
-page-locked and pageable buffers, line gaps, lines off a 16-byte boundary."""
+page-locked and pageable buffers, line gaps, lines off a 16-byte boundary.
+Pageable buffers on a GPU that walks the host page tables are copied by SM
+copy kernels (16-, 8- and 4-byte units by alignment); IG_PAGEABLE_CE=1 in a
+child process keeps the copy engines and must give identical bytes."""
 import ctypes as C
 
 import numpy as np
@@ -74,3 +77,61 @@ def test_device_pointers_offset_by_one_real(engine, oracle_lib):
         assert rc == L.IG_EINVAL
     finally:
         lib.ig_destroy_cfft_plan(cplan)
+
+
+@pytest.mark.parametrize("n,dist", [(4096, 4096), (1000, 1003)])
+def test_pageable_f32_lines_off_8_bytes(engine, oracle_lib, n, dist):
+    """FP32 real lines in pageable memory starting 4 bytes past an 8-byte
+    boundary: the copy kernels move 4-byte units; the words before and between
+    the lines stay untouched."""
+    from impulse_gb300 import _lib as L
+    lib = L.load()
+    batch = (40 << 20) // (4 * dist)
+    rng = np.random.default_rng(dist)
+    buf = rng.standard_normal(batch * dist + 2).astype(np.float32)
+    x = buf.copy()
+    off = 1 if buf.ctypes.data % 8 == 0 else 2  # start at 4 mod 8
+    ptr = buf.ctypes.data + 4 * off
+    assert ptr % 8 == 4
+    plan = lib.ig_make_rfft_plan(n, L.IG_F32)
+    try:
+        L.check(lib.ig_rfft_exec_batch(plan, ptr, batch, dist, 1, 1.0))
+    finally:
+        lib.ig_destroy_rfft_plan(plan)
+    y = buf[off:off + batch * dist].reshape(batch, dist)
+    xs = x[off:off + batch * dist].reshape(batch, dist)
+    assert np.array_equal(buf[:off], x[:off]) and np.array_equal(buf[off + batch * dist:], x[off + batch * dist:])
+    assert np.array_equal(y[:, n:], xs[:, n:])
+    rows = [0, 1, batch // 3, batch - 1]
+    want = oracle_lib.rfft_hc(xs[rows, :n].astype(np.float64), forward=True, fct=1.0)
+    assert oracle_lib.rel_l2(y[rows, :n].astype(np.float64), want) < 1e-6 * np.log2(n)
+
+
+CHILD = r"""
+import ctypes as C, hashlib, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from impulse_gb300 import _lib as L
+lib = L.load()
+n = 4096
+x = np.random.default_rng(3).standard_normal((5000, n))
+plan = lib.ig_make_rfft_plan(n, L.IG_F64)
+L.check(lib.ig_rfft_exec_batch(plan, x.ctypes.data, 5000, n, 1, 1.0))
+print(hashlib.sha256(x.tobytes()).hexdigest())
+"""
+
+
+def test_pageable_sm_copies_match_copy_engines(engine):
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    for extra in ({}, {"IG_PAGEABLE_CE": "1"}):
+        env = dict(os.environ)
+        env.pop("IG_PAGEABLE_CE", None)
+        env.update(extra)
+        r = subprocess.run([sys.executable, "-c", CHILD, root], capture_output=True, text=True, env=env, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.append(r.stdout.strip().splitlines()[-1])
+    assert outs[0] == outs[1]
