@@ -867,6 +867,7 @@ static void launch_smem(Arith a, const CoreDesc &d_in, IODesc io, cudaStream_t s
     io.tpl = (int)tpl;
     set_line_divs(io);
     io.lay = choose_layout(a, io);
+    if (io.rowconv && io.lay != LAY_TW) raise(IG_EINVAL, "internal: row convolution outside the twiddle layout");
     size_t smem = (size_t)(lpc * line_bytes);
     static std::once_flag once[3];
     std::call_once(once[a], [&] {
@@ -1277,11 +1278,86 @@ static void run_fourstep_split(const Core &c, const IODesc &io, char *B, cudaStr
 // backward FFT_L.  Bluestein conjugates the kernel for the backward
 // direction; Rader always runs forward (its maps conjugate) and keeps each
 // line's A[0] from before the product in a0buf.
+// The convolution of Rader / Bluestein over a multi-pass core of length L:
+// forward FFT_L, product with the table (A[0] kept first for Rader), inverse
+// FFT_L, in place on the contiguous scratch lines A.  With the row-convolution
+// mode of the shared-memory kernel (IG_NO_ROWCONV=1 turns it off) a four-step
+// core L = N1 N2 takes three passes instead of four: columns forward with the
+// twiddle (A -> B), then per row k1 of B the forward FFT_N2, the product in
+// the natural spectrum order k1 + N1 k2, the inverse FFT_N2 and the inverse
+// twiddle w^-(k1 n2) (B in place), then columns inverse (B -> A), which leaves
+// x[n2 + N2 n1] in natural order; a one-CTA core takes one launch instead of two.
+static const bool g_rowconv = getenv("IG_NO_ROWCONV") == nullptr;
+
 static void convolve_passes(const Core &c, char *A, long long L, long long nl, int fwd, void *a0buf,
                             cudaStream_t st)
 {
     const long long ES = 2 * (long long)store_real_bytes(c.a);
     const bool rader = c.kind == 3;
+    const Core &s = *c.sub;
+    if (g_rowconv && c.a != A_F64 && (s.kind == 0 || s.kind == 1) && (s.kind == 1 || s.d.blue == 0)) {
+        IODesc q = blank_io();
+        contig_side(q, false, A, ES, L, nl);
+        contig_side(q, true, A, ES, L, nl);
+        q.nlines = nl;
+        q.in_kind = IN_C;
+        q.out_kind = OUT_C;
+        q.cnt_in = q.cnt_out = (int)L;
+        q.nreal = L;
+        q.fwd = 1;
+        const void *tab = rader ? c.d.chirpf : c.chirpf;
+        const int tconj = (!rader && !fwd) ? 1 : 0;
+        if (s.kind == 0) {
+            q.mul = tab;
+            q.mul_a = 0;
+            q.mul_b = 1;
+            q.mul_conj = tconj;
+            q.keep0 = a0buf;
+            q.keep0_rows = 1;
+            q.rowconv = 1;
+            launch_smem(c.a, s.d, q, st);
+            return;
+        }
+        const long long N1 = s.N1, N2 = s.N2;
+        char *B = (char *)scratch_for(st).get(1, (size_t)(nl * L * ES));
+        IODesc p1, p2;
+        fourstep_passes(s, q, B, p1, p2);
+        launch_smem(c.a, s.c1->d, p1, st);
+        // rows of B in place
+        IODesc r = p2;
+        r.out = B;
+        r.out_kind = OUT_C;
+        r.os = ES;
+        r.bso[0] = N2 * ES;
+        r.bso[1] = L * ES;
+        r.bso[2] = L * ES * q.bn[0];
+        r.cols_out = 0;
+        r.mul = tab;
+        r.mul_a = 1;
+        r.mul_b = N1;
+        r.mul_conj = tconj;
+        r.keep0 = a0buf;
+        r.keep0_rows = (int)N1;
+        r.rowconv = 1;
+        r.tw4 = 1;
+        r.tw4N = L;
+        r.tw4S = N2;
+        r.fdS = make_fdiv((unsigned)N2);
+        r.tw4hi = s.whi;
+        r.tw4lo = s.wlo;
+        r.tw4tab = nullptr;
+        r.tw4_dim1 = 0;
+        launch_smem(c.a, s.c2->d, r, st);
+        // columns inverse, B -> A, natural order
+        IODesc p3 = p1;
+        p3.in = B;
+        p3.out = A;
+        p3.tw4 = 0;
+        p3.tw4hi = p3.tw4lo = p3.tw4tab = nullptr;
+        p3.fwd = 0;
+        launch_smem(c.a, s.c1->d, p3, st);
+        return;
+    }
     for (int pass = 0; pass < 2; ++pass) {
         IODesc q = blank_io();
         contig_side(q, false, A, ES, L, nl);

@@ -485,7 +485,9 @@ __device__ __forceinline__ void rader_permute(cx<T> *line, const int *__restrict
     __syncthreads();
 }
 
-template <class T, int E, int RS, int LAY, bool DB = (E == 8)>
+// RC: the row-convolution mode (IODesc::rowconv) compiled in; the
+// stand-alone twiddle / table variant only
+template <class T, int E, int RS, int LAY, bool DB = (E == 8), bool RC = (LAY == LAY_TW)>
 __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, long long blk, const char *in_base,
                                           char *out_base)
 {
@@ -718,13 +720,19 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
     // Rader (prime M, L = M - 1; forward): a[q] = x[g^-q], A = FFT_L(a),
     // C = A * B with B = FFT_L(w^(g^m)) / L, c = IFFT_L(C) as conj(FFT_L(conj C)),
     // X[0] = x[0] + A[0], X[g^p] = x[0] + c[p].
+    // Row convolution (io.rowconv; the rows of a four-step core L = N1 N2, or
+    // whole lines when N1 = 1): Y = FFT_N2(row k1), C = Y * tab[k1 mul_a + u
+    // mul_b] (the product of a convolution in the natural spectrum order
+    // k1 + N1 k2), the inverse FFT_N2 as conj(FFT_N2(conj C)); the epilogue
+    // applies the final conjugation and the inverse four-step twiddle.
     {
         const cx<T> *ch = reinterpret_cast<const cx<T> *>(P.chirp);
         const cx<T> *chf = reinterpret_cast<const cx<T> *>(P.chirpf);
         const int L = P.L;
         constexpr bool kRader = RS == RS_FULL;  // Rader steps compiled in the full class only
         const bool blue = P.blue == 1, rader = kRader && P.blue == 2;
-        const int npass = P.blue ? 2 : 1;
+        const bool rowconv = RC && io.rowconv;
+        const int npass = (P.blue || rowconv) ? 2 : 1;
         for (int pass = 0; pass < npass; ++pass) {
             if (blue && g < nl) {
                 if (pass == 0) {
@@ -763,7 +771,40 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                     }
                 }
             }
-            if (P.blue) __syncthreads();
+            if constexpr (RC) if (rowconv && pass == 1 && g < nl) {
+                const long long l = line0 + g;
+                const int k1 = line_i0(io, l);
+                const cx<T> *tb = reinterpret_cast<const cx<T> *>(io.mul) + (long long)k1 * io.mul_a;
+                const long long mb = io.mul_b;
+                // unit 0 of row 0 before the product (Rader's A[0]), by the
+                // thread that owns unit 0
+                if (t == 0 && io.keep0 && (io.keep0_rows == 1 || k1 == 0)) {
+                    OutScale<T> sc;
+                    sc.init(io);
+                    const int esc = scaled ? s_esc[2 * g] : 0;
+                    const cx<T> z = sget(myline);
+                    S2 o;
+                    o.x = sc.apply(z.r, esc);
+                    o.y = sc.apply(z.i, esc);
+                    reinterpret_cast<S2 *>(io.keep0)[io.keep0_rows == 1 ? l : (long long)fdiv((unsigned)l, io.fb0)] = o;
+                }
+                bool done = false;
+                if constexpr (std::is_same<T, df>::value) {
+                    if (!io.mul_conj) {
+                        for (int u = t; u < L; u += tpl) {
+                            cx<df> *p = myline + sp(u, pad);
+                            pst(p, pconj(prenorm(pmulw_cx<false>(pld(p), tb + (long long)u * mb, P.neg1))));
+                        }
+                        done = true;
+                    }
+                }
+                if (!done)
+                    for (int u = t; u < L; u += tpl) {
+                        const cx<T> z = sget(myline + sp(u, pad)), w = tb[(long long)u * mb];
+                        sput(myline + sp(u, pad), conjx(io.mul_conj ? cmulc(z, w) : cmul(z, w)));
+                    }
+            }
+            if (P.blue || rowconv) __syncthreads();
             if constexpr (DB) {
                 cur = run_stages_db<T, E, RS>(sm, cur, P, nl, tpl, g, t, LSt);
                 myline = line_a + cur;
@@ -976,24 +1017,28 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 // output pointer and the table rows advance by one add per unit
                 const int cnt = io.cnt_out;
                 const long long os = io.os, pstep = (long long)tpl * os;
+                // row convolution: the product and unit 0 were taken between
+                // the passes; here the final conjugation and the inverse twiddle
+                const bool rc = RC && io.rowconv;
                 const auto *wrow = io.tw4 && io.tw4tab
                                        ? reinterpret_cast<const typename Bfly<T>::W *>(io.tw4tab) + (size_t)n2 * cnt
                                        : nullptr;
-                const cx<T> *mrow = io.mul ? mt + ml : nullptr;
+                const cx<T> *mrow = io.mul && !rc ? mt + ml : nullptr;
                 const long long mb = io.mul_b;
+                const bool twf = io.fwd && !rc;
                 char *p = base + (long long)t2 * os;
                 for (int u = t2; u < cnt; u += tpl, p += pstep) {
                     cx<T> z = sget(line + sp(u, pad));
-                    if (cc) z.i = -z.i;
+                    if (cc || rc) z.i = -z.i;
                     if (wrow) {
-                        z = tw_apply<T>(z, wrow + u, io.fwd, P);
+                        z = tw_apply<T>(z, wrow + u, twf, P);
                     } else if (io.tw4) {
                         const unsigned tt = (unsigned)n2 * (unsigned)u;
                         const unsigned hi = fdiv(tt, io.fdS), lo = tt - hi * (unsigned)io.tw4S;
                         const cx<T> w = cmul(whi[hi], wlo[lo]);
-                        z = io.fwd ? cmul(z, w) : cmulc(z, w);
+                        z = twf ? cmul(z, w) : cmulc(z, w);
                     }
-                    if (io.keep0 && u == 0 && (io.keep0_rows == 1 || i0l == 0)) {
+                    if (io.keep0 && !rc && u == 0 && (io.keep0_rows == 1 || i0l == 0)) {
                         S2 o;
                         o.x = sc.apply(z.r, esc);
                         o.y = sc.apply(z.i, esc);
@@ -1149,7 +1194,7 @@ __global__ void __launch_bounds__(512) __maxnreg__((fft_smem_regs<T, E, RS, DB>(
         const WorkGroup &G = groups[lo];
         const char *ib = G.in_base == 0 ? in : G.in_base == 1 ? (const char *)out : (const char *)scr;
         char *ob = G.out_base == 1 ? out : G.out_base == 2 ? scr : (char *)in;
-        fft_block<T, E, RS, LAY, DB>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]),
+        fft_block<T, E, RS, LAY, DB, false>(G.P, G.io, (long long)(w - (unsigned long long)prefix[lo]),
                                      ib + (size_t)G.io.in, ob + (size_t)G.io.out);
         __syncthreads();
     }

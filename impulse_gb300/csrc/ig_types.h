@@ -123,6 +123,11 @@ struct IODesc {
     // the product), one per transform: Rader's A[0] on a multi-pass core
     void *keep0;
     int keep0_rows;  // lines per transform: 1 (one-pass core) or N1 (four-step second pass)
+    // row convolution (twiddle / table layout only): the lines are rows k1 of
+    // a four-step core (or whole lines, N1 = 1); forward FFT, the `mul` product
+    // (and keep0) between two stage passes, inverse FFT, and the inverse
+    // four-step twiddle (tw4) in the epilogue
+    int rowconv;
     // per-line byte offsets (device arrays) replacing the batch dims when set
     const long long *loff_in, *loff_out;
     // POST_SPLIT4 (when split_N1 != 0): the real-split twiddles exp(-2 pi i k / 2M), k <= M, and N1
