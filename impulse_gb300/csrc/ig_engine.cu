@@ -288,6 +288,9 @@ static int choose_layout(Arith a, const IODesc &io)
     const bool plain = !io.conj_in && !io.conj_out && !io.real_out && io.pre == PRE_NONE;
     // the twiddle / table variant also keeps Rader's unit 0 (keep0) before the product
     if (io.keep0 && !(io.tw4 || io.mul)) return LAY_GEN;
+    if (io.rowconv)
+        return (plain && !io.pair && io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C) ? LAY_RC
+                                                                                                          : LAY_GEN;
     if (io.tw4 || io.mul)
         return (plain && !io.pair && io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C) ? LAY_TW
                                                                                                           : LAY_GEN;
@@ -867,7 +870,7 @@ static void launch_smem(Arith a, const CoreDesc &d_in, IODesc io, cudaStream_t s
     io.tpl = (int)tpl;
     set_line_divs(io);
     io.lay = choose_layout(a, io);
-    if (io.rowconv && io.lay != LAY_TW) raise(IG_EINVAL, "internal: row convolution outside the twiddle layout");
+    if (io.rowconv && io.lay != LAY_RC) raise(IG_EINVAL, "internal: row convolution outside its layout class");
     size_t smem = (size_t)(lpc * line_bytes);
     static std::once_flag once[3];
     std::call_once(once[a], [&] {

@@ -20,6 +20,7 @@ static void launch_rs(const CoreDesc &d, const IODesc &io, unsigned grid, unsign
     case LAY_R2HC: IG_K(RS, LAY_R2HC); break;
     case LAY_PR2HC: IG_K(RS, LAY_PR2HC); break;
     case LAY_TW: IG_K(RS, LAY_TW); break;
+    case LAY_RC: IG_K(RS, LAY_RC); break;
     default: IG_K(RS_FULL, LAY_GEN); break;
     }
 }
@@ -91,13 +92,12 @@ template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes)
 {
     cudaError_t e = set_smem_attr(k_fft_smem<T, E, RS_FULL, LAY_GEN, DB>, bytes);
     if constexpr (Variants<T, E>::kSpecialised) {
-        const int lays[4] = {LAY_C2C, LAY_R2HC, LAY_PR2HC, LAY_TW};
-        (void)lays;
 #define IG_S(RS_)                                                                                         \
     if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_C2C, DB>, bytes);                     \
     if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_R2HC, DB>, bytes);                    \
     if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_PR2HC, DB>, bytes);                   \
-    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_TW, DB>, bytes);
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_TW, DB>, bytes);                     \
+    if (e == cudaSuccess) e = set_smem_attr(k_fft_smem<T, E, RS_, LAY_RC, DB>, bytes);
         IG_S(RS_P2)
         IG_S(RS_ALL)
         IG_S(RS_FULL)

@@ -485,9 +485,10 @@ __device__ __forceinline__ void rader_permute(cx<T> *line, const int *__restrict
     __syncthreads();
 }
 
-// RC: the row-convolution mode (IODesc::rowconv) compiled in; the
-// stand-alone twiddle / table variant only
-template <class T, int E, int RS, int LAY, bool DB = (E == 8), bool RC = (LAY == LAY_TW)>
+// RC: the row-convolution mode (IODesc::rowconv) compiled in (layout class
+// LAY_RC: the twiddle / table variant plus the mode, kept apart so that the
+// plain twiddle variant keeps its registers)
+template <class T, int E, int RS, int LAY, bool DB = (E == 8), bool RC = (LAY == LAY_RC)>
 __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, long long blk, const char *in_base,
                                           char *out_base)
 {
@@ -545,7 +546,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
             const int esc = (scaled && act) ? s_esc[2 * gi] : 0;
             const int escb = (scaled && act) ? s_esc[2 * gi + 1] : 0;
             unsigned emax = 0, emaxb = 0;  // largest magnitude words (dmag / fmag)
-            if (act && (LAY == LAY_C2C || LAY == LAY_R2HC || LAY == LAY_TW)) {
+            if (act && (LAY == LAY_C2C || LAY == LAY_R2HC || LAY == LAY_TW || LAY == LAY_RC)) {
                 // complex units, no conjugation / Hermitian steps / pairs
                 // loads in flight per thread before the first is used: the prologue is
                 // latency-bound on global loads; FP32 units are small enough for eight
@@ -1011,7 +1012,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
                 }
                 return;
             }
-            if constexpr (LAY == LAY_TW) {
+            if constexpr (LAY == LAY_TW || LAY == LAY_RC) {
                 // complex units out (the layout class guarantees it), with the
                 // four-step twiddle and / or the pointwise table product; the
                 // output pointer and the table rows advance by one add per unit

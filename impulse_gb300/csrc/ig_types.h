@@ -28,6 +28,7 @@ constexpr int LAY_R2HC = 2;   // contiguous reals as complex pairs, real split, 
 constexpr int LAY_PR2HC = 3;  // two real lines per complex line, pair split, halfcomplex out
 constexpr int LAY_TW = 4;     // complex in / out with the four-step twiddle or a pointwise table
 constexpr int LAY_C2R = 6;    // half spectrum in (Hermitian pre-step), real pairs out (c2r; as LAY_R2C)
+constexpr int LAY_RC = 7;     // LAY_TW with the row-convolution mode (IODesc::rowconv) compiled in
 constexpr int LAY_R2C = 5;    // contiguous reals as complex pairs, real split, half spectrum out (r2c; the
                               // shared-memory kernel runs it as LAY_GEN, the FP32 line kernel natively)
 
