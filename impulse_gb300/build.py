@@ -18,7 +18,7 @@ UNITS = ["ig_engine.cu", "ig_inst_f32.cu", "ig_inst_df.cu", "ig_inst_f64.cu", "i
          "ig_inst_f32_e16.cu", "ig_inst_df_e8.cu", "ig_inst_df_e16.cu", "ig_inst_f64_e8.cu", "ig_inst_f64_e16.cu",
          "ig_inst_f32_e16db.cu", "ig_inst_df_e16db.cu", "ig_inst_f64_e16db.cu",
          "ig_line_f32_e8.cu", "ig_line_f32_e16.cu", "ig_line_f32_e16db.cu", "ig_line_df_e8.cu", "ig_line_df_e16.cu",
-         "ig_line_df_e16db.cu", "ig_pair_f32.cu", "ig_copy.cu"]
+         "ig_line_df_e16db.cu", "ig_pair_f32.cu", "ig_copy.cu", "ig_wide_df.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden"]

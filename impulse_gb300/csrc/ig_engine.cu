@@ -129,15 +129,24 @@ static thread_local int g_cfg_override_arith = -1;
 
 static TuneCfg tune_lookup(int a, long long L)
 {
-    if (g_cfg_override && g_cfg_override_len == L && g_cfg_override_arith == a) return *g_cfg_override;
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tune.find(std::make_pair(a, L));
-    return it == g_tune.end() ? TuneCfg() : it->second;
+    TuneCfg c;
+    if (g_cfg_override && g_cfg_override_len == L && g_cfg_override_arith == a) {
+        c = *g_cfg_override;
+    } else {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(std::make_pair(a, L));
+        if (it != g_tune.end()) c = it->second;
+    }
+    // 8 elements a thread beyond 4096 points: the wide variants exist for
+    // double-float only (elsewhere the default, 16 beyond 4096, applies)
+    if (a != A_DF && c.E == 8) c.E = 0;
+    return c;
 }
 
 static int elems_per_thread(long long L, int cfgE = 0)
 {
-    if (cfgE == 8 && L <= 4096) return 8;
+    // (tuned plans may take 8 elements a thread up to kMaxThreadsE8 threads)
+    if (cfgE == 8 && L <= 8LL * kMaxThreadsE8) return 8;
     if (cfgE == 16) return 16;
     return L <= 4096 ? 8 : 16;
 }
@@ -717,6 +726,9 @@ static bool line_kernel_ok(Arith a, const CoreDesc &d, const IODesc &io)
     if (!g_line_kernel || (a != A_F32 && a != A_DF) || d.blue != 0 || d.nst < 2 || d.L != d.M) return false;
     if (d.rs == RS_FULL || !line_edge_ok(d.st[0].R) || !line_edge_ok(d.st[d.nst - 1].R)) return false;
     if (io.cols_in || io.cols_out || io.loff_in || io.loff_out || io.pair || io.split_N1) return false;
+    // the double-float line variants other than the 8-element halfcomplex one
+    // run at 128 registers: 512 threads a CTA at most
+    if (a == A_DF && !(io.lay == LAY_R2HC && d.E == 8) && (d.L + d.E - 1) / d.E > 512) return false;
     if (io.lay == LAY_C2C) return io.post == POST_NONE && io.in_kind == IN_C && io.out_kind == OUT_C;
     // r2c half spectra (FP32): the halfcomplex butterflies storing complex units
     if (io.lay == LAY_R2C)
@@ -3174,7 +3186,9 @@ ig_multi_plan ig_make_multi_plan(int dtype, size_t count, const size_t *lengths,
         for (size_t i = 0; i < count; ++i) {
             auto c = get_core(m->a, m->len[i], false);
             m->cores.push_back(c);
-            if (c->kind == 0) by_len[m->len[i]].push_back((long long)i);
+            // (wide cores, more than 512 threads a line, take the general path:
+            // the work-list kernel is bounded at 512 threads)
+            if (c->kind == 0 && (c->d.L + c->d.E - 1) / c->d.E <= 512) by_len[m->len[i]].push_back((long long)i);
             else if (c->kind == 1) four.push_back((long long)i);
             else m->general.push_back((long long)i);
         }
@@ -3497,10 +3511,11 @@ int ig_autotune(int dtype, size_t length, int kind, double *best_ms)
             }
             for (int order : {0, 1})
                 for (int E : {8, 16}) {
-                    if (E == 8 && L > 4096) continue;
+                    const long long e8max = a == A_DF ? 8LL * kMaxThreadsE8 : 4096;
+                    if (E == 8 && L > e8max) continue;
                     for (int lpc : {0, 1, 2, 4, 8, 16, 32}) {
                         long long tpl = (L + E - 1) / E;
-                        if (lpc * tpl > 512) continue;
+                        if (lpc * tpl > (E == 8 && L > 4096 ? kMaxThreadsE8 : 512)) continue;
                         for (int no9 : {0, 1}) {
                             if (no9 && L % 9) continue;
                             TuneCfg c;

@@ -29,6 +29,12 @@ template <class T, int E, bool DB>
 cudaError_t launch_line_pipe_E(const CoreDesc &d, const IODesc &io, size_t work_bytes, int nslot, int sms,
                                cudaStream_t st);
 template <class T, int E, bool DB> cudaError_t line_pipe_faults_E(unsigned *count);
+// the wide double-float 8-element variants (more than 512 threads a CTA), in
+// their own translation unit (ig_wide_df.cu)
+template <class T> cudaError_t launch_fft_wide(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
+template <class T> cudaError_t set_smem_wide(int bytes);
+template <class T> cudaError_t launch_line_wide(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st);
+template <class T> cudaError_t set_smem_line_wide(int bytes);
 
 template <class Tag> cudaError_t Launch<Tag>::fft_smem(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
@@ -86,6 +92,10 @@ template <class Tag> cudaError_t Launch<Tag>::set_max_smem(int bytes)
     // the dynamic limit excludes each kernel's static shared memory
     cudaError_t e;
     if ((e = set_smem_E<T, 8, true>(bytes)) != cudaSuccess) return e;
+    if constexpr (std::is_same<T, df>::value) {
+        if ((e = set_smem_wide<T>(bytes)) != cudaSuccess) return e;
+        if ((e = set_smem_line_wide<T>(bytes)) != cudaSuccess) return e;
+    }
     if ((e = set_smem_E<T, 16, false>(bytes)) != cudaSuccess) return e;
     if ((e = set_smem_E<T, 16, true>(bytes)) != cudaSuccess) return e;
     if constexpr (!std::is_same<T, double>::value) {

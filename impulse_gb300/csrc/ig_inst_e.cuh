@@ -30,6 +30,10 @@ template <class T, int E, bool DB>
 cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
     const unsigned grid = (unsigned)((io.nlines + io.lpc - 1) / io.lpc), blk = (unsigned)(io.lpc * io.tpl);
+    if (blk > 512) {
+        if constexpr (std::is_same<T, df>::value && E == 8 && DB) return launch_fft_wide<T>(d, io, smem, st);
+        return cudaErrorInvalidConfiguration;
+    }
     if constexpr (!Variants<T, E>::kSpecialised) {
         k_fft_smem<T, E, RS_FULL, LAY_GEN, DB><<<grid, blk, smem, st>>>(d, io);
     } else {

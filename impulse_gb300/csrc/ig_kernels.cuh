@@ -1140,8 +1140,9 @@ template <class T, int E, int RS, bool DB> constexpr int fft_smem_regs()
     return 128;
 }
 
-template <class T, int E, int RS, int LAY, bool DB>
-__global__ void __launch_bounds__(512) __maxnreg__((fft_smem_regs<T, E, RS, DB>()))
+// NT: the launch bound (kMaxThreadsE8 for the wide double-float variants)
+template <class T, int E, int RS, int LAY, bool DB, int NT = 512>
+__global__ void __launch_bounds__(NT) __maxnreg__((fft_smem_regs<T, E, RS, DB>()))
     k_fft_smem(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
 {
     fft_block<T, E, RS, LAY, DB>(P, io, blockIdx.x, io.in, io.out);

@@ -375,8 +375,8 @@ template <class T, int E, int RS, int K, bool DB> constexpr int fft_line_regs()
 // batch dimensions, complex units in (contiguous reals as pairs for LK_R2HC)
 // and complex units (LK_C2C) or halfcomplex reals (LK_R2HC) out, and first and
 // last radices with line_edge_ok (LK_R2HC: last radix with line_r2hc_last_ok).
-template <class T, int E, int RS, int K, bool DB>
-__global__ void __launch_bounds__(512) __maxnreg__((fft_line_regs<T, E, RS, K, DB>()))
+template <class T, int E, int RS, int K, bool DB, int NT = 512>
+__global__ void __launch_bounds__(NT) __maxnreg__((fft_line_regs<T, E, RS, K, DB>()))
     k_fft_line(const __grid_constant__ CoreDesc P, const __grid_constant__ IODesc io)
 {
     constexpr bool RAW = Traits<T>::kRaw;
@@ -508,6 +508,10 @@ template <class T, int E, bool DB>
 cudaError_t launch_line_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaStream_t st)
 {
     const unsigned grid = (unsigned)((io.nlines + io.lpc - 1) / io.lpc), blk = (unsigned)(io.lpc * io.tpl);
+    if (blk > 512) {
+        if constexpr (std::is_same<T, df>::value && E == 8 && DB) return launch_line_wide<T>(d, io, smem, st);
+        return cudaErrorInvalidConfiguration;
+    }
     if (d.rs == RS_P2) launch_line_rs<T, E, DB, RS_P2>(d, io, grid, blk, smem, st);
     else if (E == 8 && d.rs == RS_P235) launch_line_rs<T, E, DB, (E == 8 ? RS_P235 : RS_ALL)>(d, io, grid, blk, smem, st);
     else if (d.rs == RS_ALL || d.rs == RS_P235) launch_line_rs<T, E, DB, RS_ALL>(d, io, grid, blk, smem, st);

@@ -29,6 +29,12 @@ constexpr int LAY_PR2HC = 3;  // two real lines per complex line, pair split, ha
 constexpr int LAY_TW = 4;     // complex in / out with the four-step twiddle or a pointwise table
 constexpr int LAY_C2R = 6;    // half spectrum in (Hermitian pre-step), real pairs out (c2r; as LAY_R2C)
 constexpr int LAY_RC = 7;     // LAY_TW with the row-convolution mode (IODesc::rowconv) compiled in
+
+// Threads a CTA may have: 512; the wide double-float 8-element variants (a
+// separate instantiation at 80-96 registers) run lines of up to 8 x 672 =
+// 5376 points as one 672-thread CTA instead of 16-element threads at half the
+// warps
+constexpr int kMaxThreadsE8 = 672;
 constexpr int LAY_R2C = 5;    // contiguous reals as complex pairs, real split, half spectrum out (r2c; the
                               // shared-memory kernel runs it as LAY_GEN, the FP32 line kernel natively)
 
