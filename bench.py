@@ -728,6 +728,10 @@ PROFILE_CASES = {
     "rfft65521_f64": ("r", "f64", 65521, 256),
     "rfft65521_f32": ("r", "f32", 65521, 512),
     "rfft8191_f64": ("r", "f64", 8191, 2048),
+    # autotuned plans (the benchmark's): wide 8-element core, Rader row convolution
+    "rfft10000_f64_tuned": ("r", "f64", 10000, 1677, "tune"),
+    "rfft8191_f64_tuned": ("r", "f64", 8191, 2048, "tune"),
+    "rfft65521_f64_tuned": ("r", "f64", 65521, 256, "tune"),
     # every 10th transform of the uneven-length workload (FP32, work-list graph)
     "uneven_tenth_f32": ("u", "f32", 0, 10),
     # FFT convolution forward, 4 images 2048^2 f32, 31x31 filters, padded to 4096^2
@@ -742,7 +746,8 @@ def run_case(name):
     captures just that)."""
     import torch
     from impulse_gb300 import _lib as L
-    kind, dt, n, b = PROFILE_CASES[name]
+    kind, dt, n, b = PROFILE_CASES[name][:4]
+    tune = PROFILE_CASES[name][4:] == ("tune",)
     lib = L.load()
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     code = L.IG_F64 if dt == "f64" else L.IG_F32
@@ -790,6 +795,9 @@ def run_case(name):
         prof.cudaProfilerStop()
         print(json.dumps({"case": name, "ok": True}))
         return
+    if tune:
+        ms = C.c_double(0.0)
+        L.check(lib.ig_autotune(code, n, 1 if kind == "r" else 0, C.byref(ms)))
     if kind == "r":
         x = torch.randn((b, n), device="cuda", dtype=torch.float64 if dt == "f64" else torch.float32)
         plan = lib.ig_make_rfft_plan(n, code)
