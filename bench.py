@@ -732,6 +732,9 @@ PROFILE_CASES = {
     "rfft10000_f64_tuned": ("r", "f64", 10000, 1677, "tune"),
     "rfft8191_f64_tuned": ("r", "f64", 8191, 2048, "tune"),
     "rfft65521_f64_tuned": ("r", "f64", 65521, 256, "tune"),
+    "rfft65521_f32_tuned": ("r", "f32", 65521, 512, "tune"),
+    "rfft8191_f32_tuned": ("r", "f32", 8191, 4096, "tune"),
+    "rfft29403_f32_tuned": ("r", "f32", 29403, 1141, "tune"),
     # every 10th transform of the uneven-length workload (FP32, work-list graph)
     "uneven_tenth_f32": ("u", "f32", 0, 10),
     # FFT convolution forward, 4 images 2048^2 f32, 31x31 filters, padded to 4096^2
