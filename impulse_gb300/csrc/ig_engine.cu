@@ -789,7 +789,7 @@ static int sm_count()
 static const bool g_pair_kernel = getenv("IG_NO_PAIR") == nullptr;
 static bool pair_ok(Arith a, const CoreDesc &d, const IODesc &io)
 {
-    if (io.lay != LAY_C2C && io.lay != LAY_R2HC) return false;
+    if (io.lay != LAY_C2C && io.lay != LAY_R2HC && io.lay != LAY_R2C) return false;
     // below 512 points k_fft_line measured faster (a line's 16-element
     // threads are too few: N = 96 real 1966 vs 1679 GB/s, 256 3070 vs 2675);
     // from 512 on the pairs win (1200 real 1927 -> 2178, 1280 2145 -> 2421,
@@ -801,8 +801,11 @@ static bool pair_ok(Arith a, const CoreDesc &d, const IODesc &io)
         const int R = d.st[s].R;
         if (R == 16 || R == 13 || (d.L / R) % 2) return false;
     }
-    const long long oal = io.lay == LAY_R2HC ? 8 : 16;
-    if (io.lay == LAY_R2HC ? io.os != 4 || !d.rtw : io.os != 8) return false;
+    // (r2c: half-spectrum units, 8-byte stores)
+    const long long oal = io.lay == LAY_C2C ? 16 : 8;
+    if (io.lay == LAY_R2HC && (io.os != 4 || !d.rtw)) return false;
+    if (io.lay == LAY_R2C && (io.os != 8 || !d.rtw || io.cnt_out != d.M + 1)) return false;
+    if (io.lay == LAY_C2C && io.os != 8) return false;
     if ((uintptr_t)io.out % oal) return false;
     for (int k = 0; k < 3; ++k)
         if (io.bn[k] > 1 && io.bso[k] % oal) return false;

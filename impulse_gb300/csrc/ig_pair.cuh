@@ -245,11 +245,55 @@ __device__ __forceinline__ void pair_split(const float4 *z, char *obase, const f
     }
 }
 
+// The same split to the half spectrum of r2c: X[k], k = 0..M, as complex
+// units (DC and Nyquist imaginary parts 0), conjugated when cj (a backward
+// r2c); 8-byte stores, since a line of M + 1 units starts 16-byte aligned
+// only every other line.  sc = fct / 2.
+__device__ __forceinline__ void pair_split_c(const float4 *z, char *obase, const float2 *rtw, int M, int tpl, int t,
+                                             float sc, bool cj)
+{
+    const int npair = M / 4 + 1;
+    const f2p half = bcast(sc);
+    const float sg = cj ? -1.0f : 1.0f;
+    float2 *o = reinterpret_cast<float2 *>(obase);
+    for (int c = t; c < npair; c += tpl) {
+        const int k = 2 * c;
+        if (k > M / 2) break;
+        const PV a = pv_ld(z, c);
+        const int gh = (M - k) >> 1;
+        const float4 G1 = z[pgi(k == 0 ? 0 : gh)], G0 = z[pgi(gh - 1)];
+        const PV cb = PV{pk(G1.x, G0.y), pk(-G1.z, -G0.w)};
+        const float4 w4 = __ldg(reinterpret_cast<const float4 *>(rtw + k));
+        const PV w = PV{pk(w4.x, w4.z), pk(w4.y, w4.w)};
+        const PV Ev = a + cb, D = a - cb;
+        const PV Tm = pv_mul(PV{D.i, -D.r}, w);
+        const PV X = Ev + Tm, Y = Ev - Tm;  // X[k], X[k + 1]; conj X[M - k], conj X[M - k - 1]
+        float xr0, xr1, xi0, xi1, yr0, yr1, yi0, yi1;
+        upk(X.r * half, xr0, xr1);
+        upk(X.i * half, xi0, xi1);
+        upk(Y.r * half, yr0, yr1);
+        upk(Y.i * half, yi0, yi1);
+        if (k == 0) {
+            __stcs(o, make_float2(xr0, 0.0f));
+            __stcs(o + 1, make_float2(xr1, sg * xi1));
+            __stcs(o + M, make_float2(yr0, 0.0f));
+            __stcs(o + M - 1, make_float2(yr1, -sg * yi1));
+        } else if (2 * k == M) {
+            __stcs(o + k, make_float2(xr0, sg * xi0));
+        } else {
+            __stcs(o + k, make_float2(xr0, sg * xi0));
+            __stcs(o + k + 1, make_float2(xr1, sg * xi1));
+            __stcs(o + M - k - 1, make_float2(yr1, -sg * yi1));
+            __stcs(o + M - k, make_float2(yr0, -sg * yi0));
+        }
+    }
+}
+
 // register cap: the 16-element pairs fit in 64 registers (a few spilled
 // bytes in the 7/11 class), which allows 32 resident warps per SM
 constexpr int kPairRegs = 64;
 
-constexpr int PK_C2C = 0, PK_R2HC = 1;
+constexpr int PK_C2C = 0, PK_R2HC = 1, PK_R2C = 2;
 
 #define IG_PAIR_RADIX_SWITCH(RV, CALL)                                                 \
     switch (RV) {                                                                       \
@@ -334,7 +378,10 @@ __device__ __forceinline__ void pair_rest(const CoreDesc &P, const IODesc &io, f
             IG_PAIR_RADIX_SWITCH(P.st[s].R, (pair_mid<E, R_>(src, dst, tw, L, P.st[s].ns, P.st[s].fns, tpl, t)))
         }
         __syncthreads();
-        if (act) pair_split(dst, obase, rtw, L, tpl, t, 0.5f * io.fct_f);
+        if (act) {
+            if constexpr (K == PK_R2HC) pair_split(dst, obase, rtw, L, tpl, t, 0.5f * io.fct_f);
+            else pair_split_c(dst, obase, rtw, L, tpl, t, 0.5f * io.fct_f, io.conj_out != 0);
+        }
     }
 }
 

@@ -14,11 +14,16 @@ template <int RS, int K> static void pair_go(const CoreDesc &d, const IODesc &io
 cudaError_t launch_pair(const CoreDesc &d, const IODesc &io, int GS, size_t smem, cudaStream_t st)
 {
     const unsigned grid = (unsigned)((io.nlines + io.lpc - 1) / io.lpc), blk = (unsigned)(io.lpc * io.tpl);
-    const bool hc = io.lay == LAY_R2HC;
-    if (d.rs == RS_P2) hc ? pair_go<RS_P2, PK_R2HC>(d, io, GS, grid, blk, smem, st) : pair_go<RS_P2, PK_C2C>(d, io, GS, grid, blk, smem, st);
-    else if (d.rs == RS_P235) hc ? pair_go<RS_P235, PK_R2HC>(d, io, GS, grid, blk, smem, st) : pair_go<RS_P235, PK_C2C>(d, io, GS, grid, blk, smem, st);
-    else if (d.rs == RS_ALL) hc ? pair_go<RS_ALL, PK_R2HC>(d, io, GS, grid, blk, smem, st) : pair_go<RS_ALL, PK_C2C>(d, io, GS, grid, blk, smem, st);
+    const int k = io.lay == LAY_R2HC ? PK_R2HC : io.lay == LAY_R2C ? PK_R2C : PK_C2C;
+#define IG_PG(RS_)                                                                      \
+    (k == PK_R2HC  ? pair_go<RS_, PK_R2HC>(d, io, GS, grid, blk, smem, st)              \
+     : k == PK_R2C ? pair_go<RS_, PK_R2C>(d, io, GS, grid, blk, smem, st)               \
+                   : pair_go<RS_, PK_C2C>(d, io, GS, grid, blk, smem, st))
+    if (d.rs == RS_P2) IG_PG(RS_P2);
+    else if (d.rs == RS_P235) IG_PG(RS_P235);
+    else if (d.rs == RS_ALL) IG_PG(RS_ALL);
     else return cudaErrorNotSupported;
+#undef IG_PG
     return cudaGetLastError();
 }
 
@@ -35,7 +40,8 @@ cudaError_t set_smem_pair(int bytes)
     cudaError_t e = cudaSuccess;
 #define IG_PA(RS_)                                                                     \
     if (e == cudaSuccess) e = pair_attr(k_fft_pair<RS_, PK_C2C>, bytes);               \
-    if (e == cudaSuccess) e = pair_attr(k_fft_pair<RS_, PK_R2HC>, bytes);
+    if (e == cudaSuccess) e = pair_attr(k_fft_pair<RS_, PK_R2HC>, bytes);              \
+    if (e == cudaSuccess) e = pair_attr(k_fft_pair<RS_, PK_R2C>, bytes);
     IG_PA(RS_P2)
     IG_PA(RS_P235)
     IG_PA(RS_ALL)

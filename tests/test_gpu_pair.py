@@ -66,9 +66,10 @@ def test_pair_complex(engine, oracle_lib, n, fwd, out_off):
                                         ((4, 5, 2048), [2]), ((64, 512), [0, 1]), ((2, 40, 256), [1, 2])])
 @pytest.mark.parametrize("fwd", [True, False])
 def test_r2c_half_spectrum_f32(engine, oracle_lib, shape, axes, fwd):
-    """pocketfft::r2c FP32 with an even contiguous last axis: the line kernel's
-    half-spectrum split (DC and Nyquist imaginary parts 0, conjugated for a
-    backward transform)."""
+    """pocketfft::r2c FP32 with an even contiguous last axis: the half-spectrum
+    split of the paired-lane kernel (last axes of 1024+ points) or of the line
+    kernel (shorter ones); DC and Nyquist imaginary parts 0, conjugated for a
+    backward transform."""
     from impulse_gb300 import fft as F
     rng = np.random.default_rng(sum(shape) + fwd)
     x = rng.standard_normal(shape).astype(np.float32)
