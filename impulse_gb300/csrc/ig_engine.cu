@@ -402,6 +402,15 @@ static void finish_layout(Core &c, long long L, long long M, const TuneCfg &cfg 
         full |= c.d.st[s].R == 13;
     }
     c.d.rs = full ? RS_FULL : odd711 ? RS_ALL : odd35 ? (c.d.E == 8 ? RS_P235 : RS_ALL) : RS_P2;
+    // Rader in one CTA without radix 13, double-float 8-element cores: the
+    // 7/11 class with the Rader steps, at 80 registers instead of the full
+    // class's 96 (three CTAs per SM instead of two; IG_NO_RADER_ALL=1: full)
+    static const bool rader_all = getenv("IG_NO_RADER_ALL") == nullptr;
+    if (c.d.blue == 2 && rader_all && c.a == A_DF && c.d.E == 8) {
+        bool r13 = false;
+        for (int s = 0; s < c.d.nst; ++s) r13 |= c.d.st[s].R == 13;
+        if (!r13) c.d.rs = RS_ALLR;
+    }
     // double-float 8-element kernels: the 2/3/5 variant fits the register cap
     // without spills where the power-of-two one does not
     if (c.a == A_DF && c.d.E == 8 && c.d.rs == RS_P2) c.d.rs = RS_P235;

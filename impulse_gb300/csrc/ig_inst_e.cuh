@@ -41,7 +41,11 @@ cudaError_t launch_fft_E(const CoreDesc &d, const IODesc &io, size_t smem, cudaS
         else if (d.rs == RS_P2) launch_rs<T, E, DB, RS_P2>(d, io, grid, blk, smem, st);
         else if (E == 8 && d.rs == RS_P235) launch_rs<T, E, DB, (E == 8 ? RS_P235 : RS_ALL)>(d, io, grid, blk, smem, st);
         else if (d.rs == RS_ALL) launch_rs<T, E, DB, RS_ALL>(d, io, grid, blk, smem, st);
-        else launch_rs<T, E, DB, RS_FULL>(d, io, grid, blk, smem, st);
+        else if constexpr (std::is_same<T, df>::value && E == 8 && DB) {
+            if (d.rs == RS_ALLR) launch_rs<T, E, DB, RS_ALLR>(d, io, grid, blk, smem, st);
+            else launch_rs<T, E, DB, RS_FULL>(d, io, grid, blk, smem, st);
+        } else
+            launch_rs<T, E, DB, RS_FULL>(d, io, grid, blk, smem, st);
     }
     return cudaGetLastError();
 }
@@ -106,6 +110,7 @@ template <class T, int E, bool DB> cudaError_t set_smem_E(int bytes)
         IG_S(RS_ALL)
         IG_S(RS_FULL)
         if constexpr (E == 8) { IG_S(RS_P235) }
+        if constexpr (std::is_same<T, df>::value && E == 8 && DB) { IG_S(RS_ALLR) }
 #undef IG_S
         if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_FULL, LAY_C2C, DB>, bytes);
         if (e == cudaSuccess) e = set_smem_attr(k_fft_worklist<T, E, RS_FULL, LAY_TW, DB>, bytes);

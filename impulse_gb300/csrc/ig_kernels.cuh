@@ -730,7 +730,7 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
         const cx<T> *ch = reinterpret_cast<const cx<T> *>(P.chirp);
         const cx<T> *chf = reinterpret_cast<const cx<T> *>(P.chirpf);
         const int L = P.L;
-        constexpr bool kRader = RS == RS_FULL;  // Rader steps compiled in the full class only
+        constexpr bool kRader = RS == RS_FULL || RS == RS_ALLR;  // Rader steps: these two classes only
         const bool blue = P.blue == 1, rader = kRader && P.blue == 2;
         const bool rowconv = RC && io.rowconv;
         const int npass = (P.blue || rowconv) ? 2 : 1;
@@ -1132,11 +1132,11 @@ __device__ __forceinline__ void fft_block(const CoreDesc &P, const IODesc &io, l
 // registers, which lets three 256-thread CTAs share an SM
 template <class T, int E, int RS, bool DB> constexpr int fft_smem_regs()
 {
-    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS >= RS_FULL ? 96 : 80;
+    if constexpr (DB && E == 8 && std::is_same<T, df>::value) return RS == RS_FULL ? 96 : 80;
     if constexpr (DB && E == 8 && std::is_same<T, float>::value) return 80;
     // FP32 16-element double-buffered lines (4097-8192 points) fit 64 registers
     // without spills below the full class: two 512-thread CTAs per SM
-    if constexpr (DB && E == 16 && std::is_same<T, float>::value) return RS >= RS_FULL ? 128 : 64;
+    if constexpr (DB && E == 16 && std::is_same<T, float>::value) return RS == RS_FULL ? 128 : 64;
     return 128;
 }
 

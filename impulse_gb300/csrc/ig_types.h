@@ -43,6 +43,7 @@ constexpr int RS_P2 = 0;   // 2, 4, 8, 16
 constexpr int RS_P235 = 1; // 2, 4, 8, 16, 3, 5, 9
 constexpr int RS_ALL = 2;  // 2, 3, 4, 5, 7, 8, 9, 11, 16
 constexpr int RS_FULL = 3; // all of RS_ALL, 13, and the Rader steps (also the generic-layout kernels)
+constexpr int RS_ALLR = 4; // the radices of RS_ALL and the Rader steps (double-float 8-element cores only)
 
 // last radices of k_fft_line's halfcomplex variant: the two mirror
 // butterflies of a pair slot stay in registers, so larger radices would spill
