@@ -78,3 +78,32 @@ def test_rowconv_matches_four_passes(engine):
         a = np.asarray(outs[0][n][0]) + 1j * np.asarray(outs[0][n][1])
         b = np.asarray(outs[1][n][0]) + 1j * np.asarray(outs[1][n][1])
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-13, n
+
+
+@pytest.mark.parametrize("shape,axes,dtype", [((8191, 3), [0], np.complex128), ((3, 8191), [1], np.complex128),
+                                              ((10007, 2), [0], np.complex64), ((2, 65521), [1], np.complex64),
+                                              ((65521, 2), [0], np.complex128)])
+def test_rowconv_nd_axes(engine, oracle_lib, shape, axes, dtype):
+    """The row-convolution plans through the N-d interface: prime axes along
+    the strided and the contiguous dimension, both directions."""
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(sum(shape))
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(dtype)
+    for fwd in (True, False):
+        got = F.c2c(x, axes, forward=fwd, fct=0.5)
+        want = oracle_lib.c2c(x.astype(np.complex128), axes, forward=fwd, fct=0.5)
+        assert oracle_lib.rel_l2(got, want) < tol(dtype, max(shape)), (shape, axes, fwd)
+
+
+@pytest.mark.parametrize("shape,dtype", [((4, 8191), np.float64), ((3, 65521), np.float32), ((2, 2 * 10007), np.float64)])
+def test_rowconv_r2c_c2r(engine, oracle_lib, shape, dtype):
+    """r2c / c2r with a prime (or twice a prime) last axis: the half spectrum
+    through Rader / Bluestein over multi-pass cores, and back."""
+    from impulse_gb300 import fft as F
+    rng = np.random.default_rng(shape[-1])
+    x = rng.standard_normal(shape).astype(dtype)
+    spec = F.r2c(x, [1], forward=True)
+    want = oracle_lib.r2c(x.astype(np.float64), [1], forward=True)
+    assert oracle_lib.rel_l2(spec, want) < tol(dtype, shape[-1])
+    back = F.c2r(spec, shape, [1], forward=False, fct=1.0 / shape[-1])
+    assert oracle_lib.rel_l2(back, x.astype(np.float64)) < 2 * tol(dtype, shape[-1])
